@@ -1,0 +1,151 @@
+/*
+ * tfq_gb300: C ABI of the GB300 (sm_103a) implementation of TensorFlow
+ * Quantum's state-vector ops.
+ *
+ * Each entry point replaces the Compute() of one reference TF op kernel;
+ * inputs keep the reference's meaning:
+ *   programs       serialized tfq.proto.Program, one per batch row
+ *   symbol_names   symbol names, one per column of symbol_values
+ *   symbol_values  float32 [batch, num_symbols], row-major
+ *   pauli_sums     serialized tfq.proto.PauliSum, [batch, num_ops] row-major
+ * Strings are passed as arrays of (pointer, length); nothing is retained
+ * after a call returns except inside a tfqg_batch handle.
+ *
+ * Errors: every function returns a tensorflow::error::Code value
+ * (0 = OK, 3 = INVALID_ARGUMENT, 8 = RESOURCE_EXHAUSTED, 12 = UNIMPLEMENTED,
+ * 13 = INTERNAL).  tfqg_last_error() returns the message of the last failed
+ * call on the calling thread; the texts of INVALID_ARGUMENT errors are the
+ * reference's.
+ *
+ * Buffers: functions taking `device_buffers` read inputs and write outputs
+ * through device pointers when it is nonzero (asynchronously on `stream`),
+ * else through host pointers (the call copies and synchronizes).  `stream`
+ * is a cudaStream_t or NULL for the legacy default stream.
+ */
+#ifndef TFQ_GB300_H_
+#define TFQ_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TFQG_OK 0
+#define TFQG_INVALID_ARGUMENT 3
+#define TFQG_RESOURCE_EXHAUSTED 8
+#define TFQG_UNIMPLEMENTED 12
+#define TFQG_INTERNAL 13
+
+/* Batch kinds (what the batch will be run for). */
+#define TFQG_KIND_FORWARD 0 /* expectation / state / samples */
+#define TFQG_KIND_ADJOINT 1 /* adjoint gradient (and forward) */
+#define TFQG_KIND_NOISY 2   /* noisy trajectories (channels allowed) */
+
+/* Derivative rule of the adjoint gradient. */
+#define TFQG_GRAD_REFERENCE_FD 0 /* (G(x+5e-3)-G(x-5e-3))/1e-2, adj_util.cc:32 */
+#define TFQG_GRAD_EXACT 1        /* exact dG/dx */
+
+const char* tfqg_last_error(void);
+const char* tfqg_version(void);
+
+/* ---------------------------------------------------------------------
+ * Compiled batch: parse + qubit/symbol resolution + pass planning once,
+ * run many times with new symbol values.  Creation touches no GPU.
+ * ------------------------------------------------------------------- */
+typedef struct tfqg_batch tfqg_batch;
+
+/* Parses programs and pauli_sums (pauli_sums may be NULL with num_ops = 0)
+ * and resolves symbols.  Mirrors the parse/validation part of
+ *   TfqSimulateExpectationOp::Compute  tfq_simulate_expectation_op.cc:50-114
+ *   TfqAdjointGradientOp::Compute      tfq_adj_grad_op.cc:51-129
+ *   TfqNoisyExpectationOp::Compute     noise/tfq_noisy_expectation.cc:62-135
+ * (GetProgramsAndNumQubits parse_context.cc:268-320, GetSymbolMaps :405-461,
+ * QsimCircuitFromProgram circuit_parser_qsim.cc:828-861). */
+int tfqg_batch_create(const char* const* programs, const int64_t* program_lens,
+                      int64_t batch, const char* const* symbol_names,
+                      const int64_t* symbol_name_lens, int64_t num_symbols,
+                      const char* const* pauli_sums,
+                      const int64_t* pauli_sum_lens, int64_t num_ops, int kind,
+                      tfqg_batch** out);
+
+/* Largest qubit count in the batch (output width of state / samples). */
+int tfqg_batch_max_num_qubits(const tfqg_batch* b, int32_t* out);
+void tfqg_batch_destroy(tfqg_batch* b);
+
+/* Expectations [batch, num_ops]; -2 for empty programs.
+ * Replaces TfqSimulateExpectationOp::ComputeSmall/Large
+ * (tfq_simulate_expectation_op.cc:130-250). */
+int tfqg_batch_expectation(tfqg_batch* b, const float* symbol_values,
+                           float* expectations, int device_buffers,
+                           void* stream);
+
+/* States complex64 [batch, 2^max_num_qubits] (interleaved float re, im),
+ * padded with -2.  Replaces TfqSimulateStateOp (tfq_simulate_state_op.cc:
+ * 120-215). */
+int tfqg_batch_state(tfqg_batch* b, const float* symbol_values, void* states,
+                     int device_buffers, void* stream);
+
+/* Samples int8 [batch, num_samples, max_num_qubits]; padding -2 in the
+ * leading columns.  Replaces TfqSimulateSamplesOp
+ * (tfq_simulate_samples_op.cc:132-251).  num_samples must be >= 0. */
+int tfqg_batch_samples(tfqg_batch* b, const float* symbol_values,
+                       int32_t num_samples, uint64_t seed, int8_t* samples,
+                       int device_buffers, void* stream);
+
+/* Adjoint gradient [batch, num_symbols] of sum_j downstream_grads[i, j] *
+ * <pauli_sums[i, j]>.  Replaces TfqAdjointGradientOp::ComputeSmall/Large
+ * (tfq_adj_grad_op.cc:173-390).  The batch must be TFQG_KIND_ADJOINT. */
+int tfqg_batch_adj_grad(tfqg_batch* b, const float* symbol_values,
+                        const float* downstream_grads, int grad_rule,
+                        float* grads, int device_buffers, void* stream);
+
+/* Monte-Carlo trajectory expectations [batch, num_ops]; num_samples int32
+ * [batch, num_ops] trajectories per entry (each >= 1).  Replaces
+ * TfqNoisyExpectationOp::ComputeSmall/Large (noise/tfq_noisy_expectation.cc:
+ * 161-391).  The batch must be TFQG_KIND_NOISY. */
+int tfqg_batch_noisy_expectation(tfqg_batch* b, const float* symbol_values,
+                                 const int32_t* num_samples, uint64_t seed,
+                                 float* expectations, int device_buffers,
+                                 void* stream);
+
+/* ---------------------------------------------------------------------
+ * One-shot entry points with the reference op signatures and HOST buffers
+ * (what a TF CPU-side OpKernel::Compute holds).  They create a transient
+ * batch, run it and destroy it.
+ * ------------------------------------------------------------------- */
+/* tfq_simulate_expectation (tfq_simulate_ops.py:22-45) */
+int tfqg_simulate_expectation(const char* const* programs,
+                              const int64_t* program_lens, int64_t batch,
+                              const char* const* symbol_names,
+                              const int64_t* symbol_name_lens,
+                              int64_t num_symbols, const float* symbol_values,
+                              const char* const* pauli_sums,
+                              const int64_t* pauli_sum_lens, int64_t num_ops,
+                              float* expectations);
+
+/* tfq_adj_grad (tfq_adj_grad_op.py:22-48) */
+int tfqg_adj_grad(const char* const* programs, const int64_t* program_lens,
+                  int64_t batch, const char* const* symbol_names,
+                  const int64_t* symbol_name_lens, int64_t num_symbols,
+                  const float* symbol_values, const char* const* pauli_sums,
+                  const int64_t* pauli_sum_lens, int64_t num_ops,
+                  const float* downstream_grads, float* grads);
+
+/* tfq.noise.expectation (noise/noisy_expectation_op.py:23-98) */
+int tfqg_noisy_expectation(const char* const* programs,
+                           const int64_t* program_lens, int64_t batch,
+                           const char* const* symbol_names,
+                           const int64_t* symbol_name_lens,
+                           int64_t num_symbols, const float* symbol_values,
+                           const char* const* pauli_sums,
+                           const int64_t* pauli_sum_lens, int64_t num_ops,
+                           const int32_t* num_samples, uint64_t seed,
+                           float* expectations);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TFQ_GB300_H_ */

@@ -1,0 +1,118 @@
+"""ctypes binding of the C ABI in include/tfq_gb300.h.
+
+The library is the in-tree build product quantum_gb300/_lib/libtfq_gb300.so
+(`python -m quantum_gb300.build`).  There is no fallback: if the library is
+missing every op raises.
+"""
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+c_char_pp = ctypes.POINTER(ctypes.c_char_p)
+c_int64_p = ctypes.POINTER(ctypes.c_int64)
+c_void_p = ctypes.c_void_p
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+class InvalidArgumentError(ValueError):
+    """tensorflow.errors.InvalidArgumentError counterpart."""
+
+
+class ResourceExhaustedError(MemoryError):
+    """tensorflow.errors.ResourceExhaustedError counterpart."""
+
+
+class UnimplementedError(NotImplementedError):
+    pass
+
+
+class InternalError(RuntimeError):
+    pass
+
+
+_ERRORS = {3: InvalidArgumentError, 8: ResourceExhaustedError,
+           12: UnimplementedError, 13: InternalError}
+
+EXPORTED = (
+    "tfqg_last_error", "tfqg_version", "tfqg_batch_create",
+    "tfqg_batch_max_num_qubits", "tfqg_batch_destroy",
+    "tfqg_batch_expectation", "tfqg_batch_state", "tfqg_batch_samples",
+    "tfqg_batch_adj_grad", "tfqg_batch_noisy_expectation",
+    "tfqg_simulate_expectation", "tfqg_adj_grad", "tfqg_noisy_expectation",
+)
+
+
+def _declare(lib):
+    lib.tfqg_last_error.restype = ctypes.c_char_p
+    lib.tfqg_version.restype = ctypes.c_char_p
+    lib.tfqg_batch_create.argtypes = [
+        c_char_pp, c_int64_p, ctypes.c_int64, c_char_pp, c_int64_p,
+        ctypes.c_int64, c_char_pp, c_int64_p, ctypes.c_int64, ctypes.c_int,
+        ctypes.POINTER(c_void_p)]
+    lib.tfqg_batch_max_num_qubits.argtypes = [c_void_p,
+                                              ctypes.POINTER(ctypes.c_int32)]
+    lib.tfqg_batch_destroy.argtypes = [c_void_p]
+    lib.tfqg_batch_destroy.restype = None
+    lib.tfqg_batch_expectation.argtypes = [c_void_p, c_void_p, c_void_p,
+                                           ctypes.c_int, c_void_p]
+    lib.tfqg_batch_state.argtypes = [c_void_p, c_void_p, c_void_p,
+                                     ctypes.c_int, c_void_p]
+    lib.tfqg_batch_samples.argtypes = [c_void_p, c_void_p, ctypes.c_int32,
+                                       ctypes.c_uint64, c_void_p, ctypes.c_int,
+                                       c_void_p]
+    lib.tfqg_batch_adj_grad.argtypes = [c_void_p, c_void_p, c_void_p,
+                                        ctypes.c_int, c_void_p, ctypes.c_int,
+                                        c_void_p]
+    lib.tfqg_batch_noisy_expectation.argtypes = [
+        c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p, ctypes.c_int,
+        c_void_p]
+    for name in ("tfqg_batch_create", "tfqg_batch_max_num_qubits",
+                 "tfqg_batch_expectation", "tfqg_batch_state",
+                 "tfqg_batch_samples", "tfqg_batch_adj_grad",
+                 "tfqg_batch_noisy_expectation", "tfqg_simulate_expectation",
+                 "tfqg_adj_grad", "tfqg_noisy_expectation"):
+        getattr(lib, name).restype = ctypes.c_int
+
+
+def lib():
+    """Load (once) and return the native library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            path = _build.lib_path()
+            if not os.path.exists(path):
+                raise NativeLibraryMissing(
+                    f"{path} is missing; build it with "
+                    "`python -m quantum_gb300.build`")
+            handle = ctypes.CDLL(path)
+            _declare(handle)
+            _lib = handle
+    return _lib
+
+
+def check(rc):
+    if rc != 0:
+        msg = lib().tfqg_last_error().decode("utf-8", "replace")
+        raise _ERRORS.get(rc, InternalError)(msg)
+
+
+def string_array(items):
+    """(char**, int64*, keepalive) for a sequence of bytes/str."""
+    bs = [x if isinstance(x, (bytes, bytearray)) else str(x).encode("utf-8")
+          for x in items]
+    bs = [bytes(x) for x in bs]
+    n = len(bs)
+    ptrs = (ctypes.c_char_p * max(n, 1))(*bs) if n else (ctypes.c_char_p * 1)()
+    lens = (ctypes.c_int64 * max(n, 1))(*[len(x) for x in bs])
+    return ctypes.cast(ptrs, c_char_pp), ctypes.cast(lens, c_int64_p), (bs, ptrs, lens)

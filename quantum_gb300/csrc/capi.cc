@@ -1,0 +1,681 @@
+// C ABI (include/tfq_gb300.h): batch compilation on the host, device upload,
+// kernel launches.  See the header for the reference functions each entry
+// point replaces.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/tfq_gb300.h"
+#include "host.h"
+#include "kernels.h"
+
+using namespace tfqg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define TFQG_CUDA(call)                                                    \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess)                                                 \
+      throw Error(kInternal, std::string("CUDA error: ") +                 \
+                                 cudaGetErrorString(e_) + " at " #call);   \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int device = -1;
+  void reserve(size_t need, int dev) {
+    if (need <= bytes && dev == device) return;
+    release();
+    size_t sz = std::max<size_t>(need, 256);
+    TFQG_CUDA(cudaMalloc(&p, sz));
+    bytes = sz;
+    device = dev;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  ~DevBuf() { release(); }
+};
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+struct tfqg_batch {
+  int kind = 0;
+  int64_t B = 0, P = 0, n_ops = 0;
+  int max_n = 0;
+  int max_resident_n = -1;   // largest resident row (-1: none)
+  bool any_streamed = false;
+  int max_streamed_n = 0;
+  int max_grads = 0;
+  int64_t total_gates = 0, total_grads = 0;
+
+  // packed host copies of the device tables
+  std::vector<DevProgram> programs;
+  std::vector<DevRow> rows;
+  std::vector<GateTemplate> gates;
+  std::vector<DevPass> passes;
+  std::vector<DevOp> ops;
+  std::vector<DevTerm> terms;
+  std::vector<DevChannel> channels;
+  std::vector<float2> kraus;
+  std::vector<int32_t> grad_cols;
+  std::vector<int32_t> order;
+
+  // device state
+  std::mutex mu;
+  int device = -1;
+  DevBuf tables, mats, dmats, work, counter, values, out, aux, aux2;
+  BatchDevice bd;
+};
+
+namespace {
+
+struct Str {
+  const char* p;
+  int64_t n;
+};
+
+std::string make_key(const char* p, int64_t n) { return std::string(p, size_t(n)); }
+
+// Parses/compiles every row.  Throws Error on invalid input.
+void build_batch(tfqg_batch* b, const char* const* programs,
+                 const int64_t* program_lens, int64_t batch,
+                 const char* const* symbol_names, const int64_t* name_lens,
+                 int64_t num_symbols, const char* const* pauli_sums,
+                 const int64_t* psum_lens, int64_t num_ops, int kind) {
+  if (batch < 0 || num_symbols < 0 || num_ops < 0)
+    throw Error(kInvalidArgument, "negative dimension");
+  if (num_ops > 65535)
+    throw Error(kInvalidArgument, "at most 65535 pauli_sums columns are supported");
+  b->kind = kind;
+  b->B = batch;
+  b->P = num_symbols;
+  b->n_ops = num_ops;
+  const JobKind job = kind == TFQG_KIND_ADJOINT ? kJobAdjoint
+                      : kind == TFQG_KIND_NOISY ? kJobNoisy
+                                                : kJobForward;
+
+  // 1. parse programs (ParsePrograms, parse_context.cc:174-206), deduplicated
+  std::unordered_map<std::string, int> prog_ids;
+  std::vector<ProgramP> parsed;
+  std::vector<int> row_prog(static_cast<size_t>(batch));
+  for (int64_t i = 0; i < batch; ++i) {
+    std::string key = make_key(programs[i], program_lens[i]);
+    auto it = prog_ids.find(key);
+    if (it != prog_ids.end()) {
+      row_prog[i] = it->second;
+      continue;
+    }
+    ProgramP p;
+    decode_program(programs[i], size_t(program_lens[i]), &p);
+    int id = int(parsed.size());
+    parsed.push_back(std::move(p));
+    prog_ids.emplace(std::move(key), id);
+    row_prog[i] = id;
+  }
+  // 2. parse pauli sums (GetPauliSums, parse_context.cc:367-403)
+  std::unordered_map<std::string, int> psum_ids;
+  std::vector<PauliSumP> psums;
+  std::vector<int> row_psum(static_cast<size_t>(batch * num_ops));
+  for (int64_t k = 0; k < batch * num_ops; ++k) {
+    std::string key = make_key(pauli_sums[k], psum_lens[k]);
+    auto it = psum_ids.find(key);
+    if (it != psum_ids.end()) {
+      row_psum[k] = it->second;
+      continue;
+    }
+    PauliSumP ps;
+    decode_paulisum(pauli_sums[k], size_t(psum_lens[k]), &ps);
+    int id = int(psums.size());
+    psums.push_back(std::move(ps));
+    psum_ids.emplace(std::move(key), id);
+    row_psum[k] = id;
+  }
+  // 3. symbol map (GetSymbolMaps): name -> column, last column wins
+  SymbolTable names;
+  names.num_symbols = num_symbols;
+  for (int64_t j = 0; j < num_symbols; ++j)
+    names.col[make_key(symbol_names[j], name_lens[j])] = int(j);
+
+  // 4. resolve + compile each distinct program; check pauli-sum qubits
+  std::vector<CompiledProgram> compiled(parsed.size());
+  std::vector<std::unordered_map<std::string, int>> index(parsed.size());
+  std::vector<char> resolved(parsed.size(), 0);
+  // qubit resolution errors surface per row in batch order, before
+  // circuit-construction errors, like GetProgramsAndNumQubits
+  for (int64_t i = 0; i < batch; ++i) {
+    int pid = row_prog[i];
+    if (!resolved[pid]) {
+      resolve_qubits(parsed[pid], &index[pid]);
+      resolved[pid] = 1;
+    }
+    if (parsed[pid].moments.empty()) continue;  // (#679) empty program
+    for (int64_t j = 0; j < num_ops; ++j) {
+      const PauliSumP& ps = psums[row_psum[i * num_ops + j]];
+      for (const TermP& t : ps)
+        for (const auto& pq : t.paulis)
+          if (!index[pid].count(pq.first))
+            throw Error(kInvalidArgument,
+                        "Found a Pauli sum operating on qubits not found in "
+                        "circuit.");
+    }
+  }
+  for (size_t pid = 0; pid < parsed.size(); ++pid) {
+    compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
+    plan_program(&compiled[pid], job);
+  }
+
+  // 5. pack programs
+  b->programs.resize(compiled.size());
+  for (size_t pid = 0; pid < compiled.size(); ++pid) {
+    const CompiledProgram& cp = compiled[pid];
+    DevProgram& dp = b->programs[pid];
+    memset(&dp, 0, sizeof(dp));
+    dp.n = cp.empty() ? 0 : cp.n;
+    dp.num_gates = int32_t(cp.gates.size());
+    dp.num_grads = int32_t(cp.grad_col.size());
+    dp.grad_col_begin = uint32_t(b->grad_cols.size());
+    b->grad_cols.insert(b->grad_cols.end(), cp.grad_col.begin(), cp.grad_col.end());
+    dp.gate_begin = uint32_t(b->gates.size());
+    b->gates.insert(b->gates.end(), cp.gates.begin(), cp.gates.end());
+    dp.channel_begin = uint32_t(b->channels.size());
+    dp.num_channels = int32_t(cp.channels.size());
+    for (const ChannelHost& ch : cp.channels) {
+      DevChannel d = ch.dev;
+      d.kraus = uint32_t(b->kraus.size() / 4);
+      for (size_t k = 0; k < ch.kraus.size(); k += 2)
+        b->kraus.push_back(make_float2(float(ch.kraus[k]), float(ch.kraus[k + 1])));
+      b->channels.push_back(d);
+    }
+    dp.resident = cp.resident ? 1 : 0;
+    const uint32_t op_base = uint32_t(b->ops.size());
+    dp.fwd_pass_begin = uint32_t(b->passes.size());
+    for (DevPass ps : cp.fwd_passes) {
+      ps.op_begin += op_base;
+      ps.op_end += op_base;
+      b->passes.push_back(ps);
+    }
+    dp.fwd_pass_end = uint32_t(b->passes.size());
+    b->ops.insert(b->ops.end(), cp.fwd_ops.begin(), cp.fwd_ops.end());
+    const uint32_t bop_base = uint32_t(b->ops.size());
+    dp.bwd_pass_begin = uint32_t(b->passes.size());
+    for (DevPass ps : cp.bwd_passes) {
+      ps.op_begin += bop_base;
+      ps.op_end += bop_base;
+      b->passes.push_back(ps);
+    }
+    dp.bwd_pass_end = uint32_t(b->passes.size());
+    b->ops.insert(b->ops.end(), cp.bwd_ops.begin(), cp.bwd_ops.end());
+    if (dp.n > 0) {
+      b->max_n = std::max(b->max_n, dp.n);
+      if (cp.resident) b->max_resident_n = std::max(b->max_resident_n, dp.n);
+      else {
+        b->any_streamed = true;
+        b->max_streamed_n = std::max(b->max_streamed_n, dp.n);
+      }
+      b->max_grads = std::max(b->max_grads, dp.num_grads);
+    } else {
+      // the reference sizes outputs by the resolved qubit count even for
+      // programs that hold no gates
+      b->max_n = std::max(b->max_n, cp.n);
+    }
+  }
+
+  // 6. rows: matrices, terms (deduplicated per distinct pauli-sum row)
+  b->rows.resize(size_t(batch));
+  std::unordered_map<std::string, std::pair<uint32_t, uint32_t>> term_rows;
+  int64_t mat = 0, dmat = 0;
+  for (int64_t i = 0; i < batch; ++i) {
+    DevRow& r = b->rows[i];
+    memset(&r, 0, sizeof(r));
+    const int pid = row_prog[i];
+    r.program = pid;
+    r.n = b->programs[pid].n;
+    r.mat_offset = uint64_t(mat);
+    r.dmat_offset = uint64_t(dmat);
+    mat += b->programs[pid].num_gates;
+    dmat += b->programs[pid].num_grads;
+    if (r.n == 0 || num_ops == 0) {
+      r.term_begin = r.term_end = uint32_t(b->terms.size());
+      continue;
+    }
+    std::string key = std::to_string(pid) + ":";
+    for (int64_t j = 0; j < num_ops; ++j)
+      key += std::to_string(row_psum[i * num_ops + j]) + ",";
+    auto it = term_rows.find(key);
+    if (it != term_rows.end()) {
+      r.term_begin = it->second.first;
+      r.term_end = it->second.second;
+      continue;
+    }
+    r.term_begin = uint32_t(b->terms.size());
+    for (int64_t j = 0; j < num_ops; ++j)
+      lower_paulisum(psums[row_psum[i * num_ops + j]], index[pid], r.n, int(j),
+                     &b->terms);
+    r.term_end = uint32_t(b->terms.size());
+    term_rows.emplace(key, std::make_pair(r.term_begin, r.term_end));
+  }
+  b->total_gates = mat;
+  b->total_grads = dmat;
+  // most expensive rows first (approximate longest-processing-time order)
+  b->order.resize(size_t(batch));
+  for (int64_t i = 0; i < batch; ++i) b->order[i] = int32_t(i);
+  auto cost = [&](int32_t i) {
+    const DevProgram& p = b->programs[b->rows[i].program];
+    return double(p.num_gates + 1) * double(int64_t(1) << std::min(p.n, 40));
+  };
+  std::stable_sort(b->order.begin(), b->order.end(),
+                   [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
+  if (b->max_grads > 8192)
+    throw Error(kResourceExhausted,
+                "A circuit has more than 8192 symbolic gate parameters; the "
+                "adjoint kernel keeps one accumulator per parameter in shared "
+                "memory.");
+}
+
+template <class T>
+size_t put(std::vector<unsigned char>* blob, const std::vector<T>& v) {
+  size_t off = align256(blob->size());
+  blob->resize(off + std::max<size_t>(v.size() * sizeof(T), 1));
+  if (!v.empty()) memcpy(blob->data() + off, v.data(), v.size() * sizeof(T));
+  return off;
+}
+
+void ensure_device(tfqg_batch* b, cudaStream_t s) {
+  int dev;
+  TFQG_CUDA(cudaGetDevice(&dev));
+  if (b->device == dev && b->tables.p) return;
+  std::vector<unsigned char> blob;
+  size_t o_prog = put(&blob, b->programs), o_rows = put(&blob, b->rows),
+         o_gates = put(&blob, b->gates), o_pass = put(&blob, b->passes),
+         o_ops = put(&blob, b->ops), o_terms = put(&blob, b->terms),
+         o_chan = put(&blob, b->channels), o_kraus = put(&blob, b->kraus),
+         o_gc = put(&blob, b->grad_cols), o_order = put(&blob, b->order);
+  b->tables.reserve(blob.size(), dev);
+  TFQG_CUDA(cudaMemcpyAsync(b->tables.p, blob.data(), blob.size(),
+                            cudaMemcpyHostToDevice, s));
+  TFQG_CUDA(cudaStreamSynchronize(s));  // blob is a temporary
+  unsigned char* base = static_cast<unsigned char*>(b->tables.p);
+  BatchDevice& d = b->bd;
+  d.programs = reinterpret_cast<const DevProgram*>(base + o_prog);
+  d.rows = reinterpret_cast<const DevRow*>(base + o_rows);
+  d.gates = reinterpret_cast<const GateTemplate*>(base + o_gates);
+  d.passes = reinterpret_cast<const DevPass*>(base + o_pass);
+  d.ops = reinterpret_cast<const DevOp*>(base + o_ops);
+  d.terms = reinterpret_cast<const DevTerm*>(base + o_terms);
+  d.channels = reinterpret_cast<const DevChannel*>(base + o_chan);
+  d.kraus = reinterpret_cast<const float2*>(base + o_kraus);
+  d.grad_cols = reinterpret_cast<const int32_t*>(base + o_gc);
+  d.order = reinterpret_cast<const int32_t*>(base + o_order);
+  d.num_rows = int32_t(b->B);
+  d.num_ops = int32_t(b->n_ops);
+  d.num_symbols = int32_t(b->P);
+  d.max_n = b->max_n;
+  d.total_gates = b->total_gates;
+  d.total_grads = b->total_grads;
+  b->device = dev;
+}
+
+// Common preamble: device tables, symbol values on the device, matrices.
+const float* prepare(tfqg_batch* b, const float* values, int device_buffers,
+                     bool grads, int grad_rule, cudaStream_t s, RunArgs* a) {
+  ensure_device(b, s);
+  const float* dvals = values;
+  size_t vbytes = size_t(b->B * b->P) * sizeof(float);
+  if (!device_buffers && vbytes) {
+    b->values.reserve(vbytes, b->device);
+    TFQG_CUDA(cudaMemcpyAsync(b->values.p, values, vbytes,
+                              cudaMemcpyHostToDevice, s));
+    dvals = static_cast<const float*>(b->values.p);
+  }
+  a->values = dvals;
+  b->mats.reserve(size_t(b->total_gates) * 16 * sizeof(float2), b->device);
+  a->mats = static_cast<float2*>(b->mats.p);
+  if (grads) {
+    b->dmats.reserve(size_t(b->total_grads) * 16 * sizeof(float2), b->device);
+    a->dmats = static_cast<float2*>(b->dmats.p);
+  }
+  a->grad_rule = grad_rule;
+  b->counter.reserve(sizeof(int), b->device);
+  a->counter = static_cast<int*>(b->counter.p);
+  TFQG_CUDA(launch_build_matrices(b->bd, *a, grads, s));
+  return dvals;
+}
+
+int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
+  const int max_grads = mode == kModeAdjoint ? b->max_grads : 0;
+  size_t smem = sim_smem_bytes(mode, b->max_resident_n, b->any_streamed, max_grads);
+  if (smem > 227 * 1024)
+    throw Error(kResourceExhausted, "shared memory request too large");
+  int grid = sim_grid_size(mode, smem);
+  int64_t units = mode == kModeNoisy ? a->total_traj : b->B;
+  if (units < grid) grid = int(std::max<int64_t>(units, 1));
+  if (b->any_streamed) {
+    int64_t per = int64_t(1) << b->max_streamed_n;
+    if (mode == kModeAdjoint) per *= 2;
+    a->slot_amps = per;
+    b->work.reserve(size_t(per) * grid * sizeof(float2), b->device);
+    a->work = static_cast<float2*>(b->work.p);
+  }
+  TFQG_CUDA(cudaMemsetAsync(a->counter, 0, sizeof(int), s));
+  int state_amps = sim_state_amps(b->max_resident_n, b->any_streamed);
+  TFQG_CUDA(launch_simulate(mode, b->bd, *a, grid, smem, state_amps, s));
+  return grid;
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const Error& e) {
+    return fail(e.code, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(kResourceExhausted, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(kInternal, e.what());
+  }
+}
+
+void finish(tfqg_batch* b, void* host_dst, const void* dev_src, size_t bytes,
+            int device_buffers, cudaStream_t s) {
+  if (!device_buffers && bytes)
+    TFQG_CUDA(cudaMemcpyAsync(host_dst, dev_src, bytes, cudaMemcpyDeviceToHost, s));
+  if (!device_buffers) TFQG_CUDA(cudaStreamSynchronize(s));
+  TFQG_CUDA(cudaGetLastError());
+  (void)b;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tfqg_last_error(void) { return g_last_error.c_str(); }
+const char* tfqg_version(void) { return "tfq_gb300 0.1.0 (sm_103a)"; }
+
+int tfqg_batch_create(const char* const* programs, const int64_t* program_lens,
+                      int64_t batch, const char* const* symbol_names,
+                      const int64_t* symbol_name_lens, int64_t num_symbols,
+                      const char* const* pauli_sums,
+                      const int64_t* pauli_sum_lens, int64_t num_ops, int kind,
+                      tfqg_batch** out) {
+  return guarded([&]() {
+    if (!out) throw Error(kInvalidArgument, "out is NULL");
+    *out = nullptr;
+    if (kind < TFQG_KIND_FORWARD || kind > TFQG_KIND_NOISY)
+      throw Error(kInvalidArgument, "unknown batch kind");
+    std::unique_ptr<tfqg_batch> b(new tfqg_batch());
+    build_batch(b.get(), programs, program_lens, batch, symbol_names,
+                symbol_name_lens, num_symbols, pauli_sums, pauli_sum_lens,
+                pauli_sums ? num_ops : 0, kind);
+    b->n_ops = num_ops;
+    *out = b.release();
+    return 0;
+  });
+}
+
+int tfqg_batch_max_num_qubits(const tfqg_batch* b, int32_t* out) {
+  if (!b || !out) return fail(kInvalidArgument, "NULL argument");
+  *out = b->max_n;
+  return 0;
+}
+
+void tfqg_batch_destroy(tfqg_batch* b) { delete b; }
+
+int tfqg_batch_expectation(tfqg_batch* b, const float* symbol_values,
+                           float* expectations, int device_buffers,
+                           void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    size_t obytes = size_t(b->B * b->n_ops) * sizeof(float);
+    if (b->B == 0 || b->n_ops == 0) return 0;
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, false, 0, s, &a);
+    float* dout = expectations;
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<float*>(b->out.p);
+    }
+    a.out_f = dout;
+    simulate(b, kModeExpect, &a, s);
+    finish(b, expectations, dout, obytes, device_buffers, s);
+    return 0;
+  });
+}
+
+int tfqg_batch_state(tfqg_batch* b, const float* symbol_values, void* states,
+                     int device_buffers, void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    size_t obytes = size_t(b->B) * (size_t(1) << b->max_n) * sizeof(float2);
+    if (b->B == 0) return 0;
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, false, 0, s, &a);
+    float2* dout = static_cast<float2*>(states);
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<float2*>(b->out.p);
+    }
+    a.out_state = dout;
+    simulate(b, kModeState, &a, s);
+    finish(b, states, dout, obytes, device_buffers, s);
+    return 0;
+  });
+}
+
+int tfqg_batch_samples(tfqg_batch* b, const float* symbol_values,
+                       int32_t num_samples, uint64_t seed, int8_t* samples,
+                       int device_buffers, void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    if (num_samples < 0)
+      throw Error(kInvalidArgument, "num_samples must be non-negative.");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    size_t obytes = size_t(b->B) * size_t(num_samples) * size_t(b->max_n);
+    if (obytes == 0) return 0;
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, false, 0, s, &a);
+    int8_t* dout = samples;
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<int8_t*>(b->out.p);
+    }
+    a.out_samples = dout;
+    a.num_samples = num_samples;
+    a.seed = seed;
+    simulate(b, kModeSample, &a, s);
+    finish(b, samples, dout, obytes, device_buffers, s);
+    return 0;
+  });
+}
+
+int tfqg_batch_adj_grad(tfqg_batch* b, const float* symbol_values,
+                        const float* downstream_grads, int grad_rule,
+                        float* grads, int device_buffers, void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    if (b->kind != TFQG_KIND_ADJOINT)
+      throw Error(kInvalidArgument, "batch was not created for the adjoint");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    size_t obytes = size_t(b->B * b->P) * sizeof(float);
+    if (b->B == 0 || b->P == 0) return 0;
+    float* dout = grads;
+    ensure_device(b, s);
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<float*>(b->out.p);
+    }
+    TFQG_CUDA(cudaMemsetAsync(dout, 0, obytes, s));
+    if (b->n_ops == 0) {
+      finish(b, grads, dout, obytes, device_buffers, s);
+      return 0;
+    }
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, true, grad_rule, s, &a);
+    const float* dg = downstream_grads;
+    size_t gbytes = size_t(b->B * b->n_ops) * sizeof(float);
+    if (!device_buffers) {
+      b->aux.reserve(gbytes, b->device);
+      TFQG_CUDA(cudaMemcpyAsync(b->aux.p, downstream_grads, gbytes,
+                                cudaMemcpyHostToDevice, s));
+      dg = static_cast<const float*>(b->aux.p);
+    }
+    a.dgrads = dg;
+    a.out_f = dout;
+    simulate(b, kModeAdjoint, &a, s);
+    finish(b, grads, dout, obytes, device_buffers, s);
+    return 0;
+  });
+}
+
+int tfqg_batch_noisy_expectation(tfqg_batch* b, const float* symbol_values,
+                                 const int32_t* num_samples, uint64_t seed,
+                                 float* expectations, int device_buffers,
+                                 void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    if (b->kind != TFQG_KIND_NOISY)
+      throw Error(kInvalidArgument, "batch was not created for noisy simulation");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t cells = b->B * b->n_ops;
+    size_t obytes = size_t(cells) * sizeof(float);
+    if (cells == 0) return 0;
+    // trajectories per row = max over its ops; the host needs the counts
+    std::vector<int32_t> reps(static_cast<size_t>(cells));
+    if (device_buffers) {
+      TFQG_CUDA(cudaMemcpyAsync(reps.data(), num_samples, cells * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream)));
+      TFQG_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    } else {
+      memcpy(reps.data(), num_samples, cells * sizeof(int32_t));
+    }
+    for (int32_t r : reps)
+      if (r < 1)
+        throw Error(kInvalidArgument,
+                    "Each element of num_samples must be greater than 0.");
+    std::vector<int64_t> prefix(static_cast<size_t>(b->B) + 1, 0);
+    for (int64_t i = 0; i < b->B; ++i) {
+      int32_t m = 0;
+      const DevProgram& p = b->programs[b->rows[i].program];
+      if (p.n > 0 && p.fwd_pass_begin != p.fwd_pass_end)
+        for (int64_t j = 0; j < b->n_ops; ++j) m = std::max(m, reps[i * b->n_ops + j]);
+      prefix[i + 1] = prefix[i] + m;
+    }
+    for (const DevChannel& ch : b->channels)
+      if (!ch.mixed_unitary && b->any_streamed)
+        throw Error(kUnimplemented,
+                    "Amplitude-damping, reset and phase-damping channels are "
+                    "supported up to 14 qubits.");
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, false, 0, s, &a);
+    // aux: reps (int32) ; aux2: prefix (int64) + accumulators (double)
+    b->aux.reserve(cells * sizeof(int32_t), b->device);
+    TFQG_CUDA(cudaMemcpyAsync(b->aux.p, reps.data(), cells * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, s));
+    size_t pbytes = align256(prefix.size() * sizeof(int64_t));
+    b->aux2.reserve(pbytes + cells * sizeof(double), b->device);
+    TFQG_CUDA(cudaMemcpyAsync(b->aux2.p, prefix.data(), prefix.size() * sizeof(int64_t),
+                              cudaMemcpyHostToDevice, s));
+    double* acc = reinterpret_cast<double*>(static_cast<char*>(b->aux2.p) + pbytes);
+    TFQG_CUDA(cudaMemsetAsync(acc, 0, cells * sizeof(double), s));
+    float* dout = expectations;
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<float*>(b->out.p);
+    }
+    a.reps = static_cast<const int32_t*>(b->aux.p);
+    a.traj_prefix = static_cast<const int64_t*>(b->aux2.p);
+    a.total_traj = prefix.back();
+    a.acc = acc;
+    a.seed = seed;
+    a.out_f = dout;
+    if (a.total_traj > 0) simulate(b, kModeNoisy, &a, s);
+    TFQG_CUDA(launch_noisy_finalize(b->bd, a, s));
+    finish(b, expectations, dout, obytes, device_buffers, s);
+    // the host vectors above are read by async copies: keep them alive
+    TFQG_CUDA(cudaStreamSynchronize(s));
+    return 0;
+  });
+}
+
+int tfqg_simulate_expectation(const char* const* programs,
+                              const int64_t* program_lens, int64_t batch,
+                              const char* const* symbol_names,
+                              const int64_t* symbol_name_lens,
+                              int64_t num_symbols, const float* symbol_values,
+                              const char* const* pauli_sums,
+                              const int64_t* pauli_sum_lens, int64_t num_ops,
+                              float* expectations) {
+  tfqg_batch* b = nullptr;
+  int rc = tfqg_batch_create(programs, program_lens, batch, symbol_names,
+                             symbol_name_lens, num_symbols, pauli_sums,
+                             pauli_sum_lens, num_ops, TFQG_KIND_FORWARD, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_expectation(b, symbol_values, expectations, 0, nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
+int tfqg_adj_grad(const char* const* programs, const int64_t* program_lens,
+                  int64_t batch, const char* const* symbol_names,
+                  const int64_t* symbol_name_lens, int64_t num_symbols,
+                  const float* symbol_values, const char* const* pauli_sums,
+                  const int64_t* pauli_sum_lens, int64_t num_ops,
+                  const float* downstream_grads, float* grads) {
+  tfqg_batch* b = nullptr;
+  int rc = tfqg_batch_create(programs, program_lens, batch, symbol_names,
+                             symbol_name_lens, num_symbols, pauli_sums,
+                             pauli_sum_lens, num_ops, TFQG_KIND_ADJOINT, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_adj_grad(b, symbol_values, downstream_grads,
+                           TFQG_GRAD_REFERENCE_FD, grads, 0, nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
+int tfqg_noisy_expectation(const char* const* programs,
+                           const int64_t* program_lens, int64_t batch,
+                           const char* const* symbol_names,
+                           const int64_t* symbol_name_lens,
+                           int64_t num_symbols, const float* symbol_values,
+                           const char* const* pauli_sums,
+                           const int64_t* pauli_sum_lens, int64_t num_ops,
+                           const int32_t* num_samples, uint64_t seed,
+                           float* expectations) {
+  tfqg_batch* b = nullptr;
+  int rc = tfqg_batch_create(programs, program_lens, batch, symbol_names,
+                             symbol_name_lens, num_symbols, pauli_sums,
+                             pauli_sum_lens, num_ops, TFQG_KIND_NOISY, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_noisy_expectation(b, symbol_values, num_samples, seed,
+                                    expectations, 0, nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,794 @@
+// Host compiler: wire decoding, qubit/symbol resolution, gate templates and
+// tile-pass planning.  Follows the reference's parse path:
+//   ParseProto ............ tensorflow_quantum/core/ops/parse_context.cc:155-170
+//   ResolveQubitIds ....... tensorflow_quantum/core/src/program_resolution.cc:49-186
+//   ParseAppendGate ....... tensorflow_quantum/core/src/circuit_parser_qsim.cc:53-596
+//   channels .............. circuit_parser_qsim.cc:598-769
+#include "host.h"
+
+#include "gate_math.cuh"
+
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <set>
+#include <tuple>
+
+namespace tfqg {
+
+// ---------------------------------------------------------------------------
+// protobuf wire decoding
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Reader {
+  const uint8_t* p;
+  const uint8_t* end;
+  bool ok = true;
+
+  bool done() const { return p >= end; }
+
+  uint64_t varint() {
+    uint64_t v = 0;
+    for (int shift = 0; shift < 64; shift += 7) {
+      if (p >= end) { ok = false; return 0; }
+      uint8_t c = *p++;
+      v |= uint64_t(c & 0x7F) << shift;
+      if (!(c & 0x80)) return v;
+    }
+    ok = false;
+    return 0;
+  }
+
+  // Reads one field; returns false at end or on malformed input.
+  bool field(uint32_t* num, uint32_t* wt, const uint8_t** data, size_t* len,
+             uint64_t* ival) {
+    if (p >= end) return false;
+    uint64_t key = varint();
+    if (!ok) return false;
+    *num = uint32_t(key >> 3);
+    *wt = uint32_t(key & 7);
+    if (*num == 0) { ok = false; return false; }
+    switch (*wt) {
+      case 0:
+        *ival = varint();
+        return ok;
+      case 1:
+        if (end - p < 8) { ok = false; return false; }
+        *data = p; *len = 8; p += 8;
+        return true;
+      case 2: {
+        uint64_t l = varint();
+        if (!ok || uint64_t(end - p) < l) { ok = false; return false; }
+        *data = p; *len = size_t(l); p += l;
+        return true;
+      }
+      case 5:
+        if (end - p < 4) { ok = false; return false; }
+        *data = p; *len = 4; p += 4;
+        return true;
+      default:
+        ok = false;
+        return false;
+    }
+  }
+};
+
+// Calls f(field, wire_type, data, len) for each field; false on bad input.
+template <class F>
+bool for_fields(const uint8_t* b, size_t n, F&& f) {
+  Reader rd{b, b + n};
+  uint32_t fn, wt;
+  const uint8_t* fd = nullptr;
+  size_t fl = 0;
+  uint64_t iv = 0;
+  while (rd.field(&fn, &wt, &fd, &fl, &iv))
+    if (!f(fn, wt, fd, fl)) return false;
+  return rd.ok;
+}
+
+float read_f32(const uint8_t* d) {
+  float f;
+  memcpy(&f, d, 4);
+  return f;
+}
+
+bool parse_arg(const uint8_t* b, size_t n, ArgP* a) {
+  return for_fields(b, n, [&](uint32_t fn, uint32_t wt, const uint8_t* fd,
+                              size_t fl) {
+    if (fn == 1 && wt == 2) {
+      return for_fields(fd, fl, [&](uint32_t fn2, uint32_t wt2,
+                                    const uint8_t* d2, size_t l2) {
+        if (fn2 == 1 && wt2 == 5) a->f = read_f32(d2);
+        else if (fn2 == 3 && wt2 == 2) a->str.assign((const char*)d2, l2);
+        return true;
+      });
+    }
+    if (fn == 2 && wt == 2) a->symbol.assign((const char*)fd, fl);
+    return true;
+  });
+}
+
+bool parse_op(const uint8_t* b, size_t n, OpP* op) {
+  return for_fields(b, n, [&](uint32_t fn, uint32_t wt, const uint8_t* fd,
+                              size_t fl) {
+    if (fn == 1 && wt == 2) {
+      return for_fields(fd, fl, [&](uint32_t f2, uint32_t w2,
+                                    const uint8_t* d2, size_t l2) {
+        if (f2 == 1 && w2 == 2) op->gate.assign((const char*)d2, l2);
+        return true;
+      });
+    }
+    if (fn == 2 && wt == 2) {
+      std::string key;
+      ArgP val;
+      bool ok = for_fields(fd, fl, [&](uint32_t f2, uint32_t w2,
+                                       const uint8_t* d2, size_t l2) {
+        if (f2 == 1 && w2 == 2) {
+          key.assign((const char*)d2, l2);
+        } else if (f2 == 2 && w2 == 2) {
+          val = ArgP();
+          return parse_arg(d2, l2, &val);
+        }
+        return true;
+      });
+      if (!ok) return false;
+      op->args.emplace_back(std::move(key), std::move(val));
+      return true;
+    }
+    if (fn == 3 && wt == 2) {
+      std::string id;
+      bool ok = for_fields(fd, fl, [&](uint32_t f2, uint32_t w2,
+                                       const uint8_t* d2, size_t l2) {
+        if (f2 == 2 && w2 == 2) id.assign((const char*)d2, l2);
+        return true;
+      });
+      if (!ok) return false;
+      op->qubits.push_back(std::move(id));
+    }
+    return true;
+  });
+}
+
+bool parse_program(const uint8_t* b, size_t n, ProgramP* prog) {
+  return for_fields(b, n, [&](uint32_t fn, uint32_t wt, const uint8_t* fd,
+                              size_t fl) {
+    if (!(fn == 2 && wt == 2)) return true;  // circuit (messages merge)
+    return for_fields(fd, fl, [&](uint32_t f2, uint32_t w2, const uint8_t* d2,
+                                  size_t l2) {
+      if (!(f2 == 2 && w2 == 2)) return true;  // moment
+      std::vector<OpP> ops;
+      bool ok = for_fields(d2, l2, [&](uint32_t f3, uint32_t w3,
+                                       const uint8_t* d3, size_t l3) {
+        if (f3 == 1 && w3 == 2) {
+          OpP op;
+          if (!parse_op(d3, l3, &op)) return false;
+          ops.push_back(std::move(op));
+        }
+        return true;
+      });
+      if (!ok) return false;
+      prog->moments.push_back(std::move(ops));
+      return true;
+    });
+  });
+}
+
+bool parse_paulisum(const uint8_t* b, size_t n, PauliSumP* ps) {
+  return for_fields(b, n, [&](uint32_t fn, uint32_t wt, const uint8_t* fd,
+                              size_t fl) {
+    if (!(fn == 1 && wt == 2)) return true;
+    TermP t;
+    bool ok = for_fields(fd, fl, [&](uint32_t f2, uint32_t w2,
+                                     const uint8_t* d2, size_t l2) {
+      if (f2 == 1 && w2 == 5) {
+        t.re = read_f32(d2);
+      } else if (f2 == 2 && w2 == 5) {
+        t.im = read_f32(d2);
+      } else if (f2 == 3 && w2 == 2) {
+        std::string q, ty;
+        bool ok2 = for_fields(d2, l2, [&](uint32_t f3, uint32_t w3,
+                                          const uint8_t* d3, size_t l3) {
+          if (f3 == 1 && w3 == 2) q.assign((const char*)d3, l3);
+          else if (f3 == 2 && w3 == 2) ty.assign((const char*)d3, l3);
+          return true;
+        });
+        if (!ok2) return false;
+        t.paulis.emplace_back(std::move(q), std::move(ty));
+      }
+      return true;
+    });
+    if (!ok) return false;
+    ps->push_back(std::move(t));
+    return true;
+  });
+}
+
+}  // namespace
+
+const ArgP* OpP::find(const std::string& key) const {
+  for (auto it = args.rbegin(); it != args.rend(); ++it)
+    if (it->first == key) return &it->second;
+  return nullptr;
+}
+
+void decode_program(const char* data, size_t len, ProgramP* out) {
+  *out = ProgramP();
+  if (!parse_program(reinterpret_cast<const uint8_t*>(data), len, out))
+    throw Error(kInvalidArgument,
+                "Unparseable proto: " + std::string(data, len));
+}
+
+void decode_paulisum(const char* data, size_t len, PauliSumP* out) {
+  out->clear();
+  if (!parse_paulisum(reinterpret_cast<const uint8_t*>(data), len, out))
+    throw Error(kInvalidArgument,
+                "Unparseable proto: " + std::string(data, len));
+}
+
+bool simple_atoi(const std::string& s, int64_t* out) {
+  size_t i = 0, j = s.size();
+  while (i < j && isspace((unsigned char)s[i])) ++i;
+  while (j > i && isspace((unsigned char)s[j - 1])) --j;
+  if (i == j) return false;
+  bool neg = false;
+  if (s[i] == '+' || s[i] == '-') {
+    neg = s[i] == '-';
+    ++i;
+  }
+  if (i == j) return false;
+  int64_t v = 0;
+  for (; i < j; ++i) {
+    if (s[i] < '0' || s[i] > '9') return false;
+    v = v * 10 + (s[i] - '0');
+    if (v > int64_t(2147483648LL)) return false;
+  }
+  v = neg ? -v : v;
+  if (v > 2147483647LL || v < -2147483648LL) return false;
+  *out = v;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// qubit resolution (program_resolution.cc:49-186)
+// ---------------------------------------------------------------------------
+namespace {
+
+std::vector<std::string> split(const std::string& s, char sep) {
+  std::vector<std::string> out;
+  size_t start = 0;
+  while (true) {
+    size_t k = s.find(sep, start);
+    if (k == std::string::npos) {
+      out.push_back(s.substr(start));
+      return out;
+    }
+    out.push_back(s.substr(start, k - start));
+    start = k + 1;
+  }
+}
+
+using QubitKey = std::tuple<int64_t, int64_t, std::string>;
+
+void register_qubits(const std::string& qb_string, std::set<QubitKey>* ids) {
+  if (qb_string.empty()) return;
+  for (const std::string& qb : split(qb_string, ',')) {
+    std::vector<std::string> parts = split(qb, '_');
+    if (parts.size() == 1) parts.insert(parts.begin(), "2147483647");
+    int64_t r, c;
+    if (parts.size() != 2 || !simple_atoi(parts[0], &r) ||
+        !simple_atoi(parts[1], &c))
+      throw Error(kInvalidArgument, "Unable to parse qubit: " + qb);
+    ids->insert(QubitKey(r, c, qb));
+  }
+}
+
+const std::string& control_string(const OpP& op, const char* key) {
+  static const std::string empty;
+  const ArgP* a = op.find(key);
+  return a ? a->str : empty;
+}
+
+}  // namespace
+
+int resolve_qubits(const ProgramP& prog,
+                   std::unordered_map<std::string, int>* index) {
+  index->clear();
+  if (prog.moments.empty()) return 0;  // (#679) empty program
+  std::set<QubitKey> ids;
+  for (const auto& m : prog.moments)
+    for (const auto& op : m) {
+      for (const auto& q : op.qubits) register_qubits(q, &ids);
+      register_qubits(control_string(op, "control_qubits"), &ids);
+    }
+  int i = 0;
+  for (const auto& k : ids) (*index)[std::get<2>(k)] = i++;
+  return i;
+}
+
+// ---------------------------------------------------------------------------
+// gate templates (circuit_parser_qsim.cc:53-596)
+// ---------------------------------------------------------------------------
+namespace {
+
+struct GateInfo {
+  GateKind kind;
+  int nq;
+};
+
+bool lookup_gate(const std::string& id, GateInfo* g) {
+  static const std::unordered_map<std::string, GateInfo> table = {
+      {"I", {GK_I1, 1}},    {"HP", {GK_HP, 1}},    {"XP", {GK_XP, 1}},
+      {"XXP", {GK_XXP, 2}}, {"YP", {GK_YP, 1}},    {"YYP", {GK_YYP, 2}},
+      {"ZP", {GK_ZP, 1}},   {"ZZP", {GK_ZZP, 2}},  {"CZP", {GK_CZP, 2}},
+      {"I2", {GK_I2, 2}},   {"CNP", {GK_CNP, 2}},  {"SP", {GK_SP, 2}},
+      {"ISP", {GK_ISP, 2}}, {"PXP", {GK_PXP, 1}},  {"FSIM", {GK_FSIM, 2}},
+      {"PISP", {GK_PISP, 2}}};
+  auto it = table.find(id);
+  if (it == table.end()) return false;
+  *g = it->second;
+  return true;
+}
+
+bool lookup_channel(const std::string& id, ChannelKind* k) {
+  static const std::unordered_map<std::string, ChannelKind> table = {
+      {"DP", CK_DP}, {"ADP", CK_ADP}, {"GAD", CK_GAD}, {"AD", CK_AD},
+      {"RST", CK_RST}, {"PD", CK_PD}, {"PF", CK_PF}, {"BF", CK_BF}};
+  auto it = table.find(id);
+  if (it == table.end()) return false;
+  *k = it->second;
+  return true;
+}
+
+// ParseProtoArg: constant value, or the symbol's column.
+void parse_arg(const OpP& op, const char* name, const SymbolTable& names,
+               float* value, int16_t* src) {
+  const ArgP* a = op.find(name);
+  if (!a)
+    throw Error(kInvalidArgument,
+                std::string("Could not find arg: ") + name + " in op.");
+  *value = a->f;
+  *src = -1;
+  if (!a->symbol.empty()) {
+    auto it = names.col.find(a->symbol);
+    if (it == names.col.end())
+      throw Error(kInvalidArgument,
+                  "Could not find symbol in parameter map: " + a->symbol);
+    *src = int16_t(it->second);
+  }
+}
+
+int qubit_bit(const OpP& op, int i, int n,
+              const std::unordered_map<std::string, int>& index) {
+  if (int(op.qubits.size()) <= i)
+    throw Error(kInvalidArgument,
+                "Operation " + op.gate + " has too few qubits.");
+  auto it = index.find(op.qubits[i]);
+  if (it == index.end())
+    throw Error(kInvalidArgument, "Unable to parse qubit: " + op.qubits[i]);
+  return n - it->second - 1;
+}
+
+// ParseProtoControls (circuit_parser_qsim.cc:84-129).
+void parse_controls(const OpP& op, int n,
+                    const std::unordered_map<std::string, int>& index,
+                    uint32_t* cmask, uint32_t* cval) {
+  *cmask = 0;
+  *cval = 0;
+  const std::string& cq = control_string(op, "control_qubits");
+  const std::string& cv = control_string(op, "control_values");
+  if (cq.empty() && cv.empty()) return;
+  std::vector<std::string> qt = split(cq, ','), vt = split(cv, ',');
+  if (qt.size() != vt.size())
+    throw Error(kInvalidArgument,
+                "Mistmatched number of control qubits and control values.");
+  std::vector<int> bits;
+  for (const auto& t : qt) {
+    auto it = index.find(t);
+    if (it == index.end())
+      throw Error(kInvalidArgument, "Unable to parse qubit: " + t);
+    bits.push_back(n - it->second - 1);
+  }
+  for (size_t k = 0; k < vt.size(); ++k) {
+    int64_t v;
+    if (!simple_atoi(vt[k], &v))
+      throw Error(kInvalidArgument, "Unparseable control value: " + vt[k]);
+    *cmask |= 1u << bits[k];
+    if (v & 1) *cval |= 1u << bits[k];
+  }
+}
+
+void build_gate(const OpP& op, const GateInfo& info, int n,
+                const SymbolTable& names,
+                const std::unordered_map<std::string, int>& index,
+                GateTemplate* g) {
+  memset(g, 0, sizeof(*g));
+  g->kind = info.kind;
+  g->nq = uint8_t(info.nq);
+  for (int i = 0; i < 5; ++i) g->src[i] = -1;
+  g->grad_slot = -1;
+  g->b0 = uint8_t(qubit_bit(op, 0, n, index));
+  if (info.nq == 2) g->b1 = uint8_t(qubit_bit(op, 1, n, index));
+  switch (info.kind) {
+    case GK_I1: case GK_I2:
+      break;
+    case GK_PXP:
+      // argument order of PhasedXGate (circuit_parser_qsim.cc:393-421)
+      parse_arg(op, "exponent", names, &g->a[2], &g->src[2]);
+      parse_arg(op, "exponent_scalar", names, &g->a[3], &g->src[3]);
+      parse_arg(op, "phase_exponent", names, &g->a[0], &g->src[0]);
+      parse_arg(op, "phase_exponent_scalar", names, &g->a[1], &g->src[1]);
+      parse_arg(op, "global_shift", names, &g->a[4], &g->src[4]);
+      break;
+    case GK_FSIM:
+      parse_arg(op, "theta", names, &g->a[0], &g->src[0]);
+      parse_arg(op, "theta_scalar", names, &g->a[1], &g->src[1]);
+      parse_arg(op, "phi", names, &g->a[2], &g->src[2]);
+      parse_arg(op, "phi_scalar", names, &g->a[3], &g->src[3]);
+      break;
+    case GK_PISP:
+      parse_arg(op, "exponent", names, &g->a[2], &g->src[2]);
+      parse_arg(op, "exponent_scalar", names, &g->a[3], &g->src[3]);
+      parse_arg(op, "phase_exponent", names, &g->a[0], &g->src[0]);
+      parse_arg(op, "phase_exponent_scalar", names, &g->a[1], &g->src[1]);
+      break;
+    default:  // eigen gates (SingleEigenGate / TwoEigenGate)
+      parse_arg(op, "exponent", names, &g->a[0], &g->src[0]);
+      parse_arg(op, "exponent_scalar", names, &g->a[1], &g->src[1]);
+      parse_arg(op, "global_shift", names, &g->a[2], &g->src[2]);
+      break;
+  }
+  parse_controls(op, n, index, &g->cmask, &g->cval);
+  const uint32_t tmask = (1u << g->b0) | (info.nq == 2 ? (1u << g->b1) : 0u);
+  if (info.nq == 2 && g->b0 == g->b1)
+    throw Error(kInvalidArgument,
+                "Operation " + op.gate + " acts twice on qubit " + op.qubits[0] + ".");
+  if (g->cmask & tmask)
+    throw Error(kInvalidArgument,
+                "A control qubit of operation " + op.gate + " is also a target.");
+  // Symbolic parameters get gradients, in the reference's metadata order:
+  // phase exponent / theta first, then exponent / phi (adj_util.cc:37-150).
+  bool two_param =
+      info.kind == GK_PXP || info.kind == GK_FSIM || info.kind == GK_PISP;
+  if (g->src[0] >= 0) g->gparam[g->ngrad++] = 0;
+  if (two_param && g->src[2] >= 0) g->gparam[g->ngrad++] = 1;
+}
+
+float channel_arg(const OpP& op, const char* name) {
+  const ArgP* a = op.find(name);
+  if (!a)
+    throw Error(kInvalidArgument,
+                std::string("Could not find arg: ") + name + " in op.");
+  if (!a->symbol.empty())
+    throw Error(kInvalidArgument,
+                "Could not find symbol in parameter map: " + a->symbol);
+  return a->f;
+}
+
+// Kraus operators of the supported channels: the published definitions of
+// cirq.depolarize, asymmetric_depolarize, generalized_amplitude_damp,
+// amplitude_damp, reset, phase_damp, phase_flip and bit_flip, which the
+// reference builds through qsim (circuit_parser_qsim.cc:598-747).
+void build_channel(const OpP& op, ChannelKind kind, ChannelHost* ch) {
+  std::vector<std::vector<double>> K;  // each 8 doubles: re,im row-major
+  auto mat = [](double a, double b, double c, double d) {
+    return std::vector<double>{a, 0, b, 0, c, 0, d, 0};
+  };
+  auto paulis = [&](double p0, double px, double py, double pz) {
+    K.push_back(mat(sqrt(p0), 0, 0, sqrt(p0)));
+    K.push_back(mat(0, sqrt(px), sqrt(px), 0));
+    K.push_back({0, 0, 0, -sqrt(py), 0, sqrt(py), 0, 0});
+    K.push_back(mat(sqrt(pz), 0, 0, -sqrt(pz)));
+  };
+  bool mixed = false;
+  std::vector<double> probs;
+  switch (kind) {
+    case CK_DP: {
+      double p = channel_arg(op, "p");
+      paulis(1 - p, p / 3, p / 3, p / 3);
+      probs = {1 - p, p / 3, p / 3, p / 3};
+      mixed = true;
+      break;
+    }
+    case CK_ADP: {
+      double px = channel_arg(op, "p_x"), py = channel_arg(op, "p_y"),
+             pz = channel_arg(op, "p_z");
+      paulis(1 - px - py - pz, px, py, pz);
+      probs = {1 - px - py - pz, px, py, pz};
+      mixed = true;
+      break;
+    }
+    case CK_PF: {
+      double p = channel_arg(op, "p");
+      K.push_back(mat(sqrt(1 - p), 0, 0, sqrt(1 - p)));
+      K.push_back(mat(sqrt(p), 0, 0, -sqrt(p)));
+      probs = {1 - p, p};
+      mixed = true;
+      break;
+    }
+    case CK_BF: {
+      double p = channel_arg(op, "p");
+      K.push_back(mat(sqrt(1 - p), 0, 0, sqrt(1 - p)));
+      K.push_back(mat(0, sqrt(p), sqrt(p), 0));
+      probs = {1 - p, p};
+      mixed = true;
+      break;
+    }
+    case CK_GAD: {
+      double p = channel_arg(op, "p"), g = channel_arg(op, "gamma");
+      K.push_back(mat(sqrt(p), 0, 0, sqrt(p) * sqrt(1 - g)));
+      K.push_back(mat(0, sqrt(p) * sqrt(g), 0, 0));
+      K.push_back(mat(sqrt(1 - p) * sqrt(1 - g), 0, 0, sqrt(1 - p)));
+      K.push_back(mat(0, 0, sqrt(1 - p) * sqrt(g), 0));
+      break;
+    }
+    case CK_AD: {
+      double g = channel_arg(op, "gamma");
+      K.push_back(mat(1, 0, 0, sqrt(1 - g)));
+      K.push_back(mat(0, sqrt(g), 0, 0));
+      break;
+    }
+    case CK_RST:
+      K.push_back(mat(1, 0, 0, 0));
+      K.push_back(mat(0, 1, 0, 0));
+      break;
+    case CK_PD: {
+      double g = channel_arg(op, "gamma");
+      K.push_back(mat(1, 0, 0, sqrt(1 - g)));
+      K.push_back(mat(0, 0, 0, sqrt(g)));
+      break;
+    }
+  }
+  memset(&ch->dev, 0, sizeof(ch->dev));
+  ch->dev.kind = kind;
+  ch->dev.nk = uint8_t(K.size());
+  ch->dev.mixed_unitary = mixed;
+  ch->kraus.clear();
+  double cum = 0;
+  for (size_t k = 0; k < K.size(); ++k) {
+    ch->kraus.insert(ch->kraus.end(), K[k].begin(), K[k].end());
+    if (mixed) {
+      cum += probs[k];
+      ch->dev.cum[k] = cum;
+      ch->dev.scale[k] = probs[k] > 0 ? float(1.0 / sqrt(probs[k])) : 0.f;
+      bool ident = K[k][2] == 0 && K[k][3] == 0 && K[k][4] == 0 &&
+                   K[k][5] == 0 && K[k][0] == K[k][6] && K[k][1] == K[k][7];
+      if (ident) ch->dev.ident_mask |= uint8_t(1u << k);
+    }
+  }
+}
+
+}  // namespace
+
+void compile_program(const ProgramP& prog, const SymbolTable& names,
+                     JobKind kind, CompiledProgram* out,
+                     std::unordered_map<std::string, int>* index) {
+  *out = CompiledProgram();
+  int n = resolve_qubits(prog, index);
+  if (n > 30)
+    throw Error(kResourceExhausted,
+                "Circuit acts on " + std::to_string(n) +
+                    " qubits; at most 30 fit this simulator's state layout.");
+  out->n = n;
+  if (n <= 0) return;
+  int grad_slots = 0;
+  for (const auto& m : prog.moments) {
+    for (const auto& op : m) {
+      GateInfo info;
+      if (lookup_gate(op.gate, &info)) {
+        GateTemplate g;
+        build_gate(op, info, n, names, *index, &g);
+        if (kind == kJobAdjoint && g.ngrad > 0) {
+          g.grad_slot = grad_slots;
+          for (int k = 0; k < g.ngrad; ++k)
+            out->grad_col.push_back(g.src[2 * g.gparam[k]]);
+          grad_slots += g.ngrad;
+        }
+        out->sequence.push_back(int32_t(out->gates.size()));
+        out->gates.push_back(g);
+        continue;
+      }
+      ChannelKind ck;
+      if (kind == kJobNoisy && lookup_channel(op.gate, &ck)) {
+        ChannelHost ch;
+        ch.bit = qubit_bit(op, 0, n, *index);
+        build_channel(op, ck, &ch);
+        out->sequence.push_back(~int32_t(out->channels.size()));
+        out->channels.push_back(std::move(ch));
+        continue;
+      }
+      if (kind == kJobNoisy)
+        throw Error(kInvalidArgument, "Could not parse channel id: " + op.gate);
+      throw Error(kInvalidArgument,
+                  "Could not parse gate id: " + op.gate +
+                      ". This is likely because a cirq.Channel was used in an "
+                      "op that does not support them.");
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pass planning
+// ---------------------------------------------------------------------------
+namespace {
+
+struct PlanItem {
+  int32_t seq;       // gate index, or ~channel
+  uint32_t targets;  // target bits
+  uint32_t deps;     // targets | controls
+};
+
+uint32_t low_mask(int k) { return k >= 32 ? 0xFFFFFFFFu : ((1u << k) - 1u); }
+
+int local_pos(uint32_t tile_mask, int bit) {
+  return __builtin_popcount(tile_mask & low_mask(bit));
+}
+
+DevOp make_op(const CompiledProgram& p, const PlanItem& it, uint32_t tile,
+              bool backward, const std::vector<int>& chan_bits) {
+  DevOp op;
+  memset(&op, 0, sizeof(op));
+  op.grad_slot = -1;
+  if (it.seq < 0) {
+    int c = ~it.seq;
+    op.type = OP_CHAN;
+    op.t0 = uint8_t(local_pos(tile, chan_bits[c]));
+    op.gate = uint32_t(c);
+    return op;
+  }
+  const GateTemplate& g = p.gates[it.seq];
+  op.gate = uint32_t(it.seq);
+  op.t0 = uint8_t(local_pos(tile, g.b0));
+  op.t1 = g.nq == 2 ? uint8_t(local_pos(tile, g.b1)) : 0;
+  for (int b = 0; b < 32; ++b) {
+    if (!(g.cmask >> b & 1)) continue;
+    uint32_t v = g.cval >> b & 1;
+    if (tile >> b & 1) {
+      int lp = local_pos(tile, b);
+      op.lcmask |= 1u << lp;
+      op.lcval |= v << lp;
+    } else {
+      op.gcmask |= 1u << b;
+      op.gcval |= v << b;
+    }
+  }
+  if (backward) {
+    op.type = g.nq == 1 ? OP_B1 : OP_B2;
+    op.ngrad = g.ngrad;
+    op.grad_slot = g.grad_slot;
+  } else if (gate_is_diagonal(g.kind)) {
+    op.type = g.nq == 1 ? OP_D1 : OP_D2;
+  } else {
+    op.type = g.nq == 1 ? OP_G1 : OP_G2;
+  }
+  return op;
+}
+
+void plan_sequence(const CompiledProgram& p, const std::vector<PlanItem>& items,
+                   int tile_bits, bool backward,
+                   const std::vector<int>& chan_bits,
+                   std::vector<DevPass>* passes, std::vector<DevOp>* ops) {
+  const int n = p.n;
+  const uint32_t all = low_mask(n);
+  if (n <= tile_bits) {
+    DevPass ps{all, uint32_t(ops->size()), 0, 0};
+    for (const auto& it : items) ops->push_back(make_op(p, it, all, backward, chan_bits));
+    ps.op_end = uint32_t(ops->size());
+    passes->push_back(ps);
+    return;
+  }
+  std::vector<PlanItem> remaining = items;
+  const uint32_t lanes = low_mask(kLaneBits);
+  while (!remaining.empty()) {
+    uint32_t S = lanes, blocked = 0;
+    std::vector<PlanItem> taken, rest;
+    for (const auto& it : remaining) {
+      if (it.deps & blocked) {
+        rest.push_back(it);
+        blocked |= it.deps;
+        continue;
+      }
+      uint32_t U = S | it.targets;
+      if (__builtin_popcount(U) <= tile_bits) {
+        S = U;
+        taken.push_back(it);
+      } else {
+        rest.push_back(it);
+        blocked |= it.deps;
+      }
+    }
+    for (int b = 0; b < n && __builtin_popcount(S) < tile_bits; ++b) S |= 1u << b;
+    DevPass ps{S, uint32_t(ops->size()), 0, 0};
+    for (const auto& it : taken) ops->push_back(make_op(p, it, S, backward, chan_bits));
+    ps.op_end = uint32_t(ops->size());
+    passes->push_back(ps);
+    if (taken.empty()) throw Error(kInternal, "pass planner made no progress");
+    remaining.swap(rest);
+  }
+}
+
+}  // namespace
+
+void plan_program(CompiledProgram* p, JobKind kind) {
+  p->fwd_passes.clear();
+  p->bwd_passes.clear();
+  p->fwd_ops.clear();
+  p->bwd_ops.clear();
+  if (p->empty()) return;
+  const int res_max = kind == kJobAdjoint ? kResidentMaxAdjoint : kResidentMaxSingle;
+  p->resident = p->n <= res_max;
+  const int tile_bits = p->resident ? p->n : kStreamTileBits;
+  std::vector<int> chan_bits(p->channels.size(), 0);
+  std::vector<PlanItem> items;
+  items.reserve(p->sequence.size());
+  for (int32_t s : p->sequence) {
+    PlanItem it;
+    it.seq = s;
+    if (s >= 0) {
+      const GateTemplate& g = p->gates[s];
+      it.targets = (1u << g.b0) | (g.nq == 2 ? 1u << g.b1 : 0u);
+      it.deps = it.targets | g.cmask;
+    } else {
+      int bit = p->channels[~s].bit;
+      chan_bits[~s] = bit;
+      it.targets = 1u << bit;
+      it.deps = it.targets;
+    }
+    items.push_back(it);
+  }
+  plan_sequence(*p, items, tile_bits, false, chan_bits, &p->fwd_passes, &p->fwd_ops);
+  if (kind == kJobAdjoint) {
+    std::vector<PlanItem> rev(items.rbegin(), items.rend());
+    plan_sequence(*p, rev, tile_bits, true, chan_bits, &p->bwd_passes, &p->bwd_ops);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pauli sums -> device terms (util_qsim.h:142-188)
+// ---------------------------------------------------------------------------
+void lower_paulisum(const PauliSumP& ps,
+                    const std::unordered_map<std::string, int>& index, int n,
+                    int op, std::vector<DevTerm>* out) {
+  for (const TermP& t : ps) {
+    DevTerm d;
+    memset(&d, 0, sizeof(d));
+    d.coef = t.re;
+    d.op = uint16_t(op);
+    if (t.paulis.empty()) {
+      d.identity = 1;
+      out->push_back(d);
+      continue;
+    }
+    for (const auto& pq : t.paulis) {
+      auto it = index.find(pq.first);
+      if (it == index.end())
+        throw Error(kInvalidArgument,
+                    "Found a Pauli sum operating on qubits not found in "
+                    "circuit.");
+      int bit = n - it->second - 1;
+      uint32_t m = 1u << bit;
+      // Products on one qubit are applied in order, as the reference applies
+      // one gate per factor (circuit_parser_qsim.cc:863-895).
+      const std::string& ty = pq.second;
+      if (ty == "X") {
+        d.flip ^= m;
+      } else if (ty == "Z") {
+        // Z after the preceding factors: sign from the current bit value
+        d.zy ^= m;
+      } else if (ty == "Y") {
+        d.flip ^= m;
+        d.zy ^= m;
+        d.ny = uint8_t((d.ny + 1) & 3);
+      } else {
+        throw Error(kInvalidArgument,
+                    "Could not parse gate id: " + ty +
+                        "P. This is likely because a cirq.Channel was used in "
+                        "an op that does not support them.");
+      }
+    }
+    out->push_back(d);
+  }
+}
+
+}  // namespace tfqg

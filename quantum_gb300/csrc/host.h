@@ -1,0 +1,112 @@
+// Host side of the path: decode serialized programs / Pauli sums, resolve
+// qubits and symbols, build gate templates and plan tile passes.
+#pragma once
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "tfqg_types.h"
+
+namespace tfqg {
+
+// Status codes follow tensorflow::error::Code numbering.
+enum StatusCode {
+  kOk = 0,
+  kInvalidArgument = 3,
+  kResourceExhausted = 8,
+  kUnimplemented = 12,
+  kInternal = 13,
+};
+
+struct Error : public std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// ---- decoded wire messages (tensorflow_quantum/core/proto/*.proto) ----
+struct ArgP {
+  float f = 0.f;        // arg_value.float_value
+  std::string symbol;   // symbol
+  std::string str;      // arg_value.string_value
+};
+
+struct OpP {
+  std::string gate;
+  std::vector<std::pair<std::string, ArgP>> args;  // map entries, last wins
+  std::vector<std::string> qubits;
+  const ArgP* find(const std::string& key) const;
+};
+
+struct ProgramP {
+  std::vector<std::vector<OpP>> moments;
+};
+
+struct TermP {
+  float re = 0.f, im = 0.f;
+  std::vector<std::pair<std::string, std::string>> paulis;  // (qubit id, type)
+};
+using PauliSumP = std::vector<TermP>;
+
+void decode_program(const char* data, size_t len, ProgramP* out);
+void decode_paulisum(const char* data, size_t len, PauliSumP* out);
+
+// absl::SimpleAtoi semantics: optional surrounding whitespace and sign.
+bool simple_atoi(const std::string& s, int64_t* out);
+
+// ---- compiled programs ----
+enum JobKind { kJobForward = 0, kJobAdjoint = 1, kJobNoisy = 2 };
+
+// Largest qubit count kept resident in shared memory (one CTA per circuit).
+constexpr int kResidentMaxSingle = 14;   // one state: 2^14 * 8 B = 128 KiB
+constexpr int kResidentMaxAdjoint = 13;  // psi and lambda: 2 * 64 KiB
+constexpr int kStreamTileBits = 13;      // tile of a streamed pass: 64 KiB
+constexpr int kLaneBits = 5;             // low bits every streamed tile holds
+
+struct ChannelHost {
+  DevChannel dev;
+  int bit = 0;                // target bit
+  std::vector<double> kraus;  // nk * 8 doubles (2x2 complex)
+};
+
+struct CompiledProgram {
+  int n = 0;
+  bool resident = true;
+  std::vector<GateTemplate> gates;
+  std::vector<int32_t> grad_col;      // derivative slot -> symbol column
+  std::vector<ChannelHost> channels;  // noisy programs
+  // op list in program order: gate index, or ~channel index (< 0)
+  std::vector<int32_t> sequence;
+  std::vector<DevPass> fwd_passes, bwd_passes;
+  std::vector<DevOp> fwd_ops, bwd_ops;
+  bool empty() const { return n == 0 || sequence.empty(); }
+};
+
+struct SymbolTable {
+  std::unordered_map<std::string, int> col;  // name -> column (last wins)
+  int64_t num_symbols = 0;
+};
+
+// Builds the gate templates of `prog` (circuit_parser_qsim.cc:828-861 /
+// 773-826 for noisy programs).  `names` resolves symbols; errors mirror the
+// reference messages.  `index` maps qubit id -> resolved index.
+void compile_program(const ProgramP& prog, const SymbolTable& names,
+                     JobKind kind, CompiledProgram* out,
+                     std::unordered_map<std::string, int>* index);
+
+// Resolves qubit ids (program_resolution.cc:90-186).
+int resolve_qubits(const ProgramP& prog,
+                   std::unordered_map<std::string, int>* index);
+
+// Plans forward (and, for the adjoint, backward) passes.
+void plan_program(CompiledProgram* prog, JobKind kind);
+
+// Pauli sum -> device terms for column `op` (bits relative to n qubits).
+void lower_paulisum(const PauliSumP& ps,
+                    const std::unordered_map<std::string, int>& index, int n,
+                    int op, std::vector<DevTerm>* out);
+
+}  // namespace tfqg

@@ -1,0 +1,942 @@
+// sm_103a kernels of the TFQ state-vector hot path.
+//
+//  build_matrices_kernel   binds symbol values: one thread per (row, gate)
+//                          computes the complex64 gate matrix and, for the
+//                          adjoint, the derivative matrix of each symbolic
+//                          parameter (reference finite difference with
+//                          eps = 5e-3, adj_util.cc:32,175-302, or exact).
+//  simulate_kernel<MODE>   persistent CTAs pull rows (circuits) or
+//                          trajectories from a work queue.  A row whose state
+//                          fits shared memory is simulated entirely there
+//                          (resident); larger states live in a per-CTA global
+//                          slot and are streamed through shared memory one
+//                          tile per pass (the host planner groups gates into
+//                          passes whose targets lie inside the tile).
+//                          Epilogues: Pauli-sum expectation
+//                          (util_qsim.h:142-188), state copy with -2 padding
+//                          (tfq_simulate_state_op.cc:196-207), sampling with
+//                          the reference bit layout
+//                          (tfq_simulate_samples_op.cc:226-243), adjoint sweep
+//                          (tfq_adj_grad_op.cc:199-276), noisy trajectories
+//                          (tfq_noisy_expectation.cc:258-391).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gate_math.cuh"
+#include "kernels.h"
+
+namespace tfqg {
+namespace {
+
+constexpr int kTile = 13;              // streamed tile bits (matches host)
+constexpr int kHiBits = kTile - 5;     // tile bits above the 5 lane bits
+constexpr int kMaxChunks = 1024;       // sampler prefix chunks
+constexpr int kWarps = kSimThreads / 32;
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cfma(float2 m, float2 a, float2 acc) {
+  acc.x = fmaf(m.x, a.x, fmaf(-m.y, a.y, acc.x));
+  acc.y = fmaf(m.x, a.y, fmaf(m.y, a.x, acc.y));
+  return acc;
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ uint32_t ins0(uint32_t i, int b) {
+  return ((i >> b) << (b + 1)) | (i & ((1u << b) - 1u));
+}
+// Re(conj(a) * b)
+__device__ __forceinline__ float re_conj_mul(float2 a, float2 b) {
+  return fmaf(a.x, b.x, a.y * b.y);
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+// Uniform double in [0, 1) with 53 random bits.
+__device__ __forceinline__ double uniform01(uint64_t seed, uint32_t a,
+                                            uint32_t b, uint32_t c) {
+  uint4 r = philox(make_uint4(a, b, c, 0x9A7Eu),
+                   make_uint2(uint32_t(seed), uint32_t(seed >> 32)));
+  return (double(r.x >> 5) * 67108864.0 + double(r.y >> 6)) *
+         (1.0 / 9007199254740992.0);
+}
+
+// ---------------------------------------------------------------------------
+// matrix build
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void store_mat(float2* dst, const Cx<double>* m,
+                                          int nq) {
+  int dim = nq == 1 ? 4 : 16;
+  for (int i = 0; i < 16; ++i)
+    dst[i] = i < dim ? make_float2(float(m[i].re), float(m[i].im))
+                     : make_float2(0.f, 0.f);
+}
+
+__global__ void build_matrices_kernel(BatchDevice b, RunArgs a, int with_grads) {
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= b.total_gates) return;
+  // locate the row: rows are laid out with increasing mat_offset
+  int lo = 0, hi = b.num_rows - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (int64_t(b.rows[mid].mat_offset) <= t) lo = mid; else hi = mid - 1;
+  }
+  const DevRow row = b.rows[lo];
+  const DevProgram prog = b.programs[row.program];
+  int g = int(t - int64_t(row.mat_offset));
+  if (g >= prog.num_gates) return;
+  const GateTemplate gt = b.gates[prog.gate_begin + g];
+  float v[5];
+  for (int i = 0; i < 5; ++i)
+    v[i] = gt.src[i] >= 0 ? a.values[int64_t(lo) * b.num_symbols + gt.src[i]]
+                          : gt.a[i];
+  // effective parameters, fp32 products as in circuit_parser_qsim.cc
+  GateTemplate gv = gt;
+  for (int i = 0; i < 5; ++i) gv.a[i] = v[i];
+  float e0, e1, e2;
+  effective_params(gv, v[0], v[2], &e0, &e1, &e2);
+  Cx<double> m[16];
+  int nq = gate_matrix<double>(gt.kind, e0, e1, e2, m);
+  store_mat(a.mats + int64_t(t) * 16, m, nq);
+  if (!with_grads || gt.ngrad == 0) return;
+  for (int k = 0; k < gt.ngrad; ++k) {
+    const int p = gt.gparam[k];
+    float2* dst = a.dmats + (int64_t(row.dmat_offset) + gt.grad_slot + k) * 16;
+    Cx<double> d[16];
+    if (a.grad_rule == 0) {
+      // (G(x + eps) - G(x - eps)) * 0.5 / eps with fp32 parameter
+      // arithmetic (adj_util.cc:175-186).
+      const float eps = 5e-3f;
+      const float raw = v[2 * p];
+      float rp = raw + eps, rm = raw - eps;
+      float ep0, ep1, ep2, em0, em1, em2;
+      effective_params(gv, p == 0 ? rp : v[0], p == 1 ? rp : v[2], &ep0, &ep1, &ep2);
+      effective_params(gv, p == 0 ? rm : v[0], p == 1 ? rm : v[2], &em0, &em1, &em2);
+      Cx<double> gp[16], gm[16];
+      gate_matrix<double>(gt.kind, ep0, ep1, ep2, gp);
+      gate_matrix<double>(gt.kind, em0, em1, em2, gm);
+      const double f = 0.5 / double(eps);
+      for (int i = 0; i < 16; ++i)
+        d[i] = Cx<double>((gp[i].re - gm[i].re) * f, (gp[i].im - gm[i].im) * f);
+    } else {
+      // exact derivative: dual numbers through the same gate formulas
+      Dual d0(e0), d1(e1), d2(e2);
+      double scale = gv.a[2 * p + 1];
+      if (p == 0) d0 = Dual(e0, scale); else d1 = Dual(e1, scale);
+      Cx<Dual> md[16];
+      gate_matrix<Dual>(gt.kind, d0, d1, d2, md);
+      for (int i = 0; i < 16; ++i) d[i] = Cx<double>(md[i].re.d, md[i].im.d);
+    }
+    store_mat(dst, d, nq);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// simulation building blocks (all threads of the CTA take part)
+// ---------------------------------------------------------------------------
+struct Smem {
+  float2* psi;        // resident state / tile
+  float2* lam;        // adjoint state / tile
+  uint32_t* hi;       // tile-local high bits -> global offsets
+  double* red;        // [2][4][kWarps] reduction scratch
+  double* csum;       // sampler chunk prefix sums
+  double* grad;       // adjoint accumulators
+};
+
+__device__ __forceinline__ void load4(const float2* __restrict__ m, float2* r) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) r[i] = __ldg(m + i);
+}
+
+__device__ void op_g1(float2* s, int T, int t0, uint32_t lcm, uint32_t lcv,
+                      const float2* m) {
+  float2 g[4];
+  load4(m, g);
+  const uint32_t np = 1u << (T - 1), bit = 1u << t0;
+  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
+    uint32_t i0 = ins0(i, t0);
+    if ((i0 & lcm) != lcv) continue;
+    float2 a0 = s[i0], a1 = s[i0 | bit];
+    float2 z = make_float2(0.f, 0.f);
+    s[i0] = cfma(g[1], a1, cfma(g[0], a0, z));
+    s[i0 | bit] = cfma(g[3], a1, cfma(g[2], a0, z));
+  }
+}
+
+__device__ void op_d1(float2* s, int T, int t0, uint32_t lcm, uint32_t lcv,
+                      const float2* m) {
+  const float2 d0 = __ldg(m), d1 = __ldg(m + 3);
+  const uint32_t N = 1u << T;
+  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+    if ((x & lcm) != lcv) continue;
+    s[x] = cmul((x >> t0) & 1 ? d1 : d0, s[x]);
+  }
+}
+
+__device__ void op_d2(float2* s, int T, int t0, int t1, uint32_t lcm,
+                      uint32_t lcv, const float2* m) {
+  float2 d[4] = {__ldg(m), __ldg(m + 5), __ldg(m + 10), __ldg(m + 15)};
+  const uint32_t N = 1u << T;
+  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+    if ((x & lcm) != lcv) continue;
+    int k = (((x >> t0) & 1) << 1) | ((x >> t1) & 1);
+    s[x] = cmul(d[k], s[x]);
+  }
+}
+
+__device__ __forceinline__ void quad_index(uint32_t i, int t0, int t1,
+                                           uint32_t* idx) {
+  int lo = t0 < t1 ? t0 : t1, hi = t0 < t1 ? t1 : t0;
+  uint32_t b = ins0(ins0(i, lo), hi);
+  idx[0] = b;
+  idx[1] = b | (1u << t1);
+  idx[2] = b | (1u << t0);
+  idx[3] = b | (1u << t0) | (1u << t1);
+}
+
+__device__ void op_g2(float2* s, int T, int t0, int t1, uint32_t lcm,
+                      uint32_t lcv, const float2* m) {
+  float2 g[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) g[i] = __ldg(m + i);
+  const uint32_t nq = 1u << (T - 2);
+  for (uint32_t i = threadIdx.x; i < nq; i += blockDim.x) {
+    uint32_t idx[4];
+    quad_index(i, t0, t1, idx);
+    if ((idx[0] & lcm) != lcv) continue;
+    float2 a[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] = s[idx[k]];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc = cfma(g[r * 4 + k], a[k], acc);
+      s[idx[r]] = acc;
+    }
+  }
+}
+
+// Adjoint step on one gate (tfq_adj_grad_op.cc:225-275): psi <- G^dag psi,
+// partial Re<lambda| dG_k P_c |psi> for each symbolic parameter,
+// lambda <- G^dag lambda.  Amplitudes whose controls do not match are left
+// alone, which is both the identity and the zero derivative there.
+template <int NQ>
+__device__ void op_b(float2* s, float2* l, int T, int t0, int t1, uint32_t lcm,
+                     uint32_t lcv, const float2* m, const float2* dm, int ngrad,
+                     float* part) {
+  constexpr int D = 1 << NQ;
+  float2 h[D * D];  // G^dagger
+#pragma unroll
+  for (int r = 0; r < D; ++r)
+#pragma unroll
+    for (int c = 0; c < D; ++c) h[r * D + c] = cconj(__ldg(m + c * D + r));
+  const uint32_t cnt = 1u << (T - NQ);
+  for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+    uint32_t idx[4];
+    if (NQ == 1) {
+      idx[0] = ins0(i, t0);
+      idx[1] = idx[0] | (1u << t0);
+    } else {
+      quad_index(i, t0, t1, idx);
+    }
+    if ((idx[0] & lcm) != lcv) continue;
+    float2 a[D], bb[D], p[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) { a[k] = s[idx[k]]; bb[k] = l[idx[k]]; }
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < D; ++k) acc = cfma(h[r * D + k], a[k], acc);
+      p[r] = acc;
+    }
+    for (int q = 0; q < ngrad; ++q) {
+      const float2* dq = dm + q * 16;
+      float acc = 0.f;
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        float2 dv = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < D; ++k) dv = cfma(__ldg(dq + r * D + k), p[k], dv);
+        acc += re_conj_mul(bb[r], dv);
+      }
+      part[q] += acc;
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < D; ++k) acc = cfma(h[r * D + k], bb[k], acc);
+      s[idx[r]] = p[r];
+      l[idx[r]] = acc;
+    }
+  }
+}
+
+// Block sum of `nv` per-thread values into red[buf][v][warp]; callers
+// __syncthreads() and read them afterwards.
+__device__ __forceinline__ void warp_partials(double* red, int buf,
+                                              const float* vals, int nv) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int v = 0; v < nv; ++v) {
+    float s = warp_sum(vals[v]);
+    if (lane == 0) red[(buf * 4 + v) * kWarps + w] = double(s);
+  }
+}
+
+__device__ __forceinline__ double red_total(const double* red, int buf, int v) {
+  double s = 0.0;
+  for (int w = 0; w < kWarps; ++w) s += red[(buf * 4 + v) * kWarps + w];
+  return s;
+}
+
+// Noisy channel on local bit t0 (qsim QuantumTrajectorySimulator semantics:
+// mixed-unitary channels draw the branch from fixed probabilities, others
+// from |K_k psi|^2, then renormalize).
+__device__ void op_channel(float2* s, int T, int t0, const DevChannel& ch,
+                           const float2* kraus, double u, double* red) {
+  const uint32_t np = 1u << (T - 1), bit = 1u << t0;
+  int k = ch.nk - 1;
+  float scale = 1.f;
+  if (ch.mixed_unitary) {
+    for (int j = 0; j < ch.nk; ++j)
+      if (u < ch.cum[j]) { k = j; break; }
+    if ((ch.ident_mask >> k) & 1) return;  // identity branch: nothing to do
+    scale = ch.scale[k];
+  } else {
+    float part[4] = {0.f, 0.f, 0.f, 0.f};
+    for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
+      uint32_t i0 = ins0(i, t0);
+      float2 a0 = s[i0], a1 = s[i0 | bit];
+      for (int j = 0; j < ch.nk; ++j) {
+        const float2* K = kraus + (ch.kraus + j) * 4;
+        float2 z = make_float2(0.f, 0.f);
+        float2 v0 = cfma(K[1], a1, cfma(K[0], a0, z));
+        float2 v1 = cfma(K[3], a1, cfma(K[2], a0, z));
+        part[j] += v0.x * v0.x + v0.y * v0.y + v1.x * v1.x + v1.y * v1.y;
+      }
+    }
+    warp_partials(red, 0, part, 4);
+    __syncthreads();
+    double p[4], tot = 0.0;
+    for (int j = 0; j < ch.nk; ++j) { p[j] = red_total(red, 0, j); tot += p[j]; }
+    double c = 0.0, target = u * tot;
+    for (int j = 0; j < ch.nk; ++j) {
+      c += p[j];
+      if (target < c && p[j] > 0.0) { k = j; break; }
+    }
+    if (p[k] <= 0.0) {
+      for (int j = ch.nk - 1; j >= 0; --j) if (p[j] > 0.0) { k = j; break; }
+    }
+    scale = p[k] > 0.0 ? float(1.0 / sqrt(p[k])) : 0.f;
+    __syncthreads();  // everyone has read red before it is reused
+  }
+  const float2* K = kraus + (ch.kraus + k) * 4;
+  float2 g[4];
+  for (int j = 0; j < 4; ++j) g[j] = make_float2(K[j].x * scale, K[j].y * scale);
+  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
+    uint32_t i0 = ins0(i, t0);
+    float2 a0 = s[i0], a1 = s[i0 | bit];
+    float2 z = make_float2(0.f, 0.f);
+    s[i0] = cfma(g[1], a1, cfma(g[0], a0, z));
+    s[i0 | bit] = cfma(g[3], a1, cfma(g[2], a0, z));
+  }
+}
+
+struct RowCtx {
+  int row;
+  int traj;           // trajectory (noisy), else 0
+  DevRow r;
+  DevProgram p;
+};
+
+// Applies ops [ob, oe) to a tile (psi s, lambda l) whose fixed global bits
+// are `base`; T = tile bits.  `rbuf` alternates the reduction buffer.
+template <int MODE>
+__device__ void run_ops(const BatchDevice& b, const RunArgs& a, const Smem& sm,
+                        const RowCtx& rc, uint32_t ob, uint32_t oe, float2* s,
+                        float2* l, int T, uint32_t base, int& rbuf) {
+  const float2* mats = a.mats + int64_t(rc.r.mat_offset) * 16;
+  for (uint32_t o = ob; o < oe; ++o) {
+    const DevOp op = b.ops[o];
+    const bool active = (base & op.gcmask) == op.gcval;
+    int ngrad = 0;
+    if (active) {
+      const float2* m = mats + int64_t(op.gate) * 16;
+      switch (op.type) {
+        case OP_G1: op_g1(s, T, op.t0, op.lcmask, op.lcval, m); break;
+        case OP_G2: op_g2(s, T, op.t0, op.t1, op.lcmask, op.lcval, m); break;
+        case OP_D1: op_d1(s, T, op.t0, op.lcmask, op.lcval, m); break;
+        case OP_D2: op_d2(s, T, op.t0, op.t1, op.lcmask, op.lcval, m); break;
+        case OP_B1:
+        case OP_B2: {
+          if (MODE == kModeAdjoint) {
+            float part[2] = {0.f, 0.f};
+            const float2* dm =
+                a.dmats + (int64_t(rc.r.dmat_offset) + (op.grad_slot < 0 ? 0 : op.grad_slot)) * 16;
+            if (op.type == OP_B1)
+              op_b<1>(s, l, T, op.t0, op.t1, op.lcmask, op.lcval, m, dm, op.ngrad, part);
+            else
+              op_b<2>(s, l, T, op.t0, op.t1, op.lcmask, op.lcval, m, dm, op.ngrad, part);
+            ngrad = op.ngrad;
+            if (ngrad) warp_partials(sm.red, rbuf, part, ngrad);
+          }
+          break;
+        }
+        case OP_CHAN: {
+          if (MODE == kModeNoisy) {
+            const DevChannel ch = b.channels[rc.p.channel_begin + op.gate];
+            double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(rc.traj),
+                                 op.gate);
+            op_channel(s, T, op.t0, ch, b.kraus, u, sm.red);
+          }
+          break;
+        }
+        default: break;
+      }
+    } else if (op.type == OP_B1 || op.type == OP_B2) {
+      // inactive on this tile: contributes zero partials
+      if (MODE == kModeAdjoint && op.ngrad) {
+        float part[2] = {0.f, 0.f};
+        warp_partials(sm.red, rbuf, part, op.ngrad);
+        ngrad = op.ngrad;
+      }
+    }
+    __syncthreads();
+    if (MODE == kModeAdjoint && ngrad && int(threadIdx.x) < ngrad) {
+      sm.grad[op.grad_slot + threadIdx.x] += red_total(sm.red, rbuf, threadIdx.x);
+    }
+    if (ngrad) rbuf ^= 1;
+  }
+}
+
+// Global offset of tile-local index i (bits 0..4 are global bits 0..4).
+__device__ __forceinline__ uint32_t tile_global(const uint32_t* hi, uint32_t i) {
+  return (i & 31u) | hi[i >> 5];
+}
+
+__device__ void build_hi_table(uint32_t* hi, uint32_t tile_mask) {
+  // local bits 5.. map to the set bits of tile_mask above bit 4, in order
+  for (uint32_t j = threadIdx.x; j < (1u << kHiBits); j += blockDim.x) {
+    uint32_t g = 0, rest = tile_mask & ~31u;
+    for (int k = 0; k < kHiBits; ++k) {
+      uint32_t lowest = rest & (~rest + 1u);
+      if ((j >> k) & 1) g |= lowest;
+      rest &= rest - 1u;
+    }
+    hi[j] = g;
+  }
+}
+
+// pdep of `t` into the bits of `mask` (tile index -> fixed global bits)
+__device__ __forceinline__ uint32_t deposit(uint32_t t, uint32_t mask) {
+  uint32_t r = 0;
+  for (int k = 0; mask; ++k) {
+    uint32_t lowest = mask & (~mask + 1u);
+    if ((t >> k) & 1) r |= lowest;
+    mask &= mask - 1u;
+  }
+  return r;
+}
+
+__device__ void tile_load(float2* dst, const float2* src, const uint32_t* hi,
+                          uint32_t base) {
+  const uint32_t n2 = 1u << (kTile - 1);
+  for (uint32_t k = threadIdx.x; k < n2; k += blockDim.x) {
+    uint32_t g = tile_global(hi, 2 * k) | base;
+    reinterpret_cast<float4*>(dst)[k] =
+        __ldcg(reinterpret_cast<const float4*>(src + g));
+  }
+}
+
+__device__ void tile_store(float2* dst, const float2* src, const uint32_t* hi,
+                           uint32_t base) {
+  const uint32_t n2 = 1u << (kTile - 1);
+  for (uint32_t k = threadIdx.x; k < n2; k += blockDim.x) {
+    uint32_t g = tile_global(hi, 2 * k) | base;
+    __stcg(reinterpret_cast<float4*>(dst + g),
+           reinterpret_cast<const float4*>(src)[k]);
+  }
+}
+
+__device__ void tile_zero(float2* dst, bool first_tile) {
+  const uint32_t n = 1u << kTile;
+  for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+    dst[k] = make_float2(k == 0 && first_tile ? 1.f : 0.f, 0.f);
+}
+
+// Runs passes [pb, pe) over a state.  Resident: `s_state` (and `s_lam`) hold
+// the whole state in shared memory.  Streamed: `g_psi` (and `g_lam`) are the
+// global states; tiles go through sm.psi / sm.lam.  `init` zero-initialises
+// the state to |0...0> during the first pass instead of loading it.
+template <int MODE>
+__device__ void run_passes(const BatchDevice& b, const RunArgs& a,
+                           const Smem& sm, const RowCtx& rc, uint32_t pb,
+                           uint32_t pe, float2* g_psi, float2* g_lam,
+                           bool init, int& rbuf) {
+  const int n = rc.p.n;
+  if (rc.p.resident) {
+    for (uint32_t p = pb; p < pe; ++p) {
+      const DevPass ps = b.passes[p];
+      run_ops<MODE>(b, a, sm, rc, ps.op_begin, ps.op_end, sm.psi, sm.lam, n, 0u,
+                    rbuf);
+    }
+    return;
+  }
+  const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+  for (uint32_t p = pb; p < pe; ++p) {
+    const DevPass ps = b.passes[p];
+    build_hi_table(sm.hi, ps.tile_mask);
+    __syncthreads();
+    const uint32_t outside = all & ~ps.tile_mask;
+    const uint32_t ntiles = 1u << (n - kTile);
+    for (uint32_t t = 0; t < ntiles; ++t) {
+      const uint32_t base = deposit(t, outside);
+      if (init && p == pb) tile_zero(sm.psi, base == 0);
+      else tile_load(sm.psi, g_psi, sm.hi, base);
+      if (MODE == kModeAdjoint && g_lam) tile_load(sm.lam, g_lam, sm.hi, base);
+      __syncthreads();
+      run_ops<MODE>(b, a, sm, rc, ps.op_begin, ps.op_end, sm.psi, sm.lam, kTile,
+                    base, rbuf);
+      tile_store(g_psi, sm.psi, sm.hi, base);
+      if (MODE == kModeAdjoint && g_lam) tile_store(g_lam, sm.lam, sm.hi, base);
+      __syncthreads();
+    }
+  }
+}
+
+// sum_x conj(psi_x) (P psi)_x accumulated per thread: float inner chunks,
+// double across chunks.
+__device__ void term_partial(const float2* psi, uint32_t N, const DevTerm& t,
+                             double* re, double* im) {
+  double dre = 0.0, dim = 0.0;
+  float fre = 0.f, fim = 0.f;
+  int cnt = 0;
+  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+    uint32_t y = x ^ t.flip;
+    float2 av = psi[x], bv = psi[y];
+    float sg = (__popc(y & t.zy) & 1) ? -1.f : 1.f;
+    fre = fmaf(sg, fmaf(av.x, bv.x, av.y * bv.y), fre);
+    fim = fmaf(sg, fmaf(av.x, bv.y, -av.y * bv.x), fim);
+    if (++cnt == 32) {
+      dre += fre; dim += fim; fre = fim = 0.f; cnt = 0;
+    }
+  }
+  *re = dre + fre;
+  *im = dim + fim;
+}
+
+// Expectation of every term of the row; `sink(op, value)` is called by
+// thread 0 once per term (in order) after the block reduction.
+template <class Sink>
+__device__ void measure_terms(const BatchDevice& b, const Smem& sm,
+                              const float2* psi, int n, uint32_t tb,
+                              uint32_t te, Sink&& sink, int& rbuf) {
+  const uint32_t N = 1u << n;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (uint32_t ti = tb; ti < te; ++ti) {
+    const DevTerm t = b.terms[ti];
+    if (t.identity) {
+      if (threadIdx.x == 0) sink(int(t.op), double(t.coef));
+      continue;
+    }
+    double re, im;
+    term_partial(psi, N, t, &re, &im);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) {
+      sm.red[(rbuf * 4 + 0) * kWarps + w] = re;
+      sm.red[(rbuf * 4 + 1) * kWarps + w] = im;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sre = red_total(sm.red, rbuf, 0), sim = red_total(sm.red, rbuf, 1);
+      double v;
+      switch (t.ny & 3) {
+        case 0: v = sre; break;
+        case 1: v = -sim; break;
+        case 2: v = -sre; break;
+        default: v = sim; break;
+      }
+      sink(int(t.op), double(t.coef) * v);
+    }
+    rbuf ^= 1;
+  }
+}
+
+// lambda = sum_j g_j sum_t c_t P_t psi, skipping |g_j c_t| < 1e-5
+// (AccumulateOperators, util_qsim.h:362-414).
+__device__ void init_lambda(const BatchDevice& b, const RunArgs& a,
+                            const RowCtx& rc, const float2* psi, float2* lam,
+                            int n) {
+  const uint32_t N = 1u << n;
+  const float* dg = a.dgrads + int64_t(rc.row) * b.num_ops;
+  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+    float2 v = make_float2(0.f, 0.f);
+    for (uint32_t ti = rc.r.term_begin; ti < rc.r.term_end; ++ti) {
+      const DevTerm t = b.terms[ti];
+      float w = dg[t.op] * t.coef;
+      if (fabsf(w) < 1e-5f) continue;
+      if (t.identity) {
+        float2 p = psi[x];
+        v.x = fmaf(w, p.x, v.x);
+        v.y = fmaf(w, p.y, v.y);
+        continue;
+      }
+      uint32_t y = x ^ t.flip;
+      float2 p = psi[y];
+      if (__popc(y & t.zy) & 1) w = -w;
+      switch (t.ny & 3) {  // multiply by i^ny
+        case 1: p = make_float2(-p.y, p.x); break;
+        case 2: p = make_float2(-p.x, -p.y); break;
+        case 3: p = make_float2(p.y, -p.x); break;
+        default: break;
+      }
+      v.x = fmaf(w, p.x, v.x);
+      v.y = fmaf(w, p.y, v.y);
+    }
+    lam[x] = v;
+  }
+}
+
+// Sampler: chunked |psi|^2 prefix sums in double, then per-sample search
+// (StateSpace::Sample semantics: index x with probability |psi_x|^2).
+__device__ void sample_state(const BatchDevice& b, const RunArgs& a,
+                             const Smem& sm, const RowCtx& rc,
+                             const float2* psi) {
+  const int n = rc.p.n, maxn = b.max_n, S = a.num_samples;
+  const uint32_t N = 1u << n;
+  const uint32_t nch = N < kMaxChunks ? N : kMaxChunks;
+  const uint32_t L = N / nch;
+  for (uint32_t c = threadIdx.x; c < nch; c += blockDim.x) {
+    double acc = 0.0;
+    float f = 0.f;
+    for (uint32_t j = 0; j < L; ++j) {
+      float2 v = psi[c * L + j];
+      f = fmaf(v.x, v.x, fmaf(v.y, v.y, f));
+      if ((j & 31) == 31) { acc += f; f = 0.f; }
+    }
+    sm.csum[c] = acc + f;
+  }
+  __syncthreads();
+  // inclusive scan (Hillis-Steele, nch <= 1024, 2 elements per thread)
+  for (uint32_t off = 1; off < nch; off <<= 1) {
+    double v0 = 0.0, v1 = 0.0;
+    uint32_t i0 = threadIdx.x, i1 = threadIdx.x + blockDim.x;
+    if (i0 < nch && i0 >= off) v0 = sm.csum[i0 - off];
+    if (i1 < nch && i1 >= off) v1 = sm.csum[i1 - off];
+    __syncthreads();
+    if (i0 < nch) sm.csum[i0] += v0;
+    if (i1 < nch) sm.csum[i1] += v1;
+    __syncthreads();
+  }
+  const double total = sm.csum[nch - 1];
+  int8_t* out = a.out_samples + int64_t(rc.row) * S * maxn;
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(s), 0x5A3Fu) * total;
+    uint32_t lo = 0, hi = nch - 1;
+    while (lo < hi) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (sm.csum[mid] > u) hi = mid; else lo = mid + 1;
+    }
+    double acc = lo ? sm.csum[lo - 1] : 0.0;
+    uint32_t x = lo * L, last_nz = x;
+    bool found = false;
+    for (uint32_t j = 0; j < L; ++j) {
+      float2 v = psi[lo * L + j];
+      double p = double(v.x) * v.x + double(v.y) * v.y;
+      if (p > 0.0) last_nz = lo * L + j;
+      acc += p;
+      if (acc > u && p > 0.0) { x = lo * L + j; found = true; break; }
+    }
+    if (!found) x = last_nz;
+    int8_t* o = out + int64_t(s) * maxn;
+    for (int c = 0; c < maxn; ++c) {
+      int k = maxn - 1 - c;  // sample bit k -> column maxn-k-1
+      o[c] = k >= n ? int8_t(-2) : int8_t((x >> k) & 1);
+    }
+  }
+}
+
+__device__ void init_resident(float2* s, int n) {
+  const uint32_t N = 1u << n;
+  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x)
+    s[x] = make_float2(x == 0 ? 1.f : 0.f, 0.f);
+}
+
+template <int MODE>
+__device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
+                        int row, int traj) {
+  RowCtx rc;
+  rc.row = row;
+  rc.traj = traj;
+  rc.r = b.rows[row];
+  rc.p = b.programs[rc.r.program];
+  const int n = rc.p.n;
+  const bool empty = n == 0 || rc.p.fwd_pass_begin == rc.p.fwd_pass_end;
+  int rbuf = 0;
+
+  if (MODE == kModeExpect || MODE == kModeNoisy) {
+    if (empty) {
+      if (MODE == kModeExpect)
+        for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x)
+          a.out_f[int64_t(row) * b.num_ops + j] = -2.f;
+      return;  // noisy empty rows are finalised on the host side kernel
+    }
+  }
+  if (MODE == kModeState && empty) {
+    float2* o = a.out_state + (int64_t(row) << b.max_n);
+    for (uint32_t x = threadIdx.x; x < (1u << b.max_n); x += blockDim.x)
+      o[x] = x == 0 ? make_float2(1.f, 0.f) : make_float2(-2.f, 0.f);
+    return;
+  }
+  if (MODE == kModeSample && empty) {
+    int8_t* o = a.out_samples + int64_t(row) * a.num_samples * b.max_n;
+    for (int64_t x = threadIdx.x; x < int64_t(a.num_samples) * b.max_n; x += blockDim.x)
+      o[x] = -2;
+    return;
+  }
+  if (MODE == kModeAdjoint && empty) return;
+
+  // global slots of this CTA (streamed rows)
+  float2* g_psi = a.work + int64_t(blockIdx.x) * a.slot_amps;
+  float2* g_lam = MODE == kModeAdjoint ? g_psi + (int64_t(1) << n) : nullptr;
+  if (MODE == kModeState && !rc.p.resident)
+    g_psi = a.out_state + (int64_t(row) << b.max_n);
+
+  // ---- forward ----
+  if (rc.p.resident) {
+    init_resident(sm.psi, n);
+    __syncthreads();
+    run_passes<MODE>(b, a, sm, rc, rc.p.fwd_pass_begin, rc.p.fwd_pass_end,
+                     nullptr, nullptr, true, rbuf);
+  } else {
+    run_passes<MODE>(b, a, sm, rc, rc.p.fwd_pass_begin, rc.p.fwd_pass_end,
+                     g_psi, nullptr, true, rbuf);
+  }
+  __syncthreads();
+  const float2* psi = rc.p.resident ? sm.psi : g_psi;
+
+  if (MODE == kModeExpect) {
+    float* out = a.out_f + int64_t(row) * b.num_ops;
+    for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x) out[j] = 0.f;
+    __syncthreads();
+    int cur = -1;
+    double acc = 0.0;
+    measure_terms(b, sm, psi, n, rc.r.term_begin, rc.r.term_end,
+                  [&](int op, double v) {
+                    if (op != cur) {
+                      if (cur >= 0) out[cur] = float(acc);
+                      cur = op;
+                      acc = 0.0;
+                    }
+                    acc += v;
+                  },
+                  rbuf);
+    if (threadIdx.x == 0 && cur >= 0) out[cur] = float(acc);
+  } else if (MODE == kModeNoisy) {
+    const int64_t base = int64_t(row) * b.num_ops;
+    int cur = -1;
+    double acc = 0.0;
+    auto flush = [&]() {
+      if (cur >= 0 && rc.traj < a.reps[base + cur]) atomicAdd(a.acc + base + cur, acc);
+    };
+    measure_terms(b, sm, psi, n, rc.r.term_begin, rc.r.term_end,
+                  [&](int op, double v) {
+                    if (op != cur) {
+                      flush();
+                      cur = op;
+                      acc = 0.0;
+                    }
+                    acc += v;
+                  },
+                  rbuf);
+    if (threadIdx.x == 0) flush();
+  } else if (MODE == kModeState) {
+    float2* o = a.out_state + (int64_t(row) << b.max_n);
+    const uint32_t N = 1u << n, M = 1u << b.max_n;
+    if (rc.p.resident)
+      for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) o[x] = sm.psi[x];
+    for (uint32_t x = N + threadIdx.x; x < M; x += blockDim.x)
+      o[x] = make_float2(-2.f, 0.f);
+  } else if (MODE == kModeSample) {
+    sample_state(b, a, sm, rc, psi);
+  } else if (MODE == kModeAdjoint) {
+    for (int k = threadIdx.x; k < rc.p.num_grads; k += blockDim.x) sm.grad[k] = 0.0;
+    float2* lam = rc.p.resident ? sm.lam : g_lam;
+    init_lambda(b, a, rc, psi, lam, n);
+    __syncthreads();
+    run_passes<MODE>(b, a, sm, rc, rc.p.bwd_pass_begin, rc.p.bwd_pass_end,
+                     rc.p.resident ? nullptr : g_psi,
+                     rc.p.resident ? nullptr : g_lam, false, rbuf);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float* out = a.out_f + int64_t(row) * b.num_symbols;
+      for (int k = 0; k < rc.p.num_grads; ++k) {
+        int col = b.grad_cols[rc.p.grad_col_begin + k];
+        out[col] += float(2.0 * sm.grad[k]);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kSimThreads, 1)
+simulate_kernel(BatchDevice b, RunArgs a, int state_amps, int nstates) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Smem sm;
+  sm.psi = reinterpret_cast<float2*>(smem_raw);
+  sm.lam = sm.psi + state_amps;
+  unsigned char* p = smem_raw + size_t(state_amps) * nstates * sizeof(float2);
+  sm.hi = reinterpret_cast<uint32_t*>(p);
+  p += (1u << kHiBits) * sizeof(uint32_t);
+  sm.red = reinterpret_cast<double*>(p);
+  p += 2 * 4 * kWarps * sizeof(double);
+  sm.csum = reinterpret_cast<double*>(p);
+  if (MODE == kModeSample) p += kMaxChunks * sizeof(double);
+  sm.grad = reinterpret_cast<double*>(p);
+
+  __shared__ int s_item;
+  const int64_t total = MODE == kModeNoisy ? a.total_traj : b.num_rows;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int64_t item = s_item;
+    __syncthreads();
+    if (item >= total) break;
+    if (MODE == kModeNoisy) {
+      int lo = 0, hi = b.num_rows - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (a.traj_prefix[mid] <= item) lo = mid; else hi = mid - 1;
+      }
+      run_row<MODE>(b, a, sm, lo, int(item - a.traj_prefix[lo]));
+    } else {
+      run_row<MODE>(b, a, sm, b.order[item], 0);
+    }
+  }
+}
+
+__global__ void noisy_finalize_kernel(BatchDevice b, RunArgs a) {
+  int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(b.num_rows) * b.num_ops) return;
+  int row = int(t / b.num_ops);
+  const DevRow r = b.rows[row];
+  const DevProgram p = b.programs[r.program];
+  if (p.n == 0 || p.fwd_pass_begin == p.fwd_pass_end) {
+    a.out_f[t] = -2.f;
+    return;
+  }
+  int reps = a.reps[t];
+  a.out_f[t] = reps > 0 ? float(a.acc[t] / double(reps)) : 0.f;
+}
+
+template <int MODE>
+const void* kernel_ptr() {
+  return reinterpret_cast<const void*>(&simulate_kernel<MODE>);
+}
+
+const void* kernel_for(int mode) {
+  switch (mode) {
+    case kModeExpect: return kernel_ptr<kModeExpect>();
+    case kModeState: return kernel_ptr<kModeState>();
+    case kModeSample: return kernel_ptr<kModeSample>();
+    case kModeAdjoint: return kernel_ptr<kModeAdjoint>();
+    default: return kernel_ptr<kModeNoisy>();
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_build_matrices(const BatchDevice& b, const RunArgs& a,
+                                  bool with_grads, cudaStream_t s) {
+  if (b.total_gates == 0) return cudaSuccess;
+  const int threads = 128;
+  int64_t blocks = (b.total_gates + threads - 1) / threads;
+  build_matrices_kernel<<<unsigned(blocks), threads, 0, s>>>(b, a, with_grads ? 1 : 0);
+  return cudaGetLastError();
+}
+
+int sim_state_amps(int max_resident_n, bool any_streamed) {
+  int amps = max_resident_n >= 0 ? (1 << max_resident_n) : 0;
+  if (any_streamed && amps < (1 << kTile)) amps = 1 << kTile;
+  return amps < 2 ? 2 : amps;
+}
+
+size_t sim_smem_bytes(int mode, int max_resident_n, bool any_streamed,
+                      int max_grads) {
+  size_t amps = size_t(sim_state_amps(max_resident_n, any_streamed));
+  int nstates = mode == kModeAdjoint ? 2 : 1;
+  size_t bytes = amps * nstates * sizeof(float2);
+  bytes += (1u << kHiBits) * sizeof(uint32_t);
+  bytes += 2 * 4 * kWarps * sizeof(double);
+  if (mode == kModeSample) bytes += kMaxChunks * sizeof(double);
+  if (mode == kModeAdjoint) bytes += size_t(max_grads) * sizeof(double);
+  return bytes;
+}
+
+int sim_grid_size(int mode, size_t smem) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const void* k = kernel_for(mode);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSimThreads, smem);
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
+}
+
+cudaError_t launch_simulate(int mode, const BatchDevice& b, const RunArgs& a,
+                            int grid, size_t smem, int state_amps,
+                            cudaStream_t s) {
+  const int nstates = mode == kModeAdjoint ? 2 : 1;
+  switch (mode) {
+    case kModeExpect:
+      simulate_kernel<kModeExpect><<<grid, kSimThreads, smem, s>>>(b, a, state_amps, nstates);
+      break;
+    case kModeState:
+      simulate_kernel<kModeState><<<grid, kSimThreads, smem, s>>>(b, a, state_amps, nstates);
+      break;
+    case kModeSample:
+      simulate_kernel<kModeSample><<<grid, kSimThreads, smem, s>>>(b, a, state_amps, nstates);
+      break;
+    case kModeAdjoint:
+      simulate_kernel<kModeAdjoint><<<grid, kSimThreads, smem, s>>>(b, a, state_amps, nstates);
+      break;
+    default:
+      simulate_kernel<kModeNoisy><<<grid, kSimThreads, smem, s>>>(b, a, state_amps, nstates);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_noisy_finalize(const BatchDevice& b, const RunArgs& a,
+                                  cudaStream_t s) {
+  int64_t total = int64_t(b.num_rows) * b.num_ops;
+  if (total == 0) return cudaSuccess;
+  noisy_finalize_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(b, a);
+  return cudaGetLastError();
+}
+
+}  // namespace tfqg

@@ -1,0 +1,122 @@
+// Data structures shared by the host compiler and the sm_103a kernels.
+//
+// State layout: one complex64 vector per circuit (or trajectory), float2
+// interleaved, amplitude index x whose bit b is qubit (n-1-b) in TFQ's
+// resolved qubit order (program_resolution.cc:120-131 sorts qubits; the
+// first qubit is the most significant bit, circuit_parser_qsim.cc:161 maps
+// qubit q to simulator index n-q-1).  Bit positions below are these "bits".
+#pragma once
+#include <stdint.h>
+
+namespace tfqg {
+
+// Gate kinds: the 16 gate ids of circuit_parser_qsim.cc:577-584.
+enum GateKind : uint8_t {
+  GK_I1 = 0, GK_I2, GK_XP, GK_YP, GK_ZP, GK_HP, GK_XXP, GK_YYP, GK_ZZP,
+  GK_CZP, GK_CNP, GK_SP, GK_ISP, GK_PXP, GK_FSIM, GK_PISP, GK_COUNT
+};
+
+// Channel kinds: the 8 channel ids of circuit_parser_qsim.cc:757-761.
+enum ChannelKind : uint8_t {
+  CK_DP = 0, CK_ADP, CK_GAD, CK_AD, CK_RST, CK_PD, CK_PF, CK_BF
+};
+
+// One gate of a distinct program, with its parameters still unbound.
+// a[i] is the constant from the proto, replaced per batch row by
+// symbol_values[row, src[i]] when src[i] >= 0 (ParseProtoArg,
+// circuit_parser_qsim.cc:53-82).  Parameter k (0 or 1) of the gate is the
+// raw value a[2k] times the scalar a[2k+1]; eigen gates use a[0]*a[1] as
+// exponent and a[2] as global shift, PhasedX uses a[4] as global shift.
+struct GateTemplate {
+  uint8_t kind;
+  uint8_t nq;          // 1 or 2 targets
+  uint8_t b0, b1;      // target bits; b0 is the first listed qubit (matrix MSB)
+  uint32_t cmask;      // control bits
+  uint32_t cval;       // required control values on those bits
+  float a[5];
+  int16_t src[5];      // symbol column of a[i], or -1
+  uint8_t ngrad;       // symbolic parameters = derivative slots
+  uint8_t gparam[2];   // parameter (0 or 1) differentiated by each slot
+  uint8_t pad;
+  int32_t grad_slot;   // first derivative slot of this gate, or -1
+};
+
+// Instruction executed by the simulation kernels on a tile of the state.
+enum OpType : uint8_t {
+  OP_G1 = 0,      // 2x2 matrix on local bit t0
+  OP_G2,          // 4x4 matrix on local bits (t0 = MSB, t1)
+  OP_D1,          // diagonal 2x2 (entries 0 and 3 of the matrix)
+  OP_D2,          // diagonal 4x4 (entries 0,5,10,15)
+  OP_B1,          // adjoint step on a 1-qubit gate (psi and lambda)
+  OP_B2,          // adjoint step on a 2-qubit gate
+  OP_CHAN,        // noisy channel on local bit t0
+  OP_NOP
+};
+
+struct DevOp {
+  uint8_t type;
+  uint8_t t0, t1;
+  uint8_t ngrad;
+  uint32_t gate;     // gate index within the program (matrix slot)
+  uint32_t lcmask, lcval;  // controls on tile-local bits
+  uint32_t gcmask, gcval;  // controls on bits outside the tile (global bits)
+  int32_t grad_slot;       // first derivative slot (OP_B*)
+  uint32_t pad;
+};
+static_assert(sizeof(DevOp) == 32, "DevOp layout");
+
+// A pass streams every tile of the state once: the tile holds the 2^T
+// amplitudes whose index bits outside `tile_mask` are fixed.
+struct DevPass {
+  uint32_t tile_mask;
+  uint32_t op_begin, op_end;
+  uint32_t pad;
+};
+
+// A Pauli term: P|y> = i^ny (-1)^popc(y & zy) |y ^ flip>  (bits).
+struct DevTerm {
+  uint32_t flip;
+  uint32_t zy;
+  float coef;          // coefficient_real (util_qsim.h:184-185)
+  uint16_t op;         // which pauli_sums column this term belongs to
+  uint8_t ny;          // number of Y factors mod 4
+  uint8_t identity;    // no Pauli factors: contributes coef directly
+};
+
+// A channel: up to 4 Kraus operators on one qubit.  Mixed-unitary channels
+// (every K_k proportional to a unitary) select their branch from fixed
+// probabilities; the others from |K_k psi|^2.
+struct DevChannel {
+  uint8_t kind;
+  uint8_t nk;
+  uint8_t mixed_unitary;
+  uint8_t ident_mask;  // bit k set when K_k is proportional to identity
+  uint32_t kraus;      // index of the first Kraus matrix (2x2 float2 x4)
+  double cum[4];       // cumulative branch probabilities (mixed unitary)
+  float scale[4];      // 1/sqrt(p_k) restoring unit norm (mixed unitary)
+};
+
+// Per distinct program: where its passes/ops/gates live in the packed arrays.
+struct DevProgram {
+  int32_t n;            // qubits (0 = empty program)
+  int32_t num_gates;    // gate templates (matrix slots)
+  int32_t num_grads;    // derivative slots
+  uint32_t grad_col_begin;                 // derivative slot -> symbol column
+  uint32_t fwd_pass_begin, fwd_pass_end;   // forward passes
+  uint32_t bwd_pass_begin, bwd_pass_end;   // adjoint backward passes
+  uint32_t gate_begin;                     // first GateTemplate
+  uint32_t channel_begin;                  // first DevChannel
+  int32_t resident;                        // state kept in shared memory
+  int32_t num_channels;
+};
+
+// Per batch row.
+struct DevRow {
+  int32_t program;       // index into DevProgram[]
+  int32_t n;
+  uint32_t term_begin, term_end;   // DevTerm range for this row's pauli_sums
+  uint64_t mat_offset;   // first matrix slot (float2[16] each) of this row
+  uint64_t dmat_offset;  // first derivative matrix slot of this row
+};
+
+}  // namespace tfqg

@@ -1,0 +1,233 @@
+"""Parity of the CUDA path (through the C ABI) against the complex128 oracle.
+
+Tolerances: expectations and gradients 1e-5 absolute for unit-scale
+observables (the reference's own op tests use atol=rtol=1e-5 against cirq,
+circuit_execution_ops_test.py:189); states 1e-5; gradient tolerances scale
+with the magnitude of the observable weights."""
+
+import numpy as np
+import pytest
+
+from quantum_gb300 import ops
+from quantum_gb300 import serialize as S
+from oracle import tfq_oracle as O
+from tests.circuits import CHANNELS, random_circuit, random_paulisum
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(rng, nqs, n_moments, n_symbols=6, n_ops=2, p_control=0.3,
+           grid=True):
+    names = [f"s{i}" for i in range(n_symbols)]
+    programs, psums = [], []
+    for n in nqs:
+        qs = S.GridQubit.rect(1, n) if grid else S.LineQubit.range(n)
+        c = random_circuit(qs, n_moments, rng, names, p_control=p_control)
+        programs.append(S.serialize_circuit(c))
+        psums.append([random_paulisum(qs, rng) for _ in range(n_ops)])
+    values = rng.uniform(-2, 2, size=(len(nqs), n_symbols)).astype(np.float32)
+    return programs, names, values, psums
+
+
+@pytest.mark.parametrize("nqs", [[1, 2, 3], [4, 5, 6], [8, 8], [10, 12],
+                                 [13], [14], [15], [16, 9]])
+def test_expectation_matches_oracle(nqs):
+    rng = np.random.default_rng(sum(nqs) * 7 + len(nqs))
+    programs, names, values, psums = _batch(rng, nqs, 6)
+    got = ops.tfq_simulate_expectation(programs, names, values, psums)
+    want = O.simulate_expectation(programs, names, values, psums)
+    np.testing.assert_allclose(got, want, atol=1e-5 * 8, rtol=0)
+
+
+@pytest.mark.parametrize("nqs", [[2, 3], [1, 5, 8], [14, 3], [15, 2]])
+def test_state_matches_oracle_with_padding(nqs):
+    rng = np.random.default_rng(100 + sum(nqs))
+    programs, names, values, _ = _batch(rng, nqs, 5, n_ops=0)
+    got = ops.tfq_simulate_state(programs, names, values)
+    want = O.simulate_state(programs, names, values)
+    assert got.shape == want.shape
+    np.testing.assert_allclose(got, want, atol=1e-5, rtol=0)
+
+
+def test_expectation_golden_util_qsim():
+    """util_qsim_test.cc:119-182: 0.1234 * {ZZ,...,YY} on a fixed state."""
+    q = S.LineQubit.range(2)
+    prog = S.serialize_circuit(S.Circuit([[S.XPow(q[0], 0.25)],
+                                          [S.CNOT(q[0], q[1])],
+                                          [S.YPow(q[1], 0.5)]]))
+    cases = [("ZZ", 0.0), ("ZX", 0.1234), ("ZY", 0.0), ("XZ", 0.0),
+             ("XX", 0.0), ("XY", -0.08725), ("YZ", 0.08725), ("YX", 0.0),
+             ("YY", 0.0)]
+    psums = [[S.serialize_paulisum([(0.1234, [(q[0], p[0]), (q[1], p[1])])])
+              for p, _ in cases]]
+    got = ops.tfq_simulate_expectation([prog], [], np.zeros((1, 0)), psums)
+    np.testing.assert_allclose(got[0], [v for _, v in cases], atol=1e-5)
+
+
+def test_expectation_empty_and_identity():
+    q = S.GridQubit.rect(1, 2)
+    prog = S.serialize_circuit(S.Circuit([[S.H(q[0])], [S.CNOT(q[0], q[1])]]))
+    empty = S.serialize_circuit(S.Circuit())
+    ps = S.serialize_paulisum([(0.5, []), (2.0, [(q[0], "Z"), (q[1], "Z")])])
+    got = ops.tfq_simulate_expectation([prog, empty], [], np.zeros((2, 0)),
+                                       [[ps], [ps]])
+    np.testing.assert_allclose(got, [[2.5], [-2.0]], atol=1e-6)
+
+
+@pytest.mark.parametrize("nqs,rule", [([2, 3, 4], 0), ([6, 7], 1),
+                                      ([10, 12], 0), ([13], 1), ([14], 0),
+                                      ([15, 5], 1)])
+def test_adj_grad_matches_oracle(nqs, rule):
+    rng = np.random.default_rng(1000 + sum(nqs) + rule)
+    programs, names, values, psums = _batch(rng, nqs, 5, n_symbols=5)
+    dg = rng.normal(size=(len(nqs), len(psums[0]))).astype(np.float32)
+    got = ops.tfq_adj_grad(programs, names, values, psums, dg, grad_rule=rule)
+    want = O.adj_grad(programs, names, values, psums, dg,
+                      grad_rule="fd" if rule == 0 else "analytic")
+    scale = max(1.0, float(np.abs(want).max()))
+    np.testing.assert_allclose(got, want, atol=2e-5 * scale, rtol=0)
+
+
+@pytest.mark.parametrize("case", [
+    ("GridQubit", [("XP", "alpha"), ("YP", "beta")], None,
+     ["alpha", "beta"], [0.123, 0.456], [-1.18392, 0.43281]),
+    ("GridQubit", [("XP", "alpha"), ("YP", "beta")], ("gamma", 0.5),
+     ["alpha", "beta", "gamma"], [0.123, 0.456, 0.789], [-2.100, -1.7412, -1.5120]),
+    ("GridQubit", [("XP", "alpha"), ("YP", "beta")], ("gamma", "gamma"),
+     ["alpha", "beta", "gamma"], [0.123, 0.456, 0.789], [-2.3484, -1.7532, -1.64264]),
+    ("LineQubit", [("XP", "alpha"), ("YP", "alpha")], (-0.56, "alpha"),
+     ["alpha", "beta", "gamma"], [0.123, 0.456, 0.789], [1.2993, 0, 0]),
+])
+def test_adj_grad_reference_goldens(case):
+    """tfq_adj_grad_op_test.py:265-397 (atol 1e-3 there)."""
+    qtype, singles, fsim, names, vals, want = case
+    q = S.GridQubit.rect(1, 2) if qtype == "GridQubit" else S.LineQubit.range(2)
+    moments = [[S.XPow(q[0], S.Symbol(singles[0][1]))],
+               [S.YPow(q[1], S.Symbol(singles[1][1]))],
+               [S.CNOT(q[0], q[1])]]
+    if fsim is not None:
+        th, ph = fsim
+        th = S.Symbol(th) if isinstance(th, str) else th
+        ph = S.Symbol(ph) if isinstance(ph, str) else ph
+        moments.append([S.FSim(q[0], q[1], th, ph)])
+    prog = S.serialize_circuit(S.Circuit(moments))
+    psums = [[S.serialize_paulisum([(1.0, [(q[0], "Z")])]),
+              S.serialize_paulisum([(1.0, [(q[1], "X")])])]]
+    got = ops.tfq_adj_grad([prog], names, np.array([vals], np.float32), psums,
+                           np.ones((1, 2), np.float32))
+    np.testing.assert_allclose(got[0], want, atol=1e-3)
+
+
+def test_adj_grad_empty_rows_and_no_ops():
+    q = S.GridQubit.rect(1, 2)
+    prog = S.serialize_circuit(S.Circuit([[S.XPow(q[0], S.Symbol("a"))]]))
+    empty = S.serialize_circuit(S.Circuit())
+    ps = S.serialize_paulisum([(1.0, [(q[0], "Z")])])
+    got = ops.tfq_adj_grad([prog, empty], ["a"], np.full((2, 1), 0.3, np.float32),
+                           [[ps], [ps]], np.ones((2, 1), np.float32))
+    assert got[1, 0] == 0.0
+    want = O.adj_grad([prog, empty], ["a"], np.full((2, 1), 0.3), [[ps], [ps]],
+                      np.ones((2, 1)))
+    np.testing.assert_allclose(got, want, atol=1e-5)
+
+
+def test_samples_bit_layout_and_padding():
+    """tfq_simulate_ops_test.py:467-492: X on every qubit -> all ones in the
+    trailing n columns, -2 in the leading max_n - n."""
+    for all_n in ([2, 3], [1, 5, 8]):
+        circuits = [S.serialize_circuit(S.Circuit(
+            [[S.X(q) for q in S.GridQubit.rect(1, n)]])) for n in all_n]
+        res = ops.tfq_simulate_samples(circuits, [], np.zeros((len(all_n), 0)),
+                                       [10])
+        m = max(all_n)
+        for i, n in enumerate(all_n):
+            exp = np.zeros((10, m))
+            exp[:, m - n:] = 1
+            exp[:, :m - n] = -2
+            np.testing.assert_array_equal(res[i], exp)
+
+
+@pytest.mark.parametrize("n", [3, 6, 15])
+def test_samples_distribution_chi2(n):
+    """Sampled bitstrings follow |psi|^2 (chi-squared, p > 1e-3)."""
+    from scipy import stats
+    rng = np.random.default_rng(77 + n)
+    qs = S.GridQubit.rect(1, n)
+    c = random_circuit(qs, 4, rng, [], p_control=0.2)
+    prog = S.serialize_circuit(c)
+    shots = 40000
+    res = ops.tfq_simulate_samples([prog], [], np.zeros((1, 0)), [shots], seed=1234)
+    bits = res[0].astype(np.int64)
+    idx = np.zeros(shots, dtype=np.int64)
+    for col in range(n):  # column col holds qubit col (big-endian index)
+        idx = (idx << 1) | bits[:, col]
+    (_, probs), = O.final_probabilities([prog], [], np.zeros((1, 0)))
+    counts = np.bincount(idx, minlength=2 ** n)
+    exp = probs * shots
+    # merge bins with fewer than 5 expected counts
+    order = np.argsort(exp)
+    ce, cc, acc_e, acc_c = [], [], 0.0, 0
+    for k in order:
+        acc_e += exp[k]
+        acc_c += counts[k]
+        if acc_e >= 5:
+            ce.append(acc_e)
+            cc.append(acc_c)
+            acc_e, acc_c = 0.0, 0
+    if acc_e > 0 and ce:
+        ce[-1] += acc_e
+        cc[-1] += acc_c
+    chi2 = float(np.sum((np.array(cc) - np.array(ce)) ** 2 / np.array(ce)))
+    p = stats.chi2.sf(chi2, max(len(ce) - 1, 1))
+    assert p > 1e-3, (chi2, len(ce), p)
+
+
+@pytest.mark.parametrize("n,channels", [(3, CHANNELS), (5, ["DP", "AD", "PD"]),
+                                        (4, ["GAD", "RST", "BF", "PF", "ADP"])])
+def test_noisy_expectation_vs_density_matrix(n, channels):
+    """Trajectory mean vs exact density matrix (the reference checks 5e-2 at
+    10000 trajectories, noise/noisy_expectation_op_test.py:224-274); here the
+    bound is 5 standard errors."""
+    rng = np.random.default_rng(500 + n)
+    qs = S.GridQubit.rect(1, n)
+    names = ["a", "b"]
+    progs, psums = [], []
+    for _ in range(2):
+        c = random_circuit(qs, 5, rng, names, p_control=0.2,
+                           channels=list(channels), p_channel=0.4)
+        progs.append(S.serialize_circuit(c))
+        psums.append([S.serialize_paulisum([(1.0, [(q, "Z")]) for q in qs]),
+                      random_paulisum(qs, rng)])
+    vals = rng.uniform(-1, 1, size=(2, 2)).astype(np.float32)
+    R = 20000
+    got = ops.noisy_expectation(progs, names, vals, psums,
+                                np.full((2, 2), R, np.int32), seed=7)
+    want = O.noisy_expectation_exact(progs, names, vals, psums)
+    # std of a bounded observable's trajectory mean <= sum|c| / sqrt(R)
+    bound = 5 * n / np.sqrt(R) + 1e-4
+    np.testing.assert_allclose(got, want, atol=bound, rtol=0)
+
+
+def test_noisy_without_noise_matches_expectation():
+    rng = np.random.default_rng(9)
+    programs, names, values, psums = _batch(rng, [4, 6], 5)
+    got = ops.noisy_expectation(programs, names, values, psums,
+                                np.full((2, 2), 3, np.int32), seed=1)
+    want = O.simulate_expectation(programs, names, values, psums)
+    np.testing.assert_allclose(got, want, atol=1e-4)
+
+
+def test_torch_autograd_cuda():
+    import torch
+    rng = np.random.default_rng(21)
+    programs, names, values, psums = _batch(rng, [5, 6, 7], 5)
+    from quantum_gb300.torch_ops import Expectation
+    layer = Expectation(programs, names, psums)
+    v = torch.tensor(values, device="cuda", requires_grad=True)
+    e = layer(v)
+    w = torch.tensor(rng.normal(size=e.shape).astype(np.float32), device="cuda")
+    (e * w).sum().backward()
+    want_e = O.simulate_expectation(programs, names, values, psums)
+    want_g = O.adj_grad(programs, names, values, psums, w.cpu().numpy())
+    np.testing.assert_allclose(e.detach().cpu().numpy(), want_e, atol=1e-4)
+    np.testing.assert_allclose(v.grad.cpu().numpy(), want_g, atol=1e-4)
