@@ -1,0 +1,111 @@
+"""The C ABI without a GPU: the library loads, exports every symbol the public
+header declares, and the host half (parse, resolve, validate) behaves like the
+reference's Compute() preamble.  No kernel is launched here."""
+
+import os
+import re
+
+import numpy as np
+import pytest
+
+from quantum_gb300 import _native, ops
+from quantum_gb300 import serialize as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "tfq_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(tfqg_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _native.lib()
+    names = _declared()
+    assert len(names) >= 12
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(_native.EXPORTED) <= set(names)
+
+
+def test_version():
+    assert b"sm_103a" in _native.lib().tfqg_version()
+
+
+def _prog(ops_):
+    return S.serialize_circuit(S.Circuit([[o] for o in ops_]))
+
+
+Q = S.GridQubit.rect(1, 3)
+
+
+@pytest.mark.parametrize("programs,names,psums,kind,pattern", [
+    ([b"\xff\xff"], [], None, 0, "Unparseable proto"),
+    ([_prog([S.XPow(Q[0], S.Symbol("a"))])], ["b"], None, 0,
+     "Could not find symbol in parameter map: a"),
+    ([_prog([S.depolarize(Q[0], 0.1)])], [], None, 0, "cirq.Channel"),
+    ([_prog([S.X(Q[0])])], [],
+     [[S.serialize_paulisum([(1.0, [(Q[2], "Z")])])]], 0,
+     "Pauli sum operating on qubits not found"),
+    ([S.serialize_circuit(S.Circuit([[S.Operation("ZZZ", {}, [Q[0]])]]))], [],
+     None, 0, "Could not parse gate id: ZZZ"),
+    ([S.serialize_circuit(S.Circuit([[S.Operation("XP", {"exponent": ("float", 1.0)},
+                                                  [Q[0]])]]))], [], None, 0,
+     "Could not find arg: exponent_scalar in op."),
+    ([S.serialize_circuit(S.Circuit([[S.Operation("XP", {}, [S.LineQubit(0)])
+                                      .controlled_by(Q[1])]]))], [], None, 0,
+     "Could not find arg"),
+    ([S.serialize_circuit(S.Circuit([[S.Operation("FOO", {}, [Q[0]])]]))], [], None, 2,
+     "Could not parse channel id: FOO"),
+])
+def test_host_validation_errors(programs, names, psums, kind, pattern):
+    with pytest.raises(_native.InvalidArgumentError, match=pattern):
+        ops.Batch(programs, names, psums, kind)
+
+
+def test_unparseable_qubit():
+    op = S.X(Q[0])
+    op.qubits = [type("Q", (), {"id": "a_b"})()]
+    with pytest.raises(_native.InvalidArgumentError, match="Unable to parse qubit: a_b"):
+        ops.Batch([S.serialize_circuit(S.Circuit([[op]]))], [], None)
+
+
+def test_mismatched_controls():
+    op = S.X(Q[0])
+    op.args["control_qubits"] = ("string", "0_1,0_2")
+    op.args["control_values"] = ("string", "1")
+    with pytest.raises(_native.InvalidArgumentError, match="Mistmatched number"):
+        ops.Batch([S.serialize_circuit(S.Circuit([[op]]))], [], None)
+
+
+def test_shape_checks_match_reference_messages():
+    p = _prog([S.X(Q[0])])
+    b = ops.Batch([p], ["a"], [[S.serialize_paulisum([(1.0, [(Q[0], "Z")])])]])
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="symbol names and value sizes do not match"):
+        b.expectation(np.zeros((1, 2), np.float32))
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="Number of circuits and symbol_values do not match"):
+        b.expectation(np.zeros((2, 1), np.float32))
+    with pytest.raises(_native.InvalidArgumentError, match="must be rank 2"):
+        b.expectation(np.zeros((3,), np.float32))
+    with pytest.raises(_native.InvalidArgumentError, match="programs must be rank 1"):
+        ops.Batch([[p]], [], None)
+    with pytest.raises(_native.InvalidArgumentError, match="pauli_sums must be rank 2"):
+        ops.Batch([p], [], [b"x"])
+
+
+def test_max_num_qubits_and_resolution_order():
+    line = S.LineQubit.range(3)
+    p1 = _prog([S.X(line[0]), S.CNOT(line[1], line[2])])
+    p2 = _prog([S.X(Q[0])])
+    empty = S.serialize_circuit(S.Circuit())
+    b = ops.Batch([p1, p2, empty], [], None)
+    assert b.max_num_qubits == 3
+    assert ops.Batch([empty], [], None).max_num_qubits == 0
+
+
+def test_empty_batch():
+    b = ops.Batch([], [], np.zeros((0, 0), dtype=object).tolist() or
+                  np.empty((0, 0), dtype=object))
+    assert b.batch_size == 0
