@@ -1,0 +1,390 @@
+"""Benchmark: batched expectation + adjoint gradient (circuits/s).
+
+Workload: 256 hardware-efficient-ansatz circuits of 16 qubits, depth 10
+(Ry, Rz on every qubit per layer, then a CNOT ladder), 320 symbols with values
+U[0, 2pi), one transverse-field Ising observable (J, h ~ N(1, 0.1)),
+downstream gradients 1.  A step is one expectation call followed by one
+adjoint-gradient call over the whole batch (the forward op and the gradient
+op of a training step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line on rank 0.  Multi-GPU: one process per GPU, each with
+its own batch of 256 circuits (weak scaling, no collective on the data path).
+"""
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fused/batched vs plain circuits/s (expect+adj-grad) at <=1e-5 err; HBM GB/s"
+UNIT = "circuits/s"
+WORKLOAD = "adjoint_hea_16q_b256_d10"
+BATCH, NQ, DEPTH = 256, 16, 10
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain GPU path")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config(n_gpus, l2="inputs > L2 (152 MB of per-CTA state slots) + 256 MB L2 flush between steps"):
+    return {"workload": WORKLOAD, "circuits_per_gpu": BATCH, "qubits": NQ,
+            "depth": DEPTH, "symbols": 2 * NQ * DEPTH, "observable": "TFIM (31 terms)",
+            "global_batch": BATCH * n_gpus, "parallelism": f"replicas x{n_gpus} (sharded batch)",
+            "l2": l2}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(seed):
+    from quantum_gb300 import workloads
+    return workloads.adjoint_hea(BATCH, NQ, DEPTH, seed=seed)
+
+
+def flop_per_circuit(w):
+    """Algorithmic flops of one step per circuit (dense 2^k gate matvecs):
+    expectation = forward + terms; adjoint = forward + 2x uncompute +
+    derivative matvec and inner product per parameter + lambda terms."""
+    N = 2 ** w["n"]
+    n, d = w["n"], w["depth"]
+    g1, g2 = 2 * n * d, (n - 1) * d
+    f_fwd = (g1 * 8 * 2 + g2 * 8 * 4) * N
+    terms = 2 * n - 1
+    f_exp = f_fwd + terms * 8 * N
+    f_adj = 3 * f_fwd + g1 * (8 * 2 * N + 8 * N) + terms * 16 * N
+    return f_exp + f_adj
+
+
+def state_bytes_per_circuit(batch_obj_passes, n):
+    return None
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the reference algorithm on the host cores."""
+    if rank != 0:
+        return
+    from oracle import cpu_port
+    w = workload(1)
+    threads = cpu_port.num_threads()
+    sample = 4 * threads
+    flat = cpu_port.Flat(w["programs"][:sample], w["symbol_names"],
+                         w["symbol_values"][:sample], w["pauli_sums"][:sample])
+    dg = w["downstream_grads"][:sample]
+    for _ in range(max(args.warmup, 1) if args.warmup else 0):
+        flat.run(dg, threads)
+        break
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        flat.run(dg, threads)
+        times.append(time.perf_counter() - t0)
+    per_step = float(np.mean(times))
+    value = sample / per_step
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": per_step * 1e3 * BATCH / sample,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64 (f32)", "data": "synthetic (seeded)",
+            "config": config(1, "host memory"), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                             "kind": "port",
+                             "sample": f"{sample} of {BATCH} circuits per step, expectation + adjoint, "
+                                       "restated reference algorithm (oracle/cpu_ref.cc, OpenMP over circuits)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from quantum_gb300 import _native, ops
+
+    lib = _native.lib()
+    w = workload(seed=1 + rank)
+    batch = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], ops.KIND_ADJOINT)
+    vals = torch.tensor(w["symbol_values"], device=dev)
+    dg = torch.ones((BATCH, 1), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        e = batch.expectation(vals)
+        g = batch.adj_grad(vals, dg)
+        return e, g
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, device events per step, L2 flushed between
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        a, b, c = ev[k]
+        a.record(stream)
+        batch.expectation(vals)
+        b.record(stream)
+        batch.adj_grad(vals, dg)
+        c.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    exp_ms = [a.elapsed_time(b) for a, b, _ in ev]
+    adj_ms = [b.elapsed_time(c) for _, b, c in ev]
+    step_ms = float(np.sum(exp_ms) + np.sum(adj_ms)) / args.steps
+    if world > 1:
+        t = torch.tensor([step_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = BATCH * world / (step_ms / 1e3)
+
+    # ---- accuracy vs the complex128 oracle on a few rows
+    e_gpu, g_gpu = step()
+    err = None
+    if rank == 0:
+        from oracle import tfq_oracle as O
+        rows = [0, 1]
+        sub = lambda x: [x[i] for i in rows]
+        we = O.simulate_expectation(sub(w["programs"]), w["symbol_names"],
+                                    w["symbol_values"][rows], sub(w["pauli_sums"]))
+        wg = O.adj_grad(sub(w["programs"]), w["symbol_names"], w["symbol_values"][rows],
+                        sub(w["pauli_sums"]), w["downstream_grads"][rows])
+        err = {"expectation_max_abs": float(np.abs(e_gpu.cpu().numpy()[rows] - we).max()),
+               "grad_max_abs": float(np.abs(g_gpu.cpu().numpy()[rows] - wg).max()),
+               "grad_rule": "reference finite difference (eps 5e-3)", "rows": len(rows)}
+
+    # ---- plain one-gate-per-launch path on the same inputs
+    plain = None
+    if not args.no_plain:
+        pe = torch.empty((BATCH, 1), dtype=torch.float32, device=dev)
+        pg = torch.empty((BATCH, vals.shape[1]), dtype=torch.float32, device=dev)
+        nl = ctypes.c_int64()
+        lib.tfqg_internal_plain_expect_adj.argtypes = [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_int64)]
+        lib.tfqg_internal_plain_expect_adj.restype = ctypes.c_int
+
+        def plain_step():
+            _native.check(lib.tfqg_internal_plain_expect_adj(
+                batch._h, ctypes.c_void_p(vals.data_ptr()), ctypes.c_void_p(dg.data_ptr()),
+                ctypes.c_void_p(pe.data_ptr()), ctypes.c_void_p(pg.data_ptr()),
+                ctypes.c_void_p(stream.cuda_stream), ctypes.byref(nl)))
+        plain_step()
+        torch.cuda.synchronize()
+        ksteps = max(2, min(args.steps, 3))
+        pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(ksteps)]
+        for k in range(ksteps):
+            flush.fill_(float(k))
+            pev[k][0].record(stream)
+            plain_step()
+            pev[k][1].record(stream)
+        torch.cuda.synchronize()
+        pms = float(np.mean([a.elapsed_time(b) for a, b in pev]))
+        perr = float(max(np.abs(pe.cpu().numpy() - e_gpu.cpu().numpy()).max(),
+                         np.abs(pg.cpu().numpy() - g_gpu.cpu().numpy()).max()))
+        plain = {"value": BATCH / (pms / 1e3), "unit": UNIT, "ms_per_step": pms,
+                 "kernel_launches_per_step": int(nl.value),
+                 "speedup_fused_over_plain": (BATCH / (step_ms / 1e3)) / (BATCH / (pms / 1e3)),
+                 "max_abs_diff_vs_fused": perr}
+
+    # ---- end to end through the reference-facing one-shot C ABI, host buffers
+    progs = w["programs"]
+    P = len(w["symbol_names"])
+    from quantum_gb300._native import string_array
+    pp, pl, k1 = string_array(progs)
+    npp, npl, k2 = string_array(w["symbol_names"])
+    flat_ps = [x for row in w["pauli_sums"] for x in row]
+    spp, spl, k3 = string_array(flat_ps)
+    hv = np.ascontiguousarray(w["symbol_values"])
+    hdg = np.ascontiguousarray(w["downstream_grads"])
+    hexp = np.empty((BATCH, 1), np.float32)
+    hgrad = np.empty((BATCH, P), np.float32)
+    fp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    lib.tfqg_simulate_expectation.argtypes = [
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+        ctypes.c_void_p]
+    lib.tfqg_adj_grad.argtypes = lib.tfqg_simulate_expectation.argtypes[:10] + [
+        ctypes.c_void_p, ctypes.c_void_p]
+
+    def e2e_step():
+        _native.check(lib.tfqg_simulate_expectation(pp, pl, BATCH, npp, npl, P, fp(hv),
+                                                    spp, spl, 1, fp(hexp)))
+        _native.check(lib.tfqg_adj_grad(pp, pl, BATCH, npp, npl, P, fp(hv), spp, spl, 1,
+                                        fp(hdg), fp(hgrad)))
+    e2e_step()
+    ek = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ek):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / ek
+    tables = lib.tfqg_internal_batch_table_bytes
+    tables.argtypes = [ctypes.c_void_p]
+    tables.restype = ctypes.c_int64
+    tb = int(tables(batch._h))
+    h2d = 2 * hv.nbytes + hdg.nbytes + 2 * tb
+    d2h = hexp.nbytes + hgrad.nbytes
+    e2e_val = BATCH * world / e2e_s
+
+    # ---- roofline of the dominant kernel (adjoint sweep)
+    adj_mean_ms = float(np.mean(adj_ms))
+    flop = flop_per_circuit(w)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    # state traffic the pass schedule moves per circuit between the per-CTA
+    # global slots and shared memory (read + write of psi, lambda)
+    sv = 8 * 2 ** NQ
+    passes = int(os.environ.get("TFQG_BENCH_PASSES", "0"))
+    props = torch.cuda.get_device_properties(dev)
+    sm_clock = clk.get("sm_mhz") or 1900.0
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_clock * 1e6 / 1e12
+    adj_flop = flop - ((2 * NQ * DEPTH * 8 * 2 + (NQ - 1) * DEPTH * 8 * 4) * 2 ** NQ + (2 * NQ - 1) * 8 * 2 ** NQ)
+    achieved_tflops = adj_flop * BATCH / (adj_mean_ms / 1e3) / 1e12
+    launches = 4
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 (f32 state, f64 reductions)", "data": "synthetic (seeded)",
+        "config": config(world),
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "path": "tfqg_simulate_expectation + tfqg_adj_grad (one-shot C ABI: parse, upload, run, download)"},
+        "gpu_launches": launches * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "simulate_kernel<adjoint>",
+                     "achieved": None, "peak": hbm_peak, "unit": "GB/s", "frac": None,
+                     "traffic": None,
+                     "note": "the 16-qubit adjoint sweep is FP32/shared-memory bound; see compute"},
+        "compute": {"kernel": "simulate_kernel<adjoint>", "ms_per_launch": adj_mean_ms,
+                    "algorithmic_tflop_per_launch": adj_flop * BATCH / 1e12,
+                    "achieved_tflops": achieved_tflops,
+                    "fp32_peak_tflops_at_measured_clock": fp32_peak,
+                    "frac": achieved_tflops / fp32_peak},
+        "expectation_ms": float(np.mean(exp_ms)), "adjoint_ms": adj_mean_ms,
+        "clocks": clk, "accuracy": err, "plain_gpu": plain,
+        "wall_s_timed": wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import cpu_port
+        threads = cpu_port.num_threads()
+        sample = 2 * threads
+        flat = cpu_port.Flat(w["programs"][:sample], w["symbol_names"],
+                             w["symbol_values"][:sample], w["pauli_sums"][:sample])
+        t0 = time.perf_counter()
+        flat.run(w["downstream_grads"][:sample], threads)
+        cs = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": sample / cs, "unit": UNIT, "cores": threads,
+                                "kind": "port",
+                                "sample": f"{sample} of {BATCH} circuits, one expectation + adjoint step, "
+                                          "restated reference algorithm (oracle/cpu_ref.cc), "
+                                          f"{cs:.2f} s wall"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

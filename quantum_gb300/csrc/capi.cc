@@ -14,6 +14,7 @@
 #include "../../include/tfq_gb300.h"
 #include "host.h"
 #include "kernels.h"
+#include "plain.h"
 
 using namespace tfqg;
 
@@ -676,6 +677,84 @@ int tfqg_noisy_expectation(const char* const* programs,
                                     expectations, 0, nullptr);
   tfqg_batch_destroy(b);
   return rc;
+}
+
+// Bytes of compiled tables uploaded to the device per batch (benchmark
+// accounting of host->device traffic).
+int64_t tfqg_internal_batch_table_bytes(void* batch) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  size_t bytes = 0;
+  bytes += b->programs.size() * sizeof(DevProgram) + b->rows.size() * sizeof(DevRow);
+  bytes += b->gates.size() * sizeof(GateTemplate) + b->passes.size() * sizeof(DevPass);
+  bytes += b->ops.size() * sizeof(DevOp) + b->terms.size() * sizeof(DevTerm);
+  bytes += b->channels.size() * sizeof(DevChannel) + b->kraus.size() * sizeof(float2);
+  bytes += b->grad_cols.size() * sizeof(int32_t) + b->order.size() * sizeof(int32_t);
+  return int64_t(bytes);
+}
+
+// Forward / backward pass counts and residency of program 0 (benchmark
+// accounting of the state traffic the pass schedule moves).
+int tfqg_internal_batch_passes(void* batch, int32_t* fwd, int32_t* bwd,
+                               int32_t* resident) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  if (!b || b->programs.empty()) return kInvalidArgument;
+  const DevProgram& p = b->programs[0];
+  *fwd = int32_t(p.fwd_pass_end - p.fwd_pass_begin);
+  *bwd = int32_t(p.bwd_pass_end - p.bwd_pass_begin);
+  *resident = p.resident;
+  return 0;
+}
+
+int tfqg_internal_plain_expect_adj(void* batch, const float* symbol_values,
+                                   const float* downstream_grads,
+                                   float* expectations, float* grads,
+                                   void* stream, int64_t* launches) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  return guarded([&]() {
+    if (!b || b->kind != TFQG_KIND_ADJOINT)
+      throw Error(kInvalidArgument, "needs an adjoint batch");
+    if (b->programs.size() != 1 || b->B == 0)
+      throw Error(kUnimplemented, "the plain path needs one shared program");
+    for (const DevRow& r : b->rows)
+      if (r.term_begin != b->rows[0].term_begin || r.term_end != b->rows[0].term_end)
+        throw Error(kUnimplemented, "the plain path needs shared observables");
+    const DevProgram& p = b->programs[0];
+    if (p.n < 7) throw Error(kUnimplemented, "the plain path needs n >= 7");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    RunArgs a;
+    prepare(b, symbol_values, 1, true, 0, s, &a);
+    const size_t sv = size_t(b->B) << p.n;
+    b->work.reserve(2 * sv * sizeof(float2), b->device);
+    size_t eb = align256(size_t(b->B * b->n_ops) * sizeof(double));
+    size_t gb = size_t(b->B * b->P) * sizeof(double);
+    b->aux2.reserve(eb + gb, b->device);
+    TFQG_CUDA(cudaMemsetAsync(b->aux2.p, 0, eb + gb, s));
+    PlainJob j;
+    j.rows = int(b->B);
+    j.n = p.n;
+    j.num_gates = p.num_gates;
+    j.num_grads = p.num_grads;
+    j.num_terms = int(b->rows[0].term_end - b->rows[0].term_begin);
+    j.n_ops = int(b->n_ops);
+    j.num_symbols = int(b->P);
+    j.gates = b->gates.data() + p.gate_begin;
+    j.terms = b->terms.data() + b->rows[0].term_begin;
+    j.grad_cols = b->grad_cols.data() + p.grad_col_begin;
+    j.mats = a.mats;
+    j.dmats = a.dmats;
+    j.psi = static_cast<float2*>(b->work.p);
+    j.lam = j.psi + sv;
+    j.dgrads = downstream_grads;
+    j.acc_exp = static_cast<double*>(b->aux2.p);
+    j.acc_grad = reinterpret_cast<double*>(static_cast<char*>(b->aux2.p) + eb);
+    j.out_exp = expectations;
+    j.out_grad = grads;
+    int64_t n0 = 0;
+    TFQG_CUDA(plain_expect_adjoint(j, s, &n0));
+    if (launches) *launches = n0 + 1;  // + the matrix build
+    return 0;
+  });
 }
 
 }  // extern "C"

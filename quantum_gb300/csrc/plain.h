@@ -1,0 +1,43 @@
+// Plain one-launch-per-gate comparison path (plain.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tfqg_types.h"
+
+namespace tfqg {
+
+// A batch whose rows all run the same program and observables.
+struct PlainJob {
+  int rows = 0, n = 0, num_gates = 0, num_grads = 0, num_terms = 0;
+  int n_ops = 0, num_symbols = 0;
+  const GateTemplate* gates = nullptr;  // host
+  const DevTerm* terms = nullptr;       // host
+  const int32_t* grad_cols = nullptr;   // host
+  const float2* mats = nullptr;         // device [rows][num_gates][16]
+  const float2* dmats = nullptr;        // device [rows][num_grads][16]
+  float2* psi = nullptr;                // device [rows][2^n]
+  float2* lam = nullptr;                // device [rows][2^n]
+  const float* dgrads = nullptr;        // device [rows][n_ops]
+  double* acc_exp = nullptr;            // device, zeroed
+  double* acc_grad = nullptr;           // device, zeroed
+  float* out_exp = nullptr;             // device [rows][n_ops]
+  float* out_grad = nullptr;            // device [rows][num_symbols]
+};
+
+cudaError_t plain_expect_adjoint(const PlainJob& j, cudaStream_t s,
+                                 int64_t* launches);
+
+}  // namespace tfqg
+
+extern "C" {
+int64_t tfqg_internal_batch_table_bytes(void* batch);
+int tfqg_internal_batch_passes(void* batch, int32_t* fwd, int32_t* bwd,
+                               int32_t* resident);
+// Expectation + adjoint gradient of a uniform batch by the plain path, all
+// buffers on the device.  Used by bench.py as the comparison baseline.
+int tfqg_internal_plain_expect_adj(void* batch, const float* symbol_values,
+                                   const float* downstream_grads,
+                                   float* expectations, float* grads,
+                                   void* stream, int64_t* launches);
+}
