@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain GPU path")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the one-shot C-ABI leg")
+    ap.add_argument("--batch", type=int, default=BATCH,
+                    help="circuits per GPU (default 256; smaller only for profiling)")
     return ap.parse_args()
 
 
@@ -113,9 +116,9 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload(seed):
+def workload(seed, batch=None):
     from quantum_gb300 import workloads
-    return workloads.adjoint_hea(BATCH, NQ, DEPTH, seed=seed)
+    return workloads.adjoint_hea(batch or BATCH, NQ, DEPTH, seed=seed)
 
 
 def flop_per_circuit(w):
@@ -187,7 +190,9 @@ def main():
     from quantum_gb300 import _native, ops
 
     lib = _native.lib()
-    w = workload(seed=1 + rank)
+    global BATCH
+    BATCH = args.batch
+    w = workload(seed=1 + rank, batch=BATCH)
     batch = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], ops.KIND_ADJOINT)
     vals = torch.tensor(w["symbol_values"], device=dev)
     dg = torch.ones((BATCH, 1), dtype=torch.float32, device=dev)
@@ -283,6 +288,13 @@ def main():
                  "max_abs_diff_vs_fused": perr}
 
     # ---- end to end through the reference-facing one-shot C ABI, host buffers
+    if args.no_e2e:
+        line = {"impl": "ours", "value": value, "ms_per_step": step_ms,
+                "expectation_ms": float(np.mean(exp_ms)),
+                "adjoint_ms": float(np.mean(adj_ms)), "batch": BATCH}
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     progs = w["programs"]
     P = len(w["symbol_names"])
     from quantum_gb300._native import string_array

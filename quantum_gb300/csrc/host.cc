@@ -579,6 +579,7 @@ void compile_program(const ProgramP& prog, const SymbolTable& names,
       if (lookup_gate(op.gate, &info)) {
         GateTemplate g;
         build_gate(op, info, n, names, *index, &g);
+        g.cls = classify_gate(g);
         if (kind == kJobAdjoint && g.ngrad > 0) {
           g.grad_slot = grad_slots;
           for (int k = 0; k < g.ngrad; ++k)
@@ -609,6 +610,62 @@ void compile_program(const ProgramP& prog, const SymbolTable& names,
 }
 
 // ---------------------------------------------------------------------------
+// gate structure classes
+// ---------------------------------------------------------------------------
+namespace {
+
+bool near(double a, double b) { return fabs(a - b) < 1e-9; }
+
+}  // namespace
+
+// Chooses the cheapest exact arithmetic for a gate.  Constant gates are
+// classified from their matrix (fp32 parameter products, as the device
+// computes them); symbolic gates from their kind.
+uint8_t classify_gate(const GateTemplate& g) {
+  bool symbolic = false;
+  for (int i = 0; i < 5; ++i) symbolic |= g.src[i] >= 0;
+  if (!symbolic) {
+    float e0, e1, e2;
+    effective_params(g, g.a[0], g.a[2], &e0, &e1, &e2);
+    Cx<double> m[16];
+    int nq = gate_matrix<double>(g.kind, e0, e1, e2, m);
+    int D = nq == 1 ? 2 : 4;
+    bool diag = true, ident = true, real = true;
+    for (int r = 0; r < D; ++r)
+      for (int c = 0; c < D; ++c) {
+        const Cx<double>& v = m[r * D + c];
+        if (r != c && (fabs(v.re) > 1e-9 || fabs(v.im) > 1e-9)) diag = false;
+        if (r == c && (!near(v.re, 1.0) || fabs(v.im) > 1e-9)) ident = false;
+        if (fabs(v.im) > 1e-9) real = false;
+      }
+    if (diag && ident) return GC_SKIP;
+    if (diag) return GC_DIAG;
+    if (nq == 1 && fabs(m[0].re) < 1e-9 && fabs(m[0].im) < 1e-9 &&
+        fabs(m[3].re) < 1e-9 && fabs(m[3].im) < 1e-9 && near(m[1].re, 1.0) &&
+        near(m[2].re, 1.0) && fabs(m[1].im) < 1e-9 && fabs(m[2].im) < 1e-9)
+      return GC_X;
+    if (nq == 2 && g.kind == GK_CNP) {
+      // exactly CNOT: identity on control 0, X on the target for control 1
+      bool cx = near(m[0].re, 1) && near(m[5].re, 1) && near(m[11].re, 1) &&
+                near(m[14].re, 1);
+      for (int i = 0; i < 16; ++i) {
+        if (i == 0 || i == 5 || i == 11 || i == 14) {
+          if (fabs(m[i].im) > 1e-9) cx = false;
+        } else if (fabs(m[i].re) > 1e-9 || fabs(m[i].im) > 1e-9) {
+          cx = false;
+        }
+      }
+      if (cx) return GC_X;
+    }
+    if (nq == 1 && real) return GC_REAL;
+    return GC_GENERAL;
+  }
+  if (g.kind == GK_ZP || g.kind == GK_ZZP || g.kind == GK_CZP) return GC_DIAG;
+  if (g.kind == GK_YP && g.src[2] < 0 && g.a[2] == -0.5f) return GC_REAL;
+  return GC_GENERAL;
+}
+
+// ---------------------------------------------------------------------------
 // pass planning
 // ---------------------------------------------------------------------------
 namespace {
@@ -625,6 +682,23 @@ int local_pos(uint32_t tile_mask, int bit) {
   return __builtin_popcount(tile_mask & low_mask(bit));
 }
 
+// Targets and controls of a gate as executed (CNOT runs as X on its target
+// controlled by its first qubit).
+void gate_bits(const GateTemplate& g, uint32_t* targets, uint32_t* cmask,
+               uint32_t* cval) {
+  *cmask = g.cmask;
+  *cval = g.cval;
+  if (g.cls == GC_X && g.nq == 2) {
+    *targets = 1u << g.b1;
+    *cmask |= 1u << g.b0;
+    *cval |= 1u << g.b0;
+    return;
+  }
+  *targets = (1u << g.b0) | (g.nq == 2 ? 1u << g.b1 : 0u);
+}
+
+// One op on tile-local bits; register fields are filled by the sub-pass
+// planner.
 DevOp make_op(const CompiledProgram& p, const PlanItem& it, uint32_t tile,
               bool backward, const std::vector<int>& chan_bits) {
   DevOp op;
@@ -632,18 +706,27 @@ DevOp make_op(const CompiledProgram& p, const PlanItem& it, uint32_t tile,
   op.grad_slot = -1;
   if (it.seq < 0) {
     int c = ~it.seq;
-    op.type = OP_CHAN;
+    op.type = p.channels[c].dev.mixed_unitary ? OP_MCH : OP_CHAN;
     op.t0 = uint8_t(local_pos(tile, chan_bits[c]));
     op.gate = uint32_t(c);
+    op.cls = GC_GENERAL;
     return op;
   }
   const GateTemplate& g = p.gates[it.seq];
+  uint32_t targets, cmask, cval;
+  gate_bits(g, &targets, &cmask, &cval);
   op.gate = uint32_t(it.seq);
-  op.t0 = uint8_t(local_pos(tile, g.b0));
-  op.t1 = g.nq == 2 ? uint8_t(local_pos(tile, g.b1)) : 0;
+  op.cls = g.cls;
+  bool one = g.nq == 1 || g.cls == GC_X;
+  if (g.cls == GC_X && g.nq == 2) {
+    op.t0 = uint8_t(local_pos(tile, g.b1));
+  } else {
+    op.t0 = uint8_t(local_pos(tile, g.b0));
+    op.t1 = g.nq == 2 ? uint8_t(local_pos(tile, g.b1)) : 0;
+  }
   for (int b = 0; b < 32; ++b) {
-    if (!(g.cmask >> b & 1)) continue;
-    uint32_t v = g.cval >> b & 1;
+    if (!(cmask >> b & 1)) continue;
+    uint32_t v = cval >> b & 1;
     if (tile >> b & 1) {
       int lp = local_pos(tile, b);
       op.lcmask |= 1u << lp;
@@ -654,15 +737,90 @@ DevOp make_op(const CompiledProgram& p, const PlanItem& it, uint32_t tile,
     }
   }
   if (backward) {
-    op.type = g.nq == 1 ? OP_B1 : OP_B2;
+    op.type = one ? OP_B1 : OP_B2;
     op.ngrad = g.ngrad;
     op.grad_slot = g.grad_slot;
-  } else if (gate_is_diagonal(g.kind)) {
-    op.type = g.nq == 1 ? OP_D1 : OP_D2;
   } else {
-    op.type = g.nq == 1 ? OP_G1 : OP_G2;
+    op.type = one ? OP_F1 : OP_F2;
   }
   return op;
+}
+
+uint32_t op_local_targets(const DevOp& op) {
+  if (op.type == OP_F2 || op.type == OP_B2) return (1u << op.t0) | (1u << op.t1);
+  return 1u << op.t0;
+}
+
+// Groups the ops of one pass (tile of T local bits) into sub-passes of
+// kRegBits register bits, reordering only ops that commute (disjoint bits).
+void plan_subpasses(const std::vector<DevOp>& in, int T, int regbits,
+                    std::vector<DevOp>* out) {
+  std::vector<DevOp> remaining = in;
+  const uint32_t all = low_mask(T);
+  while (!remaining.empty()) {
+    const DevOp& first = remaining.front();
+    if (first.type == OP_CHAN) {  // needs block-wide norms: stands alone
+      out->push_back(first);
+      remaining.erase(remaining.begin());
+      continue;
+    }
+    uint32_t R = 0, blocked = 0;
+    std::vector<DevOp> taken, rest;
+    for (const DevOp& op : remaining) {
+      uint32_t tg = op_local_targets(op);
+      uint32_t deps = tg | op.lcmask;
+      bool fits = op.type != OP_CHAN &&
+                  __builtin_popcount(R | tg) <= regbits &&
+                  taken.size() < size_t(kMaxSubOps) && !(deps & blocked);
+      if (fits) {
+        R |= tg;
+        taken.push_back(op);
+      } else {
+        rest.push_back(op);
+        blocked |= deps;
+      }
+    }
+    // pad the register set, preferring bits above the 5 lane bits so the
+    // warp's lanes keep walking consecutive amplitudes
+    for (int b = T - 1; b >= kLaneBits && __builtin_popcount(R) < regbits; --b)
+      if (!(R >> b & 1)) R |= 1u << b;
+    for (int b = 0; b < T && __builtin_popcount(R) < regbits; ++b)
+      if (!(R >> b & 1)) R |= 1u << b;
+    int rb[kRegBits] = {0, 0, 0, 0}, nr = 0, regidx[32];
+    for (int b = 0; b < 32; ++b) regidx[b] = -1;
+    for (int b = 0; b < T; ++b)
+      if (R >> b & 1) { regidx[b] = nr; rb[nr++] = b; }
+    DevOp h;
+    memset(&h, 0, sizeof(h));
+    h.type = OP_SUB;
+    h.t0 = uint8_t(regbits);
+    h.gate = uint32_t(taken.size());
+    h.lcmask = uint32_t(rb[0]) | uint32_t(rb[1]) << 8 | uint32_t(rb[2]) << 16 |
+               uint32_t(rb[3]) << 24;
+    h.grad_slot = -1;
+    out->push_back(h);
+    for (DevOp op : taken) {
+      uint32_t lm = op.lcmask, lv = op.lcval;
+      op.lcmask = 0;
+      op.lcval = 0;
+      for (int b = 0; b < T; ++b) {
+        if (!(lm >> b & 1)) continue;
+        uint32_t v = lv >> b & 1;
+        if (regidx[b] >= 0) {
+          op.kmask |= uint8_t(1u << regidx[b]);
+          op.kval |= uint8_t(v << regidx[b]);
+        } else {
+          op.lcmask |= 1u << b;
+          op.lcval |= v << b;
+        }
+      }
+      op.t0 = uint8_t(regidx[op.t0]);
+      if (op.type == OP_F2 || op.type == OP_B2) op.t1 = uint8_t(regidx[op.t1]);
+      out->push_back(op);
+    }
+    (void)all;
+    remaining.swap(rest);
+  }
 }
 
 void plan_sequence(const CompiledProgram& p, const std::vector<PlanItem>& items,
@@ -670,10 +828,14 @@ void plan_sequence(const CompiledProgram& p, const std::vector<PlanItem>& items,
                    const std::vector<int>& chan_bits,
                    std::vector<DevPass>* passes, std::vector<DevOp>* ops) {
   const int n = p.n;
-  const uint32_t all = low_mask(n);
   if (n <= tile_bits) {
+    // resident: the tile is the state, padded to at least kRegBits bits
+    const int T = n < kRegBits ? kRegBits : n;
+    const uint32_t all = low_mask(T);
+    std::vector<DevOp> flat;
+    for (const auto& it : items) flat.push_back(make_op(p, it, all, backward, chan_bits));
     DevPass ps{all, uint32_t(ops->size()), 0, 0};
-    for (const auto& it : items) ops->push_back(make_op(p, it, all, backward, chan_bits));
+    plan_subpasses(flat, T, backward ? kRegBitsAdjoint : kRegBits, ops);
     ps.op_end = uint32_t(ops->size());
     passes->push_back(ps);
     return;
@@ -699,8 +861,10 @@ void plan_sequence(const CompiledProgram& p, const std::vector<PlanItem>& items,
       }
     }
     for (int b = 0; b < n && __builtin_popcount(S) < tile_bits; ++b) S |= 1u << b;
+    std::vector<DevOp> flat;
+    for (const auto& it : taken) flat.push_back(make_op(p, it, S, backward, chan_bits));
     DevPass ps{S, uint32_t(ops->size()), 0, 0};
-    for (const auto& it : taken) ops->push_back(make_op(p, it, S, backward, chan_bits));
+    plan_subpasses(flat, tile_bits, backward ? kRegBitsAdjoint : kRegBits, ops);
     ps.op_end = uint32_t(ops->size());
     passes->push_back(ps);
     if (taken.empty()) throw Error(kInternal, "pass planner made no progress");
@@ -727,8 +891,12 @@ void plan_program(CompiledProgram* p, JobKind kind) {
     it.seq = s;
     if (s >= 0) {
       const GateTemplate& g = p->gates[s];
-      it.targets = (1u << g.b0) | (g.nq == 2 ? 1u << g.b1 : 0u);
-      it.deps = it.targets | g.cmask;
+      // identity gates do nothing, also in the adjoint (no parameters)
+      if (g.cls == GC_SKIP) continue;
+      uint32_t targets, cmask, cval;
+      gate_bits(g, &targets, &cmask, &cval);
+      it.targets = targets;
+      it.deps = targets | cmask;
     } else {
       int bit = p->channels[~s].bit;
       chan_bits[~s] = bit;

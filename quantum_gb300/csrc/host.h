@@ -65,6 +65,9 @@ constexpr int kResidentMaxSingle = 14;   // one state: 2^14 * 8 B = 128 KiB
 constexpr int kResidentMaxAdjoint = 13;  // psi and lambda: 2 * 64 KiB
 constexpr int kStreamTileBits = 13;      // tile of a streamed pass: 64 KiB
 constexpr int kLaneBits = 5;             // low bits every streamed tile holds
+constexpr int kRegBits = 4;              // register bits of a sub-pass (16 amps)
+constexpr int kRegBitsAdjoint = 3;       // adjoint sub-passes (psi + lambda)
+constexpr int kMaxSubOps = 32;           // ops per sub-pass (staging limit)
 
 struct ChannelHost {
   DevChannel dev;
@@ -100,6 +103,9 @@ void compile_program(const ProgramP& prog, const SymbolTable& names,
 // Resolves qubit ids (program_resolution.cc:90-186).
 int resolve_qubits(const ProgramP& prog,
                    std::unordered_map<std::string, int>* index);
+
+// Structure class (GateClass) of a gate template.
+uint8_t classify_gate(const GateTemplate& g);
 
 // Plans forward (and, for the adjoint, backward) passes.
 void plan_program(CompiledProgram* prog, JobKind kind);

@@ -150,148 +150,31 @@ __global__ void build_matrices_kernel(BatchDevice b, RunArgs a, int with_grads) 
 // ---------------------------------------------------------------------------
 // simulation building blocks (all threads of the CTA take part)
 // ---------------------------------------------------------------------------
+constexpr int kRB = 4;            // register bits of forward sub-passes
+constexpr int kRA = 1 << kRB;     // amplitudes per forward thread group
+constexpr int kMaxOps = 32;       // ops per sub-pass (host kMaxSubOps)
+
+// One sub-pass staged in shared memory: descriptors, matrices, derivative
+// matrices, and the per-warp gradient partials of its adjoint ops.
+struct Stage {
+  DevOp op[kMaxOps];
+  float2 mat[kMaxOps][16];
+  float2 dmat[kMaxOps][2][16];
+  float red[2][2 * kMaxOps][kWarps];  // [buffer][grad slot in sub-pass][warp]
+  int32_t red_slot[2][2 * kMaxOps];   // derivative slot of each entry
+  int32_t nred[2];
+};
+
 struct Smem {
   float2* psi;        // resident state / tile
   float2* lam;        // adjoint state / tile
   uint32_t* hi;       // tile-local high bits -> global offsets
-  double* red;        // [2][4][kWarps] reduction scratch
+  double* red;        // [2][4][kWarps] reduction scratch (terms, channels)
   double* csum;       // sampler chunk prefix sums
   double* grad;       // adjoint accumulators
+  Stage* st;
 };
 
-__device__ __forceinline__ void load4(const float2* __restrict__ m, float2* r) {
-#pragma unroll
-  for (int i = 0; i < 4; ++i) r[i] = __ldg(m + i);
-}
-
-__device__ void op_g1(float2* s, int T, int t0, uint32_t lcm, uint32_t lcv,
-                      const float2* m) {
-  float2 g[4];
-  load4(m, g);
-  const uint32_t np = 1u << (T - 1), bit = 1u << t0;
-  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
-    uint32_t i0 = ins0(i, t0);
-    if ((i0 & lcm) != lcv) continue;
-    float2 a0 = s[i0], a1 = s[i0 | bit];
-    float2 z = make_float2(0.f, 0.f);
-    s[i0] = cfma(g[1], a1, cfma(g[0], a0, z));
-    s[i0 | bit] = cfma(g[3], a1, cfma(g[2], a0, z));
-  }
-}
-
-__device__ void op_d1(float2* s, int T, int t0, uint32_t lcm, uint32_t lcv,
-                      const float2* m) {
-  const float2 d0 = __ldg(m), d1 = __ldg(m + 3);
-  const uint32_t N = 1u << T;
-  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
-    if ((x & lcm) != lcv) continue;
-    s[x] = cmul((x >> t0) & 1 ? d1 : d0, s[x]);
-  }
-}
-
-__device__ void op_d2(float2* s, int T, int t0, int t1, uint32_t lcm,
-                      uint32_t lcv, const float2* m) {
-  float2 d[4] = {__ldg(m), __ldg(m + 5), __ldg(m + 10), __ldg(m + 15)};
-  const uint32_t N = 1u << T;
-  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
-    if ((x & lcm) != lcv) continue;
-    int k = (((x >> t0) & 1) << 1) | ((x >> t1) & 1);
-    s[x] = cmul(d[k], s[x]);
-  }
-}
-
-__device__ __forceinline__ void quad_index(uint32_t i, int t0, int t1,
-                                           uint32_t* idx) {
-  int lo = t0 < t1 ? t0 : t1, hi = t0 < t1 ? t1 : t0;
-  uint32_t b = ins0(ins0(i, lo), hi);
-  idx[0] = b;
-  idx[1] = b | (1u << t1);
-  idx[2] = b | (1u << t0);
-  idx[3] = b | (1u << t0) | (1u << t1);
-}
-
-__device__ void op_g2(float2* s, int T, int t0, int t1, uint32_t lcm,
-                      uint32_t lcv, const float2* m) {
-  float2 g[16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i) g[i] = __ldg(m + i);
-  const uint32_t nq = 1u << (T - 2);
-  for (uint32_t i = threadIdx.x; i < nq; i += blockDim.x) {
-    uint32_t idx[4];
-    quad_index(i, t0, t1, idx);
-    if ((idx[0] & lcm) != lcv) continue;
-    float2 a[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) a[k] = s[idx[k]];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) acc = cfma(g[r * 4 + k], a[k], acc);
-      s[idx[r]] = acc;
-    }
-  }
-}
-
-// Adjoint step on one gate (tfq_adj_grad_op.cc:225-275): psi <- G^dag psi,
-// partial Re<lambda| dG_k P_c |psi> for each symbolic parameter,
-// lambda <- G^dag lambda.  Amplitudes whose controls do not match are left
-// alone, which is both the identity and the zero derivative there.
-template <int NQ>
-__device__ void op_b(float2* s, float2* l, int T, int t0, int t1, uint32_t lcm,
-                     uint32_t lcv, const float2* m, const float2* dm, int ngrad,
-                     float* part) {
-  constexpr int D = 1 << NQ;
-  float2 h[D * D];  // G^dagger
-#pragma unroll
-  for (int r = 0; r < D; ++r)
-#pragma unroll
-    for (int c = 0; c < D; ++c) h[r * D + c] = cconj(__ldg(m + c * D + r));
-  const uint32_t cnt = 1u << (T - NQ);
-  for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-    uint32_t idx[4];
-    if (NQ == 1) {
-      idx[0] = ins0(i, t0);
-      idx[1] = idx[0] | (1u << t0);
-    } else {
-      quad_index(i, t0, t1, idx);
-    }
-    if ((idx[0] & lcm) != lcv) continue;
-    float2 a[D], bb[D], p[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) { a[k] = s[idx[k]]; bb[k] = l[idx[k]]; }
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-      float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int k = 0; k < D; ++k) acc = cfma(h[r * D + k], a[k], acc);
-      p[r] = acc;
-    }
-    for (int q = 0; q < ngrad; ++q) {
-      const float2* dq = dm + q * 16;
-      float acc = 0.f;
-#pragma unroll
-      for (int r = 0; r < D; ++r) {
-        float2 dv = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int k = 0; k < D; ++k) dv = cfma(__ldg(dq + r * D + k), p[k], dv);
-        acc += re_conj_mul(bb[r], dv);
-      }
-      part[q] += acc;
-    }
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-      float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int k = 0; k < D; ++k) acc = cfma(h[r * D + k], bb[k], acc);
-      s[idx[r]] = p[r];
-      l[idx[r]] = acc;
-    }
-  }
-}
-
-// Block sum of `nv` per-thread values into red[buf][v][warp]; callers
-// __syncthreads() and read them afterwards.
 __device__ __forceinline__ void warp_partials(double* red, int buf,
                                               const float* vals, int nv) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -307,9 +190,421 @@ __device__ __forceinline__ double red_total(const double* red, int buf, int v) {
   return s;
 }
 
-// Noisy channel on local bit t0 (qsim QuantumTrajectorySimulator semantics:
-// mixed-unitary channels draw the branch from fixed probabilities, others
-// from |K_k psi|^2, then renormalize).
+// ---- register-level gate application (J: register bit of the target) ----
+#define TFQG_PAIRS(J)                                   \
+  _Pragma("unroll") for (int k = 0; k < NA; ++k)        \
+    if (!(k & (1 << (J))) && ((k & kmask) == kval))
+
+template <int J, int NA>
+__device__ __forceinline__ void f1_general(float2 (&a)[NA], const float2* m,
+                                           int kmask, int kval) {
+  const float2 m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
+  TFQG_PAIRS(J) {
+    const int k1 = k | (1 << J);
+    float2 x = a[k], y = a[k1], z = make_float2(0.f, 0.f);
+    a[k] = cfma(m1, y, cfma(m0, x, z));
+    a[k1] = cfma(m3, y, cfma(m2, x, z));
+  }
+}
+
+template <int J, int NA>
+__device__ __forceinline__ void f1_real(float2 (&a)[NA], const float2* m,
+                                        int kmask, int kval) {
+  const float m0 = m[0].x, m1 = m[1].x, m2 = m[2].x, m3 = m[3].x;
+  TFQG_PAIRS(J) {
+    const int k1 = k | (1 << J);
+    float2 x = a[k], y = a[k1];
+    a[k] = make_float2(fmaf(m0, x.x, m1 * y.x), fmaf(m0, x.y, m1 * y.y));
+    a[k1] = make_float2(fmaf(m2, x.x, m3 * y.x), fmaf(m2, x.y, m3 * y.y));
+  }
+}
+
+template <int J, int NA>
+__device__ __forceinline__ void f1_diag(float2 (&a)[NA], const float2* m,
+                                        int kmask, int kval) {
+  const float2 d0 = m[0], d1 = m[3];
+  TFQG_PAIRS(J) {
+    const int k1 = k | (1 << J);
+    a[k] = cmul(d0, a[k]);
+    a[k1] = cmul(d1, a[k1]);
+  }
+}
+
+template <int J, int NA>
+__device__ __forceinline__ void f1_x(float2 (&a)[NA], int kmask, int kval) {
+  TFQG_PAIRS(J) {
+    const int k1 = k | (1 << J);
+    float2 t = a[k];
+    a[k] = a[k1];
+    a[k1] = t;
+  }
+}
+
+#define TFQG_QUADS(J0, J1)                                               \
+  _Pragma("unroll") for (int k = 0; k < NA; ++k)                         \
+    if (!(k & ((1 << (J0)) | (1 << (J1)))) && ((k & kmask) == kval))
+
+template <int J0, int J1, int NA>
+__device__ __forceinline__ void f2_general(float2 (&a)[NA], const float2* m,
+                                           int kmask, int kval) {
+  TFQG_QUADS(J0, J1) {
+    const int idx[4] = {k, k | (1 << J1), k | (1 << J0), k | (1 << J0) | (1 << J1)};
+    float2 x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) x[q] = a[idx[q]];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc = cfma(m[r * 4 + q], x[q], acc);
+      a[idx[r]] = acc;
+    }
+  }
+}
+
+template <int J0, int J1, int NA>
+__device__ __forceinline__ void f2_diag(float2 (&a)[NA], const float2* m,
+                                        int kmask, int kval) {
+  const float2 d[4] = {m[0], m[5], m[10], m[15]};
+  TFQG_QUADS(J0, J1) {
+    const int idx[4] = {k, k | (1 << J1), k | (1 << J0), k | (1 << J0) | (1 << J1)};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a[idx[q]] = cmul(d[q], a[idx[q]]);
+  }
+}
+
+// Adjoint step on a 1-qubit gate: psi <- G^dag psi; part[q] += Re <lam| dG_q
+// psi>; lam <- G^dag lam (tfq_adj_grad_op.cc:225-275).
+template <int J, int CLS, int NA>
+__device__ __forceinline__ void b1(float2 (&a)[NA], float2 (&l)[NA],
+                                   const float2* m, const float2* dm, int ngrad,
+                                   int kmask, int kval, float* part) {
+  TFQG_PAIRS(J) {
+    const int k1 = k | (1 << J);
+    float2 x = a[k], y = a[k1], u = l[k], v = l[k1], p0, p1, q0, q1;
+    const float2 z = make_float2(0.f, 0.f);
+    if (CLS == GC_X) {
+      p0 = y; p1 = x; q0 = v; q1 = u;
+    } else if (CLS == GC_DIAG) {
+      const float2 d0 = cconj(m[0]), d1 = cconj(m[3]);
+      p0 = cmul(d0, x); p1 = cmul(d1, y);
+#pragma unroll
+      for (int g = 0; g < 2; ++g)
+        if (g < ngrad) {
+          const float2* D = dm + g * 16;
+          part[g] += re_conj_mul(u, cmul(D[0], p0)) + re_conj_mul(v, cmul(D[3], p1));
+        }
+      q0 = cmul(d0, u); q1 = cmul(d1, v);
+    } else if (CLS == GC_REAL) {
+      const float h0 = m[0].x, h1 = m[2].x, h2 = m[1].x, h3 = m[3].x;  // G^T
+      p0 = make_float2(fmaf(h0, x.x, h1 * y.x), fmaf(h0, x.y, h1 * y.y));
+      p1 = make_float2(fmaf(h2, x.x, h3 * y.x), fmaf(h2, x.y, h3 * y.y));
+#pragma unroll
+      for (int g = 0; g < 2; ++g)
+        if (g < ngrad) {
+          const float2* D = dm + g * 16;
+          float2 e0 = make_float2(fmaf(D[0].x, p0.x, D[1].x * p1.x), fmaf(D[0].x, p0.y, D[1].x * p1.y));
+          float2 e1 = make_float2(fmaf(D[2].x, p0.x, D[3].x * p1.x), fmaf(D[2].x, p0.y, D[3].x * p1.y));
+          part[g] += re_conj_mul(u, e0) + re_conj_mul(v, e1);
+        }
+      q0 = make_float2(fmaf(h0, u.x, h1 * v.x), fmaf(h0, u.y, h1 * v.y));
+      q1 = make_float2(fmaf(h2, u.x, h3 * v.x), fmaf(h2, u.y, h3 * v.y));
+    } else {
+      const float2 h0 = cconj(m[0]), h1 = cconj(m[2]), h2 = cconj(m[1]), h3 = cconj(m[3]);
+      p0 = cfma(h1, y, cfma(h0, x, z));
+      p1 = cfma(h3, y, cfma(h2, x, z));
+#pragma unroll
+      for (int g = 0; g < 2; ++g)
+        if (g < ngrad) {
+          const float2* D = dm + g * 16;
+          float2 e0 = cfma(D[1], p1, cfma(D[0], p0, z));
+          float2 e1 = cfma(D[3], p1, cfma(D[2], p0, z));
+          part[g] += re_conj_mul(u, e0) + re_conj_mul(v, e1);
+        }
+      q0 = cfma(h1, v, cfma(h0, u, z));
+      q1 = cfma(h3, v, cfma(h2, u, z));
+    }
+    a[k] = p0; a[k1] = p1; l[k] = q0; l[k1] = q1;
+  }
+}
+
+template <int J0, int J1, int CLS, int NA>
+__device__ __forceinline__ void b2(float2 (&a)[NA], float2 (&l)[NA],
+                                   const float2* m, const float2* dm, int ngrad,
+                                   int kmask, int kval, float* part) {
+  TFQG_QUADS(J0, J1) {
+    const int idx[4] = {k, k | (1 << J1), k | (1 << J0), k | (1 << J0) | (1 << J1)};
+    float2 x[4], u[4], p[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) { x[q] = a[idx[q]]; u[q] = l[idx[q]]; }
+    if (CLS == GC_DIAG) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) p[q] = cmul(cconj(m[5 * q]), x[q]);
+#pragma unroll
+      for (int g = 0; g < 2; ++g)
+        if (g < ngrad) {
+          const float2* D = dm + g * 16;
+          float acc = 0.f;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc += re_conj_mul(u[q], cmul(D[5 * q], p[q]));
+          part[g] += acc;
+        }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[idx[q]] = p[q];
+        l[idx[q]] = cmul(cconj(m[5 * q]), u[q]);
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc = cfma(cconj(m[q * 4 + r]), x[q], acc);
+        p[r] = acc;
+      }
+#pragma unroll
+      for (int g = 0; g < 2; ++g)
+        if (g < ngrad) {
+          const float2* D = dm + g * 16;
+          float acc = 0.f;
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            float2 dv = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dv = cfma(D[r * 4 + q], p[q], dv);
+            acc += re_conj_mul(u[r], dv);
+          }
+          part[g] += acc;
+        }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc = cfma(cconj(m[q * 4 + r]), u[q], acc);
+        a[idx[r]] = p[r];
+        l[idx[r]] = acc;
+      }
+    }
+  }
+}
+
+// Dispatch on the runtime register bits; every case is fully unrolled.
+#define TFQG_J3(F, ...)                        \
+  switch (j0) {                                \
+    case 0: F<0, NA>(__VA_ARGS__); break;      \
+    case 1: F<1, NA>(__VA_ARGS__); break;      \
+    default: F<2, NA>(__VA_ARGS__); break;     \
+  }
+#define TFQG_J4(F, ...)                        \
+  switch (j0) {                                \
+    case 0: F<0, NA>(__VA_ARGS__); break;      \
+    case 1: F<1, NA>(__VA_ARGS__); break;      \
+    case 2: F<2, NA>(__VA_ARGS__); break;      \
+    default: F<3, NA>(__VA_ARGS__); break;     \
+  }
+#define TFQG_J6(F, ...)                        \
+  switch (j0 * 4 + j1) {                       \
+    case 1: F<0, 1, NA>(__VA_ARGS__); break;   \
+    case 2: F<0, 2, NA>(__VA_ARGS__); break;   \
+    case 4: F<1, 0, NA>(__VA_ARGS__); break;   \
+    case 6: F<1, 2, NA>(__VA_ARGS__); break;   \
+    case 8: F<2, 0, NA>(__VA_ARGS__); break;   \
+    default: F<2, 1, NA>(__VA_ARGS__); break;  \
+  }
+#define TFQG_J12(F, ...)                       \
+  switch (j0 * 4 + j1) {                       \
+    case 1: F<0, 1, NA>(__VA_ARGS__); break;   \
+    case 2: F<0, 2, NA>(__VA_ARGS__); break;   \
+    case 3: F<0, 3, NA>(__VA_ARGS__); break;   \
+    case 4: F<1, 0, NA>(__VA_ARGS__); break;   \
+    case 6: F<1, 2, NA>(__VA_ARGS__); break;   \
+    case 7: F<1, 3, NA>(__VA_ARGS__); break;   \
+    case 8: F<2, 0, NA>(__VA_ARGS__); break;   \
+    case 9: F<2, 1, NA>(__VA_ARGS__); break;   \
+    case 11: F<2, 3, NA>(__VA_ARGS__); break;  \
+    case 12: F<3, 0, NA>(__VA_ARGS__); break;  \
+    case 13: F<3, 1, NA>(__VA_ARGS__); break;  \
+    default: F<3, 2, NA>(__VA_ARGS__); break;  \
+  }
+
+template <int J, int NA>
+__device__ __forceinline__ void b1_x(float2 (&a)[NA], float2 (&l)[NA],
+                                     const float2* m, const float2* dm, int ng,
+                                     int kmask, int kval, float* part) {
+  b1<J, GC_X, NA>(a, l, m, dm, ng, kmask, kval, part);
+}
+template <int J, int NA>
+__device__ __forceinline__ void b1_diag(float2 (&a)[NA], float2 (&l)[NA],
+                                        const float2* m, const float2* dm, int ng,
+                                        int kmask, int kval, float* part) {
+  b1<J, GC_DIAG, NA>(a, l, m, dm, ng, kmask, kval, part);
+}
+template <int J, int NA>
+__device__ __forceinline__ void b1_real(float2 (&a)[NA], float2 (&l)[NA],
+                                        const float2* m, const float2* dm, int ng,
+                                        int kmask, int kval, float* part) {
+  b1<J, GC_REAL, NA>(a, l, m, dm, ng, kmask, kval, part);
+}
+template <int J, int NA>
+__device__ __forceinline__ void b1_general(float2 (&a)[NA], float2 (&l)[NA],
+                                           const float2* m, const float2* dm,
+                                           int ng, int kmask, int kval,
+                                           float* part) {
+  b1<J, GC_GENERAL, NA>(a, l, m, dm, ng, kmask, kval, part);
+}
+template <int J0, int J1, int NA>
+__device__ __forceinline__ void b2_diag(float2 (&a)[NA], float2 (&l)[NA],
+                                        const float2* m, const float2* dm, int ng,
+                                        int kmask, int kval, float* part) {
+  b2<J0, J1, GC_DIAG, NA>(a, l, m, dm, ng, kmask, kval, part);
+}
+template <int J0, int J1, int NA>
+__device__ __forceinline__ void b2_general(float2 (&a)[NA], float2 (&l)[NA],
+                                           const float2* m, const float2* dm,
+                                           int ng, int kmask, int kval,
+                                           float* part) {
+  b2<J0, J1, GC_GENERAL, NA>(a, l, m, dm, ng, kmask, kval, part);
+}
+
+constexpr int kFwdRB = 4;  // register bits of forward sub-passes
+constexpr int kBwdRB = 3;  // register bits of adjoint sub-passes (psi + lambda)
+
+__device__ __forceinline__ void apply_forward(const DevOp& op, float2 (&a)[1 << kFwdRB],
+                                              const float2* m) {
+  constexpr int NA = 1 << kFwdRB;
+  const int j0 = op.t0, j1 = op.t1, kmask = op.kmask, kval = op.kval;
+  if (op.type == OP_F1 || op.type == OP_MCH) {
+    switch (op.cls) {
+      case GC_REAL: TFQG_J4(f1_real, a, m, kmask, kval); break;
+      case GC_DIAG: TFQG_J4(f1_diag, a, m, kmask, kval); break;
+      case GC_X: TFQG_J4(f1_x, a, kmask, kval); break;
+      case GC_SKIP: break;
+      default: TFQG_J4(f1_general, a, m, kmask, kval); break;
+    }
+  } else {
+    if (op.cls == GC_DIAG) {
+      TFQG_J12(f2_diag, a, m, kmask, kval);
+    } else {
+      TFQG_J12(f2_general, a, m, kmask, kval);
+    }
+  }
+}
+
+__device__ __forceinline__ void apply_backward(const DevOp& op,
+                                               float2 (&a)[1 << kBwdRB],
+                                               float2 (&l)[1 << kBwdRB],
+                                               const float2* m,
+                                               const float2* dm, float* part) {
+  constexpr int NA = 1 << kBwdRB;
+  const int j0 = op.t0, j1 = op.t1, kmask = op.kmask, kval = op.kval;
+  const int ng = op.ngrad;
+  if (op.type == OP_B1) {
+    switch (op.cls) {
+      case GC_X: TFQG_J3(b1_x, a, l, m, dm, ng, kmask, kval, part); break;
+      case GC_DIAG: TFQG_J3(b1_diag, a, l, m, dm, ng, kmask, kval, part); break;
+      case GC_REAL: TFQG_J3(b1_real, a, l, m, dm, ng, kmask, kval, part); break;
+      default: TFQG_J3(b1_general, a, l, m, dm, ng, kmask, kval, part); break;
+    }
+  } else {
+    if (op.cls == GC_DIAG) {
+      TFQG_J6(b2_diag, a, l, m, dm, ng, kmask, kval, part);
+    } else {
+      TFQG_J6(b2_general, a, l, m, dm, ng, kmask, kval, part);
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t group_base(uint32_t g, uint32_t rbits, int rb) {
+  // insert zeros at the register bits, lowest first
+  for (int j = 0; j < rb; ++j) g = ins0(g, int((rbits >> (8 * j)) & 0xFF));
+  return g;
+}
+
+// Forward sub-pass: each thread group loads the 16 amplitudes spanning the
+// register bits, applies the staged ops in registers, stores once.  Compiled
+// once and shared by every kernel mode.
+__device__ __noinline__ void exec_forward(float2* s, int T, uint32_t base,
+                                          const Stage* st, int nops,
+                                          uint32_t rbits) {
+  constexpr int RB = kFwdRB, NA = 1 << RB;
+  uint32_t off[NA];
+#pragma unroll
+  for (int k = 0; k < NA; ++k) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int j = 0; j < RB; ++j)
+      if (k >> j & 1) o |= 1u << ((rbits >> (8 * j)) & 0xFF);
+    off[k] = o;
+  }
+  const uint32_t ngroups = 1u << (T - RB);
+  for (uint32_t g = threadIdx.x; g < ngroups; g += blockDim.x) {
+    const uint32_t gb = group_base(g, rbits, RB);
+    float2 av[NA];
+#pragma unroll
+    for (int k = 0; k < NA; ++k) av[k] = s[gb | off[k]];
+    for (int i = 0; i < nops; ++i) {
+      const DevOp& op = st->op[i];
+      if ((gb & op.lcmask) == op.lcval && (base & op.gcmask) == op.gcval)
+        apply_forward(op, av, st->mat[i]);
+    }
+#pragma unroll
+    for (int k = 0; k < NA; ++k) s[gb | off[k]] = av[k];
+  }
+}
+
+// Adjoint sub-pass on psi (s) and lambda (l) with 3 register bits; per-op
+// gradient partials are warp-reduced into st->red[rbuf].
+__device__ __noinline__ void exec_backward(float2* s, float2* l, int T,
+                                           uint32_t base, Stage* st, int nops,
+                                           uint32_t rbits, int rbuf) {
+  constexpr int RB = kBwdRB, NA = 1 << RB;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t off[NA];
+#pragma unroll
+  for (int k = 0; k < NA; ++k) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int j = 0; j < RB; ++j)
+      if (k >> j & 1) o |= 1u << ((rbits >> (8 * j)) & 0xFF);
+    off[k] = o;
+  }
+  const uint32_t ngroups = 1u << (T - RB);
+  const uint32_t iters = (ngroups + blockDim.x - 1) / blockDim.x;
+  for (uint32_t it = 0; it < iters; ++it) {
+    const uint32_t g = it * blockDim.x + threadIdx.x;
+    const bool active = g < ngroups;
+    const uint32_t gb = group_base(active ? g : 0u, rbits, RB);
+    float2 av[NA], lv[NA];
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < NA; ++k) { av[k] = s[gb | off[k]]; lv[k] = l[gb | off[k]]; }
+    }
+    int gi = 0;
+    for (int i = 0; i < nops; ++i) {
+      const DevOp& op = st->op[i];
+      const bool on = active && (gb & op.lcmask) == op.lcval &&
+                      (base & op.gcmask) == op.gcval;
+      float part[2] = {0.f, 0.f};
+      if (on) apply_backward(op, av, lv, st->mat[i], &st->dmat[i][0][0], part);
+      for (int q = 0; q < op.ngrad; ++q) {
+        float v = warp_sum(part[q]);
+        if (lane == 0) {
+          if (it == 0) st->red[rbuf][gi + q][warp] = v;
+          else st->red[rbuf][gi + q][warp] += v;
+        }
+      }
+      gi += op.ngrad;
+    }
+    if (active) {
+#pragma unroll
+      for (int k = 0; k < NA; ++k) { s[gb | off[k]] = av[k]; l[gb | off[k]] = lv[k]; }
+    }
+  }
+}
+
+// Any channel on local bit t0 of a shared-memory state (qsim
+// QuantumTrajectorySimulator semantics: mixed-unitary channels draw the
+// branch from fixed probabilities, others from |K_k psi|^2, then renormalize).
 __device__ void op_channel(float2* s, int T, int t0, const DevChannel& ch,
                            const float2* kraus, double u, double* red) {
   const uint32_t np = 1u << (T - 1), bit = 1u << t0;
@@ -367,63 +662,93 @@ struct RowCtx {
   DevProgram p;
 };
 
-// Applies ops [ob, oe) to a tile (psi s, lambda l) whose fixed global bits
-// are `base`; T = tile bits.  `rbuf` alternates the reduction buffer.
+// Copies the sub-pass's descriptors and matrices into shared memory.
+template <int MODE>
+__device__ void stage_subpass(const BatchDevice& b, const RunArgs& a,
+                              const RowCtx& rc, Stage* st, uint32_t first,
+                              int nops, int buf) {
+  const float2* mats = a.mats + int64_t(rc.r.mat_offset) * 16;
+  const float2* dmats = a.dmats + int64_t(rc.r.dmat_offset) * 16;
+  const int per_op = MODE == kModeAdjoint ? 24 : 8;  // 16-byte chunks
+  for (int w = threadIdx.x; w < nops * per_op; w += blockDim.x) {
+    const int i = w / per_op, c = w % per_op;
+    const DevOp op = b.ops[first + i];
+    if (op.type == OP_MCH) {
+      // draw the branch once for the whole sub-pass; the identity branch
+      // becomes a no-op, any other branch a 2x2 matrix on the register bit
+      if (c == 0 && MODE == kModeNoisy) {
+        DevOp o2 = op;
+        const DevChannel ch = b.channels[rc.p.channel_begin + op.gate];
+        double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(rc.traj), op.gate);
+        int k = ch.nk - 1;
+        for (int j = 0; j < ch.nk; ++j)
+          if (u < ch.cum[j]) { k = j; break; }
+        o2.cls = ((ch.ident_mask >> k) & 1) ? uint8_t(GC_SKIP) : uint8_t(GC_GENERAL);
+        const float2* K = b.kraus + (ch.kraus + k) * 4;
+        for (int j = 0; j < 4; ++j)
+          st->mat[i][j] = make_float2(K[j].x * ch.scale[k], K[j].y * ch.scale[k]);
+        st->op[i] = o2;
+      }
+      continue;
+    }
+    if (c == 0) st->op[i] = op;
+    if (c < 8) {
+      reinterpret_cast<float4*>(st->mat[i])[c] =
+          __ldg(reinterpret_cast<const float4*>(mats + int64_t(op.gate) * 16) + c);
+    } else if (MODE == kModeAdjoint && op.grad_slot >= 0) {
+      const int g = (c - 8) / 8, cc = (c - 8) % 8;
+      if (g < op.ngrad)
+        reinterpret_cast<float4*>(st->dmat[i][g])[cc] = __ldg(
+            reinterpret_cast<const float4*>(dmats + int64_t(op.grad_slot + g) * 16) + cc);
+    }
+  }
+  if (MODE == kModeAdjoint && threadIdx.x == 0) {
+    int nr = 0;
+    for (int i = 0; i < nops; ++i) {
+      const DevOp op = b.ops[first + i];
+      if ((op.type == OP_B1 || op.type == OP_B2) && op.ngrad)
+        for (int g = 0; g < op.ngrad; ++g) st->red_slot[buf][nr++] = op.grad_slot + g;
+    }
+    st->nred[buf] = nr;
+  }
+}
+
+// Executes the instruction stream [ob, oe) on a tile: s (psi) and l
+// (lambda) hold 2^T amplitudes; `base` are the tile's fixed global bits.
 template <int MODE>
 __device__ void run_ops(const BatchDevice& b, const RunArgs& a, const Smem& sm,
                         const RowCtx& rc, uint32_t ob, uint32_t oe, float2* s,
                         float2* l, int T, uint32_t base, int& rbuf) {
-  const float2* mats = a.mats + int64_t(rc.r.mat_offset) * 16;
-  for (uint32_t o = ob; o < oe; ++o) {
-    const DevOp op = b.ops[o];
-    const bool active = (base & op.gcmask) == op.gcval;
-    int ngrad = 0;
-    if (active) {
-      const float2* m = mats + int64_t(op.gate) * 16;
-      switch (op.type) {
-        case OP_G1: op_g1(s, T, op.t0, op.lcmask, op.lcval, m); break;
-        case OP_G2: op_g2(s, T, op.t0, op.t1, op.lcmask, op.lcval, m); break;
-        case OP_D1: op_d1(s, T, op.t0, op.lcmask, op.lcval, m); break;
-        case OP_D2: op_d2(s, T, op.t0, op.t1, op.lcmask, op.lcval, m); break;
-        case OP_B1:
-        case OP_B2: {
-          if (MODE == kModeAdjoint) {
-            float part[2] = {0.f, 0.f};
-            const float2* dm =
-                a.dmats + (int64_t(rc.r.dmat_offset) + (op.grad_slot < 0 ? 0 : op.grad_slot)) * 16;
-            if (op.type == OP_B1)
-              op_b<1>(s, l, T, op.t0, op.t1, op.lcmask, op.lcval, m, dm, op.ngrad, part);
-            else
-              op_b<2>(s, l, T, op.t0, op.t1, op.lcmask, op.lcval, m, dm, op.ngrad, part);
-            ngrad = op.ngrad;
-            if (ngrad) warp_partials(sm.red, rbuf, part, ngrad);
-          }
-          break;
-        }
-        case OP_CHAN: {
-          if (MODE == kModeNoisy) {
-            const DevChannel ch = b.channels[rc.p.channel_begin + op.gate];
-            double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(rc.traj),
-                                 op.gate);
-            op_channel(s, T, op.t0, ch, b.kraus, u, sm.red);
-          }
-          break;
-        }
-        default: break;
+  Stage* st = sm.st;
+  uint32_t o = ob;
+  while (o < oe) {
+    const DevOp h = b.ops[o];
+    if (h.type == OP_CHAN) {
+      if (MODE == kModeNoisy) {
+        const DevChannel ch = b.channels[rc.p.channel_begin + h.gate];
+        double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(rc.traj), h.gate);
+        op_channel(s, T, h.t0, ch, b.kraus, u, sm.red);
       }
-    } else if (op.type == OP_B1 || op.type == OP_B2) {
-      // inactive on this tile: contributes zero partials
-      if (MODE == kModeAdjoint && op.ngrad) {
-        float part[2] = {0.f, 0.f};
-        warp_partials(sm.red, rbuf, part, op.ngrad);
-        ngrad = op.ngrad;
-      }
+      __syncthreads();
+      ++o;
+      continue;
     }
+    // sub-pass
+    const int nops = int(h.gate);
+    stage_subpass<MODE>(b, a, rc, st, o + 1, nops, rbuf);
     __syncthreads();
-    if (MODE == kModeAdjoint && ngrad && int(threadIdx.x) < ngrad) {
-      sm.grad[op.grad_slot + threadIdx.x] += red_total(sm.red, rbuf, threadIdx.x);
+    if (MODE == kModeAdjoint && h.t0 == kBwdRB)
+      exec_backward(s, l, T, base, st, nops, h.lcmask, rbuf);
+    else
+      exec_forward(s, T, base, st, nops, h.lcmask);
+    __syncthreads();
+    if (MODE == kModeAdjoint && int(threadIdx.x) < st->nred[rbuf]) {
+      double acc = 0.0;
+      for (int w = 0; w < kWarps; ++w) acc += st->red[rbuf][threadIdx.x][w];
+      sm.grad[st->red_slot[rbuf][threadIdx.x]] += acc;
     }
-    if (ngrad) rbuf ^= 1;
+    if (MODE == kModeAdjoint) rbuf ^= 1;
+    o += 1 + nops;
   }
 }
 
@@ -493,9 +818,10 @@ __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
                            bool init, int& rbuf) {
   const int n = rc.p.n;
   if (rc.p.resident) {
+    const int T = n < kRB ? kRB : n;  // tiny states are padded to 4 bits
     for (uint32_t p = pb; p < pe; ++p) {
       const DevPass ps = b.passes[p];
-      run_ops<MODE>(b, a, sm, rc, ps.op_begin, ps.op_end, sm.psi, sm.lam, n, 0u,
+      run_ops<MODE>(b, a, sm, rc, ps.op_begin, ps.op_end, sm.psi, sm.lam, T, 0u,
                     rbuf);
     }
     return;
@@ -591,6 +917,10 @@ __device__ void init_lambda(const BatchDevice& b, const RunArgs& a,
                             int n) {
   const uint32_t N = 1u << n;
   const float* dg = a.dgrads + int64_t(rc.row) * b.num_ops;
+  // tiny resident states are padded to 4 bits: the padding must be zero
+  if (rc.p.resident)
+    for (uint32_t x = N + threadIdx.x; x < (1u << kRB); x += blockDim.x)
+      lam[x] = make_float2(0.f, 0.f);
   for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
     float2 v = make_float2(0.f, 0.f);
     for (uint32_t ti = rc.r.term_begin; ti < rc.r.term_end; ++ti) {
@@ -679,7 +1009,7 @@ __device__ void sample_state(const BatchDevice& b, const RunArgs& a,
 }
 
 __device__ void init_resident(float2* s, int n) {
-  const uint32_t N = 1u << n;
+  const uint32_t N = 1u << (n < kRB ? kRB : n);
   for (uint32_t x = threadIdx.x; x < N; x += blockDim.x)
     s[x] = make_float2(x == 0 ? 1.f : 0.f, 0.f);
 }
@@ -809,6 +1139,8 @@ simulate_kernel(BatchDevice b, RunArgs a, int state_amps, int nstates) {
   sm.psi = reinterpret_cast<float2*>(smem_raw);
   sm.lam = sm.psi + state_amps;
   unsigned char* p = smem_raw + size_t(state_amps) * nstates * sizeof(float2);
+  sm.st = reinterpret_cast<Stage*>(p);
+  p += sizeof(Stage);
   sm.hi = reinterpret_cast<uint32_t*>(p);
   p += (1u << kHiBits) * sizeof(uint32_t);
   sm.red = reinterpret_cast<double*>(p);
@@ -881,7 +1213,7 @@ cudaError_t launch_build_matrices(const BatchDevice& b, const RunArgs& a,
 int sim_state_amps(int max_resident_n, bool any_streamed) {
   int amps = max_resident_n >= 0 ? (1 << max_resident_n) : 0;
   if (any_streamed && amps < (1 << kTile)) amps = 1 << kTile;
-  return amps < 2 ? 2 : amps;
+  return amps < kRA ? kRA : amps;
 }
 
 size_t sim_smem_bytes(int mode, int max_resident_n, bool any_streamed,
@@ -889,6 +1221,7 @@ size_t sim_smem_bytes(int mode, int max_resident_n, bool any_streamed,
   size_t amps = size_t(sim_state_amps(max_resident_n, any_streamed));
   int nstates = mode == kModeAdjoint ? 2 : 1;
   size_t bytes = amps * nstates * sizeof(float2);
+  bytes += sizeof(Stage);
   bytes += (1u << kHiBits) * sizeof(uint32_t);
   bytes += 2 * 4 * kWarps * sizeof(double);
   if (mode == kModeSample) bytes += kMaxChunks * sizeof(double);

@@ -37,31 +37,45 @@ struct GateTemplate {
   int16_t src[5];      // symbol column of a[i], or -1
   uint8_t ngrad;       // symbolic parameters = derivative slots
   uint8_t gparam[2];   // parameter (0 or 1) differentiated by each slot
-  uint8_t pad;
+  uint8_t cls;         // GateClass
   int32_t grad_slot;   // first derivative slot of this gate, or -1
 };
 
-// Instruction executed by the simulation kernels on a tile of the state.
+// Structure class of a gate matrix, chosen on the host; the kernels use the
+// cheapest arithmetic the class allows.
+enum GateClass : uint8_t {
+  GC_GENERAL = 0,  // dense complex matrix
+  GC_REAL,         // real entries (e.g. Ry: YPow with global shift -1/2)
+  GC_DIAG,         // diagonal (ZPow, ZZPow, CZPow, ...)
+  GC_X,            // exact Pauli X on one target (X, CNOT: control folded in)
+  GC_SKIP          // identity: no work
+};
+
+// Instruction stream of a pass.  Gates are grouped into sub-passes: an
+// OP_SUB header names 4 tile-local "register" bits and the number of ops that
+// follow; every thread loads the 16 amplitudes spanning those bits into
+// registers, applies the ops, and stores once.
 enum OpType : uint8_t {
-  OP_G1 = 0,      // 2x2 matrix on local bit t0
-  OP_G2,          // 4x4 matrix on local bits (t0 = MSB, t1)
-  OP_D1,          // diagonal 2x2 (entries 0 and 3 of the matrix)
-  OP_D2,          // diagonal 4x4 (entries 0,5,10,15)
-  OP_B1,          // adjoint step on a 1-qubit gate (psi and lambda)
-  OP_B2,          // adjoint step on a 2-qubit gate
-  OP_CHAN,        // noisy channel on local bit t0
-  OP_NOP
+  OP_SUB = 0,   // header: gate = #ops, lcmask = r0 | r1<<8 | r2<<16 | r3<<24
+  OP_F1,        // 1-qubit gate on register bit t0 (class cls)
+  OP_F2,        // 2-qubit gate on register bits t0 (matrix MSB), t1
+  OP_B1,        // adjoint step on a 1-qubit gate (psi and lambda)
+  OP_B2,        // adjoint step on a 2-qubit gate
+  OP_MCH,       // mixed-unitary channel on register bit t0
+  OP_CHAN,      // any channel on tile-local bit t0 (outside sub-passes)
 };
 
 struct DevOp {
   uint8_t type;
   uint8_t t0, t1;
   uint8_t ngrad;
-  uint32_t gate;     // gate index within the program (matrix slot)
-  uint32_t lcmask, lcval;  // controls on tile-local bits
+  uint32_t gate;     // gate (matrix slot) or channel index within the program
+  uint32_t lcmask, lcval;  // controls on tile-local bits outside the registers
   uint32_t gcmask, gcval;  // controls on bits outside the tile (global bits)
   int32_t grad_slot;       // first derivative slot (OP_B*)
-  uint32_t pad;
+  uint8_t cls;             // GateClass
+  uint8_t kmask, kval;     // controls on register bits
+  uint8_t pad;
 };
 static_assert(sizeof(DevOp) == 32, "DevOp layout");
 
