@@ -705,6 +705,27 @@ int tfqg_internal_batch_passes(void* batch, int32_t* fwd, int32_t* bwd,
   return 0;
 }
 
+// Sub-pass statistics of program 0: number of sub-pass headers and ops in
+// the forward and backward instruction streams (planner diagnostics).
+int tfqg_internal_batch_subpasses(void* batch, int32_t* fwd_subs,
+                                  int32_t* fwd_ops, int32_t* bwd_subs,
+                                  int32_t* bwd_ops) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  if (!b || b->programs.empty()) return kInvalidArgument;
+  const DevProgram& p = b->programs[0];
+  auto count = [&](uint32_t pb, uint32_t pe, int32_t* subs, int32_t* ops) {
+    *subs = 0;
+    *ops = 0;
+    for (uint32_t q = pb; q < pe; ++q)
+      for (uint32_t o = b->passes[q].op_begin; o < b->passes[q].op_end; ++o) {
+        if (b->ops[o].type == OP_SUB) ++*subs; else ++*ops;
+      }
+  };
+  count(p.fwd_pass_begin, p.fwd_pass_end, fwd_subs, fwd_ops);
+  count(p.bwd_pass_begin, p.bwd_pass_end, bwd_subs, bwd_ops);
+  return 0;
+}
+
 int tfqg_internal_plain_expect_adj(void* batch, const float* symbol_values,
                                    const float* downstream_grads,
                                    float* expectations, float* grads,

@@ -28,6 +28,11 @@
 namespace tfqg {
 namespace {
 
+// Dynamic shared memory of the simulation kernel (layout set up in
+// simulate_kernel); device functions address it by byte offset so every
+// access compiles to a shared-space load/store.
+extern __shared__ __align__(16) unsigned char smem_raw[];
+
 constexpr int kTile = 13;              // streamed tile bits (matches host)
 constexpr int kHiBits = kTile - 5;     // tile bits above the 5 lane bits
 constexpr int kMaxChunks = 1024;       // sampler prefix chunks
@@ -45,6 +50,17 @@ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y
 __device__ __forceinline__ uint32_t ins0(uint32_t i, int b) {
   return ((i >> b) << (b + 1)) | (i & ((1u << b) - 1u));
 }
+// Shared-memory position of amplitude x: the index nibbles above bit 3 are
+// XOR-folded into the low nibble, so the 16 lanes of a half warp that walk
+// any 4 index bits hit 16 distinct bank pairs.  Linear over GF(2):
+// swz(a ^ b) = swz(a) ^ swz(b); an involution.
+__device__ __forceinline__ uint32_t swz(uint32_t x) {
+  return x ^ ((x >> 4) & 15u) ^ ((x >> 8) & 15u) ^ ((x >> 12) & 15u);
+}
+__device__ __forceinline__ uint32_t sidx(uint32_t x, bool shared) {
+  return shared ? swz(x) : x;
+}
+
 // Re(conj(a) * b)
 __device__ __forceinline__ float re_conj_mul(float2 a, float2 b) {
   return fmaf(a.x, b.x, a.y * b.y);
@@ -156,8 +172,24 @@ constexpr int kMaxOps = 32;       // ops per sub-pass (host kMaxSubOps)
 
 // One sub-pass staged in shared memory: descriptors, matrices, derivative
 // matrices, and the per-warp gradient partials of its adjoint ops.
+// Packed op code (one 32-bit word per staged op):
+//   bits 0-2 type, 3-5 class, 6-7 j0, 8-9 j1, 10-13 kmask, 14-17 kval,
+//   18-19 ngrad, 20 has non-register controls, 21 single register control,
+//   22-23 that control's register bit, 24 its value.
+__host__ __device__ __forceinline__ uint32_t op_code(const DevOp& op) {
+  uint32_t km = op.kmask & 15u, kv = op.kval & 15u;
+  uint32_t single = km && !(km & (km - 1u));
+  uint32_t jc = 0;
+  if (single) { while (!((km >> jc) & 1u)) ++jc; }
+  uint32_t cv = single ? ((kv >> jc) & 1u) : 0u;
+  return uint32_t(op.type & 7) | uint32_t(op.cls & 7) << 3 | uint32_t(op.t0 & 3) << 6 |
+         uint32_t(op.t1 & 3) << 8 | km << 10 | kv << 14 | uint32_t(op.ngrad & 3) << 18 |
+         uint32_t((op.lcmask | op.gcmask) != 0) << 20 | single << 21 | jc << 22 | cv << 24;
+}
+
 struct Stage {
-  DevOp op[kMaxOps];
+  uint32_t code[kMaxOps];
+  uint32_t lcmask[kMaxOps], lcval[kMaxOps], gcmask[kMaxOps], gcval[kMaxOps];
   float2 mat[kMaxOps][16];
   float2 dmat[kMaxOps][2][16];
   float red[2][2 * kMaxOps][kWarps];  // [buffer][grad slot in sub-pass][warp]
@@ -190,123 +222,145 @@ __device__ __forceinline__ double red_total(const double* red, int buf, int v) {
   return s;
 }
 
-// ---- register-level gate application (J: register bit of the target) ----
-#define TFQG_PAIRS(J)                                   \
-  _Pragma("unroll") for (int k = 0; k < NA; ++k)        \
-    if (!(k & (1 << (J))) && ((k & kmask) == kval))
+// ---- register-level gate application ----
+// Every function reads `in` and writes every element of `out` (ping-pong
+// arrays): results land directly in their final registers, so consecutive
+// gates need no register shuffling.  J is the target's register bit.
+#define TFQG_PAIRS_IO(J, ...)                                           \
+  _Pragma("unroll") for (int k = 0; k < NA; ++k) {                      \
+    if (k & (1 << (J))) continue;                                       \
+    const int k1 = k | (1 << (J));                                      \
+    if ((k & kmask) == kval) { __VA_ARGS__ } else { out[k] = in[k]; out[k1] = in[k1]; } \
+  }
 
 template <int J, int NA>
-__device__ __forceinline__ void f1_general(float2 (&a)[NA], const float2* m,
-                                           int kmask, int kval) {
+__device__ __forceinline__ void f1_general(const float2 (&in)[NA], float2 (&out)[NA],
+                                           const float2* m, int kmask, int kval) {
   const float2 m0 = m[0], m1 = m[1], m2 = m[2], m3 = m[3];
-  TFQG_PAIRS(J) {
-    const int k1 = k | (1 << J);
-    float2 x = a[k], y = a[k1], z = make_float2(0.f, 0.f);
-    a[k] = cfma(m1, y, cfma(m0, x, z));
-    a[k1] = cfma(m3, y, cfma(m2, x, z));
-  }
+  const float2 z = make_float2(0.f, 0.f);
+  TFQG_PAIRS_IO(J, {
+    out[k] = cfma(m1, in[k1], cfma(m0, in[k], z));
+    out[k1] = cfma(m3, in[k1], cfma(m2, in[k], z));
+  })
 }
 
 template <int J, int NA>
-__device__ __forceinline__ void f1_real(float2 (&a)[NA], const float2* m,
-                                        int kmask, int kval) {
+__device__ __forceinline__ void f1_real(const float2 (&in)[NA], float2 (&out)[NA],
+                                        const float2* m, int kmask, int kval) {
   const float m0 = m[0].x, m1 = m[1].x, m2 = m[2].x, m3 = m[3].x;
-  TFQG_PAIRS(J) {
-    const int k1 = k | (1 << J);
-    float2 x = a[k], y = a[k1];
-    a[k] = make_float2(fmaf(m0, x.x, m1 * y.x), fmaf(m0, x.y, m1 * y.y));
-    a[k1] = make_float2(fmaf(m2, x.x, m3 * y.x), fmaf(m2, x.y, m3 * y.y));
-  }
+  TFQG_PAIRS_IO(J, {
+    const float2 x = in[k], y = in[k1];
+    out[k] = make_float2(fmaf(m0, x.x, m1 * y.x), fmaf(m0, x.y, m1 * y.y));
+    out[k1] = make_float2(fmaf(m2, x.x, m3 * y.x), fmaf(m2, x.y, m3 * y.y));
+  })
 }
 
 template <int J, int NA>
-__device__ __forceinline__ void f1_diag(float2 (&a)[NA], const float2* m,
-                                        int kmask, int kval) {
+__device__ __forceinline__ void f1_diag(const float2 (&in)[NA], float2 (&out)[NA],
+                                        const float2* m, int kmask, int kval) {
   const float2 d0 = m[0], d1 = m[3];
-  TFQG_PAIRS(J) {
-    const int k1 = k | (1 << J);
-    a[k] = cmul(d0, a[k]);
-    a[k1] = cmul(d1, a[k1]);
-  }
+  TFQG_PAIRS_IO(J, {
+    out[k] = cmul(d0, in[k]);
+    out[k1] = cmul(d1, in[k1]);
+  })
 }
 
 template <int J, int NA>
-__device__ __forceinline__ void f1_x(float2 (&a)[NA], int kmask, int kval) {
-  TFQG_PAIRS(J) {
-    const int k1 = k | (1 << J);
-    float2 t = a[k];
-    a[k] = a[k1];
-    a[k1] = t;
-  }
+__device__ __forceinline__ void f1_x(const float2 (&in)[NA], float2 (&out)[NA],
+                                     int kmask, int kval) {
+  TFQG_PAIRS_IO(J, {
+    out[k] = in[k1];
+    out[k1] = in[k];
+  })
 }
 
-#define TFQG_QUADS(J0, J1)                                               \
-  _Pragma("unroll") for (int k = 0; k < NA; ++k)                         \
-    if (!(k & ((1 << (J0)) | (1 << (J1)))) && ((k & kmask) == kval))
+// X on register bit J controlled by register bit C having value V.
+template <int J, int C, int V, int NA>
+__device__ __forceinline__ void f1_cx(const float2 (&in)[NA], float2 (&out)[NA]) {
+#pragma unroll
+  for (int k = 0; k < NA; ++k)
+    out[k] = (((k >> C) & 1) == V) ? in[k ^ (1 << J)] : in[k];
+}
+
+template <int NA>
+__device__ __forceinline__ void copy_regs(const float2 (&in)[NA], float2 (&out)[NA]) {
+#pragma unroll
+  for (int k = 0; k < NA; ++k) out[k] = in[k];
+}
+
+#define TFQG_QUADS_IO(J0, J1, ...)                                                \
+  _Pragma("unroll") for (int k = 0; k < NA; ++k) {                                \
+    if (k & ((1 << (J0)) | (1 << (J1)))) continue;                                \
+    const int idx[4] = {k, k | (1 << (J1)), k | (1 << (J0)), k | (1 << (J0)) | (1 << (J1))}; \
+    if ((k & kmask) == kval) { __VA_ARGS__ } else {                               \
+      _Pragma("unroll") for (int q = 0; q < 4; ++q) out[idx[q]] = in[idx[q]];     \
+    }                                                                             \
+  }
 
 template <int J0, int J1, int NA>
-__device__ __forceinline__ void f2_general(float2 (&a)[NA], const float2* m,
-                                           int kmask, int kval) {
-  TFQG_QUADS(J0, J1) {
-    const int idx[4] = {k, k | (1 << J1), k | (1 << J0), k | (1 << J0) | (1 << J1)};
-    float2 x[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) x[q] = a[idx[q]];
+__device__ __forceinline__ void f2_general(const float2 (&in)[NA], float2 (&out)[NA],
+                                           const float2* m, int kmask, int kval) {
+  TFQG_QUADS_IO(J0, J1, {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc = cfma(m[r * 4 + q], x[q], acc);
-      a[idx[r]] = acc;
+      for (int q = 0; q < 4; ++q) acc = cfma(m[r * 4 + q], in[idx[q]], acc);
+      out[idx[r]] = acc;
     }
-  }
+  })
 }
 
 template <int J0, int J1, int NA>
-__device__ __forceinline__ void f2_diag(float2 (&a)[NA], const float2* m,
-                                        int kmask, int kval) {
+__device__ __forceinline__ void f2_diag(const float2 (&in)[NA], float2 (&out)[NA],
+                                        const float2* m, int kmask, int kval) {
   const float2 d[4] = {m[0], m[5], m[10], m[15]};
-  TFQG_QUADS(J0, J1) {
-    const int idx[4] = {k, k | (1 << J1), k | (1 << J0), k | (1 << J0) | (1 << J1)};
+  TFQG_QUADS_IO(J0, J1, {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a[idx[q]] = cmul(d[q], a[idx[q]]);
-  }
+    for (int q = 0; q < 4; ++q) out[idx[q]] = cmul(d[q], in[idx[q]]);
+  })
 }
 
-// Adjoint step on a 1-qubit gate: psi <- G^dag psi; part[q] += Re <lam| dG_q
+// Adjoint step on a 1-qubit gate: psi <- G^dag psi; part[g] += Re <lam| dG_g
 // psi>; lam <- G^dag lam (tfq_adj_grad_op.cc:225-275).
-template <int J, int CLS, int NA>
-__device__ __forceinline__ void b1(float2 (&a)[NA], float2 (&l)[NA],
-                                   const float2* m, const float2* dm, int ngrad,
-                                   int kmask, int kval, float* part) {
-  TFQG_PAIRS(J) {
+template <int J, int CLS, int NA, int NG>
+__device__ __forceinline__ void b1(const float2 (&a)[NA], const float2 (&l)[NA],
+                                   float2 (&ao)[NA], float2 (&lo)[NA],
+                                   const float2* m, const float2* dm, int kmask,
+                                   int kval, float* part) {
+#pragma unroll
+  for (int k = 0; k < NA; ++k) {
+    if (k & (1 << J)) continue;
     const int k1 = k | (1 << J);
-    float2 x = a[k], y = a[k1], u = l[k], v = l[k1], p0, p1, q0, q1;
+    if ((k & kmask) != kval) {
+      ao[k] = a[k]; ao[k1] = a[k1]; lo[k] = l[k]; lo[k1] = l[k1];
+      continue;
+    }
+    const float2 x = a[k], y = a[k1], u = l[k], v = l[k1];
     const float2 z = make_float2(0.f, 0.f);
+    float2 p0, p1, q0, q1;
     if (CLS == GC_X) {
       p0 = y; p1 = x; q0 = v; q1 = u;
     } else if (CLS == GC_DIAG) {
       const float2 d0 = cconj(m[0]), d1 = cconj(m[3]);
       p0 = cmul(d0, x); p1 = cmul(d1, y);
 #pragma unroll
-      for (int g = 0; g < 2; ++g)
-        if (g < ngrad) {
-          const float2* D = dm + g * 16;
-          part[g] += re_conj_mul(u, cmul(D[0], p0)) + re_conj_mul(v, cmul(D[3], p1));
-        }
+      for (int g = 0; g < NG; ++g) {
+        const float2* D = dm + g * 16;
+        part[g] += re_conj_mul(u, cmul(D[0], p0)) + re_conj_mul(v, cmul(D[3], p1));
+      }
       q0 = cmul(d0, u); q1 = cmul(d1, v);
     } else if (CLS == GC_REAL) {
       const float h0 = m[0].x, h1 = m[2].x, h2 = m[1].x, h3 = m[3].x;  // G^T
       p0 = make_float2(fmaf(h0, x.x, h1 * y.x), fmaf(h0, x.y, h1 * y.y));
       p1 = make_float2(fmaf(h2, x.x, h3 * y.x), fmaf(h2, x.y, h3 * y.y));
 #pragma unroll
-      for (int g = 0; g < 2; ++g)
-        if (g < ngrad) {
-          const float2* D = dm + g * 16;
-          float2 e0 = make_float2(fmaf(D[0].x, p0.x, D[1].x * p1.x), fmaf(D[0].x, p0.y, D[1].x * p1.y));
-          float2 e1 = make_float2(fmaf(D[2].x, p0.x, D[3].x * p1.x), fmaf(D[2].x, p0.y, D[3].x * p1.y));
-          part[g] += re_conj_mul(u, e0) + re_conj_mul(v, e1);
-        }
+      for (int g = 0; g < NG; ++g) {
+        const float2* D = dm + g * 16;
+        float2 e0 = make_float2(fmaf(D[0].x, p0.x, D[1].x * p1.x), fmaf(D[0].x, p0.y, D[1].x * p1.y));
+        float2 e1 = make_float2(fmaf(D[2].x, p0.x, D[3].x * p1.x), fmaf(D[2].x, p0.y, D[3].x * p1.y));
+        part[g] += re_conj_mul(u, e0) + re_conj_mul(v, e1);
+      }
       q0 = make_float2(fmaf(h0, u.x, h1 * v.x), fmaf(h0, u.y, h1 * v.y));
       q1 = make_float2(fmaf(h2, u.x, h3 * v.x), fmaf(h2, u.y, h3 * v.y));
     } else {
@@ -314,26 +368,33 @@ __device__ __forceinline__ void b1(float2 (&a)[NA], float2 (&l)[NA],
       p0 = cfma(h1, y, cfma(h0, x, z));
       p1 = cfma(h3, y, cfma(h2, x, z));
 #pragma unroll
-      for (int g = 0; g < 2; ++g)
-        if (g < ngrad) {
-          const float2* D = dm + g * 16;
-          float2 e0 = cfma(D[1], p1, cfma(D[0], p0, z));
-          float2 e1 = cfma(D[3], p1, cfma(D[2], p0, z));
-          part[g] += re_conj_mul(u, e0) + re_conj_mul(v, e1);
-        }
+      for (int g = 0; g < NG; ++g) {
+        const float2* D = dm + g * 16;
+        float2 e0 = cfma(D[1], p1, cfma(D[0], p0, z));
+        float2 e1 = cfma(D[3], p1, cfma(D[2], p0, z));
+        part[g] += re_conj_mul(u, e0) + re_conj_mul(v, e1);
+      }
       q0 = cfma(h1, v, cfma(h0, u, z));
       q1 = cfma(h3, v, cfma(h2, u, z));
     }
-    a[k] = p0; a[k1] = p1; l[k] = q0; l[k1] = q1;
+    ao[k] = p0; ao[k1] = p1; lo[k] = q0; lo[k1] = q1;
   }
 }
 
-template <int J0, int J1, int CLS, int NA>
-__device__ __forceinline__ void b2(float2 (&a)[NA], float2 (&l)[NA],
-                                   const float2* m, const float2* dm, int ngrad,
-                                   int kmask, int kval, float* part) {
-  TFQG_QUADS(J0, J1) {
+template <int J0, int J1, int CLS, int NA, int NG>
+__device__ __forceinline__ void b2(const float2 (&a)[NA], const float2 (&l)[NA],
+                                   float2 (&ao)[NA], float2 (&lo)[NA],
+                                   const float2* m, const float2* dm, int kmask,
+                                   int kval, float* part) {
+#pragma unroll
+  for (int k = 0; k < NA; ++k) {
+    if (k & ((1 << J0) | (1 << J1))) continue;
     const int idx[4] = {k, k | (1 << J1), k | (1 << J0), k | (1 << J0) | (1 << J1)};
+    if ((k & kmask) != kval) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { ao[idx[q]] = a[idx[q]]; lo[idx[q]] = l[idx[q]]; }
+      continue;
+    }
     float2 x[4], u[4], p[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) { x[q] = a[idx[q]]; u[q] = l[idx[q]]; }
@@ -341,18 +402,17 @@ __device__ __forceinline__ void b2(float2 (&a)[NA], float2 (&l)[NA],
 #pragma unroll
       for (int q = 0; q < 4; ++q) p[q] = cmul(cconj(m[5 * q]), x[q]);
 #pragma unroll
-      for (int g = 0; g < 2; ++g)
-        if (g < ngrad) {
-          const float2* D = dm + g * 16;
-          float acc = 0.f;
+      for (int g = 0; g < NG; ++g) {
+        const float2* D = dm + g * 16;
+        float acc = 0.f;
 #pragma unroll
-          for (int q = 0; q < 4; ++q) acc += re_conj_mul(u[q], cmul(D[5 * q], p[q]));
-          part[g] += acc;
-        }
+        for (int q = 0; q < 4; ++q) acc += re_conj_mul(u[q], cmul(D[5 * q], p[q]));
+        part[g] += acc;
+      }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        a[idx[q]] = p[q];
-        l[idx[q]] = cmul(cconj(m[5 * q]), u[q]);
+        ao[idx[q]] = p[q];
+        lo[idx[q]] = cmul(cconj(m[5 * q]), u[q]);
       }
     } else {
 #pragma unroll
@@ -363,53 +423,37 @@ __device__ __forceinline__ void b2(float2 (&a)[NA], float2 (&l)[NA],
         p[r] = acc;
       }
 #pragma unroll
-      for (int g = 0; g < 2; ++g)
-        if (g < ngrad) {
-          const float2* D = dm + g * 16;
-          float acc = 0.f;
+      for (int g = 0; g < NG; ++g) {
+        const float2* D = dm + g * 16;
+        float acc = 0.f;
 #pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            float2 dv = make_float2(0.f, 0.f);
+        for (int r = 0; r < 4; ++r) {
+          float2 dv = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) dv = cfma(D[r * 4 + q], p[q], dv);
-            acc += re_conj_mul(u[r], dv);
-          }
-          part[g] += acc;
+          for (int q = 0; q < 4; ++q) dv = cfma(D[r * 4 + q], p[q], dv);
+          acc += re_conj_mul(u[r], dv);
         }
+        part[g] += acc;
+      }
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc = cfma(cconj(m[q * 4 + r]), u[q], acc);
-        a[idx[r]] = p[r];
-        l[idx[r]] = acc;
+        ao[idx[r]] = p[r];
+        lo[idx[r]] = acc;
       }
     }
   }
 }
 
 // Dispatch on the runtime register bits; every case is fully unrolled.
-#define TFQG_J3(F, ...)                        \
-  switch (j0) {                                \
-    case 0: F<0, NA>(__VA_ARGS__); break;      \
-    case 1: F<1, NA>(__VA_ARGS__); break;      \
-    default: F<2, NA>(__VA_ARGS__); break;     \
-  }
 #define TFQG_J4(F, ...)                        \
   switch (j0) {                                \
     case 0: F<0, NA>(__VA_ARGS__); break;      \
     case 1: F<1, NA>(__VA_ARGS__); break;      \
     case 2: F<2, NA>(__VA_ARGS__); break;      \
     default: F<3, NA>(__VA_ARGS__); break;     \
-  }
-#define TFQG_J6(F, ...)                        \
-  switch (j0 * 4 + j1) {                       \
-    case 1: F<0, 1, NA>(__VA_ARGS__); break;   \
-    case 2: F<0, 2, NA>(__VA_ARGS__); break;   \
-    case 4: F<1, 0, NA>(__VA_ARGS__); break;   \
-    case 6: F<1, 2, NA>(__VA_ARGS__); break;   \
-    case 8: F<2, 0, NA>(__VA_ARGS__); break;   \
-    default: F<2, 1, NA>(__VA_ARGS__); break;  \
   }
 #define TFQG_J12(F, ...)                       \
   switch (j0 * 4 + j1) {                       \
@@ -426,91 +470,156 @@ __device__ __forceinline__ void b2(float2 (&a)[NA], float2 (&l)[NA],
     case 13: F<3, 1, NA>(__VA_ARGS__); break;  \
     default: F<3, 2, NA>(__VA_ARGS__); break;  \
   }
+#define TFQG_CX(NA_, I, O)                                                      \
+  switch ((j0 * 4 + jc) * 2 + cv) {                                            \
+    case 2: f1_cx<0, 1, 0, NA_>(I, O); break;  case 3: f1_cx<0, 1, 1, NA_>(I, O); break; \
+    case 4: f1_cx<0, 2, 0, NA_>(I, O); break;  case 5: f1_cx<0, 2, 1, NA_>(I, O); break; \
+    case 6: f1_cx<0, 3, 0, NA_>(I, O); break;  case 7: f1_cx<0, 3, 1, NA_>(I, O); break; \
+    case 8: f1_cx<1, 0, 0, NA_>(I, O); break;  case 9: f1_cx<1, 0, 1, NA_>(I, O); break; \
+    case 12: f1_cx<1, 2, 0, NA_>(I, O); break; case 13: f1_cx<1, 2, 1, NA_>(I, O); break; \
+    case 14: f1_cx<1, 3, 0, NA_>(I, O); break; case 15: f1_cx<1, 3, 1, NA_>(I, O); break; \
+    case 16: f1_cx<2, 0, 0, NA_>(I, O); break; case 17: f1_cx<2, 0, 1, NA_>(I, O); break; \
+    case 18: f1_cx<2, 1, 0, NA_>(I, O); break; case 19: f1_cx<2, 1, 1, NA_>(I, O); break; \
+    case 22: f1_cx<2, 3, 0, NA_>(I, O); break; case 23: f1_cx<2, 3, 1, NA_>(I, O); break; \
+    case 24: f1_cx<3, 0, 0, NA_>(I, O); break; case 25: f1_cx<3, 0, 1, NA_>(I, O); break; \
+    case 26: f1_cx<3, 1, 0, NA_>(I, O); break; case 27: f1_cx<3, 1, 1, NA_>(I, O); break; \
+    case 28: f1_cx<3, 2, 0, NA_>(I, O); break; default: f1_cx<3, 2, 1, NA_>(I, O); break; \
+  }
+#define TFQG_B3(F, NG_, ...)                          \
+  switch (j0) {                                       \
+    case 0: F<0, NA, NG_>(__VA_ARGS__); break;        \
+    case 1: F<1, NA, NG_>(__VA_ARGS__); break;        \
+    default: F<2, NA, NG_>(__VA_ARGS__); break;       \
+  }
+#define TFQG_B6(F, NG_, ...)                          \
+  switch (j0 * 4 + j1) {                              \
+    case 1: F<0, 1, NA, NG_>(__VA_ARGS__); break;     \
+    case 2: F<0, 2, NA, NG_>(__VA_ARGS__); break;     \
+    case 4: F<1, 0, NA, NG_>(__VA_ARGS__); break;     \
+    case 6: F<1, 2, NA, NG_>(__VA_ARGS__); break;     \
+    case 8: F<2, 0, NA, NG_>(__VA_ARGS__); break;     \
+    default: F<2, 1, NA, NG_>(__VA_ARGS__); break;    \
+  }
 
-template <int J, int NA>
-__device__ __forceinline__ void b1_x(float2 (&a)[NA], float2 (&l)[NA],
-                                     const float2* m, const float2* dm, int ng,
-                                     int kmask, int kval, float* part) {
-  b1<J, GC_X, NA>(a, l, m, dm, ng, kmask, kval, part);
-}
-template <int J, int NA>
-__device__ __forceinline__ void b1_diag(float2 (&a)[NA], float2 (&l)[NA],
-                                        const float2* m, const float2* dm, int ng,
-                                        int kmask, int kval, float* part) {
-  b1<J, GC_DIAG, NA>(a, l, m, dm, ng, kmask, kval, part);
-}
-template <int J, int NA>
-__device__ __forceinline__ void b1_real(float2 (&a)[NA], float2 (&l)[NA],
-                                        const float2* m, const float2* dm, int ng,
-                                        int kmask, int kval, float* part) {
-  b1<J, GC_REAL, NA>(a, l, m, dm, ng, kmask, kval, part);
-}
-template <int J, int NA>
-__device__ __forceinline__ void b1_general(float2 (&a)[NA], float2 (&l)[NA],
-                                           const float2* m, const float2* dm,
-                                           int ng, int kmask, int kval,
-                                           float* part) {
-  b1<J, GC_GENERAL, NA>(a, l, m, dm, ng, kmask, kval, part);
-}
-template <int J0, int J1, int NA>
-__device__ __forceinline__ void b2_diag(float2 (&a)[NA], float2 (&l)[NA],
-                                        const float2* m, const float2* dm, int ng,
-                                        int kmask, int kval, float* part) {
-  b2<J0, J1, GC_DIAG, NA>(a, l, m, dm, ng, kmask, kval, part);
-}
-template <int J0, int J1, int NA>
-__device__ __forceinline__ void b2_general(float2 (&a)[NA], float2 (&l)[NA],
-                                           const float2* m, const float2* dm,
-                                           int ng, int kmask, int kval,
-                                           float* part) {
-  b2<J0, J1, GC_GENERAL, NA>(a, l, m, dm, ng, kmask, kval, part);
-}
+#define TFQG_B1_WRAP(NAME, CLS)                                                  \
+  template <int J, int NA, int NG>                                               \
+  __device__ __forceinline__ void NAME(const float2 (&a)[NA], const float2 (&l)[NA], \
+                                       float2 (&ao)[NA], float2 (&lo)[NA],       \
+                                       const float2* m, const float2* dm,        \
+                                       int kmask, int kval, float* part) {       \
+    b1<J, CLS, NA, NG>(a, l, ao, lo, m, dm, kmask, kval, part);                  \
+  }
+TFQG_B1_WRAP(b1_x, GC_X)
+TFQG_B1_WRAP(b1_diag, GC_DIAG)
+TFQG_B1_WRAP(b1_real, GC_REAL)
+TFQG_B1_WRAP(b1_general, GC_GENERAL)
+#define TFQG_B2_WRAP(NAME, CLS)                                                  \
+  template <int J0, int J1, int NA, int NG>                                      \
+  __device__ __forceinline__ void NAME(const float2 (&a)[NA], const float2 (&l)[NA], \
+                                       float2 (&ao)[NA], float2 (&lo)[NA],       \
+                                       const float2* m, const float2* dm,        \
+                                       int kmask, int kval, float* part) {       \
+    b2<J0, J1, CLS, NA, NG>(a, l, ao, lo, m, dm, kmask, kval, part);             \
+  }
+TFQG_B2_WRAP(b2_diag, GC_DIAG)
+TFQG_B2_WRAP(b2_general, GC_GENERAL)
 
 constexpr int kFwdRB = 4;  // register bits of forward sub-passes
 constexpr int kBwdRB = 3;  // register bits of adjoint sub-passes (psi + lambda)
 
-__device__ __forceinline__ void apply_forward(const DevOp& op, float2 (&a)[1 << kFwdRB],
+// One forward gate: in -> out (every element of out written).
+__device__ __forceinline__ void apply_forward(uint32_t code,
+                                              const float2 (&in)[1 << kFwdRB],
+                                              float2 (&out)[1 << kFwdRB],
                                               const float2* m) {
   constexpr int NA = 1 << kFwdRB;
-  const int j0 = op.t0, j1 = op.t1, kmask = op.kmask, kval = op.kval;
-  if (op.type == OP_F1 || op.type == OP_MCH) {
-    switch (op.cls) {
-      case GC_REAL: TFQG_J4(f1_real, a, m, kmask, kval); break;
-      case GC_DIAG: TFQG_J4(f1_diag, a, m, kmask, kval); break;
-      case GC_X: TFQG_J4(f1_x, a, kmask, kval); break;
-      case GC_SKIP: break;
-      default: TFQG_J4(f1_general, a, m, kmask, kval); break;
+  const int type = code & 7, cls = (code >> 3) & 7, j0 = (code >> 6) & 3,
+            j1 = (code >> 8) & 3, kmask = (code >> 10) & 15, kval = (code >> 14) & 15;
+  if (type == OP_F1 || type == OP_MCH) {
+    if (cls == GC_SKIP) { copy_regs(in, out); return; }
+    if (kmask == 0) {
+      switch (cls) {
+        case GC_REAL: TFQG_J4(f1_real, in, out, m, 0, 0); break;
+        case GC_DIAG: TFQG_J4(f1_diag, in, out, m, 0, 0); break;
+        case GC_X: TFQG_J4(f1_x, in, out, 0, 0); break;
+        default: TFQG_J4(f1_general, in, out, m, 0, 0); break;
+      }
+    } else if (cls == GC_X && ((code >> 21) & 1)) {
+      const int jc = (code >> 22) & 3, cv = (code >> 24) & 1;
+      TFQG_CX(NA, in, out);
+    } else {
+      switch (cls) {
+        case GC_REAL: TFQG_J4(f1_real, in, out, m, kmask, kval); break;
+        case GC_DIAG: TFQG_J4(f1_diag, in, out, m, kmask, kval); break;
+        case GC_X: TFQG_J4(f1_x, in, out, kmask, kval); break;
+        default: TFQG_J4(f1_general, in, out, m, kmask, kval); break;
+      }
     }
   } else {
-    if (op.cls == GC_DIAG) {
-      TFQG_J12(f2_diag, a, m, kmask, kval);
+    if (cls == GC_DIAG) {
+      if (kmask == 0) { TFQG_J12(f2_diag, in, out, m, 0, 0); }
+      else { TFQG_J12(f2_diag, in, out, m, kmask, kval); }
     } else {
-      TFQG_J12(f2_general, a, m, kmask, kval);
+      if (kmask == 0) { TFQG_J12(f2_general, in, out, m, 0, 0); }
+      else { TFQG_J12(f2_general, in, out, m, kmask, kval); }
     }
   }
 }
 
-__device__ __forceinline__ void apply_backward(const DevOp& op,
-                                               float2 (&a)[1 << kBwdRB],
-                                               float2 (&l)[1 << kBwdRB],
+// One adjoint step: (a, l) -> (ao, lo).
+__device__ __forceinline__ void apply_backward(uint32_t code,
+                                               const float2 (&a)[1 << kBwdRB],
+                                               const float2 (&l)[1 << kBwdRB],
+                                               float2 (&ao)[1 << kBwdRB],
+                                               float2 (&lo)[1 << kBwdRB],
                                                const float2* m,
                                                const float2* dm, float* part) {
   constexpr int NA = 1 << kBwdRB;
-  const int j0 = op.t0, j1 = op.t1, kmask = op.kmask, kval = op.kval;
-  const int ng = op.ngrad;
-  if (op.type == OP_B1) {
-    switch (op.cls) {
-      case GC_X: TFQG_J3(b1_x, a, l, m, dm, ng, kmask, kval, part); break;
-      case GC_DIAG: TFQG_J3(b1_diag, a, l, m, dm, ng, kmask, kval, part); break;
-      case GC_REAL: TFQG_J3(b1_real, a, l, m, dm, ng, kmask, kval, part); break;
-      default: TFQG_J3(b1_general, a, l, m, dm, ng, kmask, kval, part); break;
+  const int type = code & 7, cls = (code >> 3) & 7, j0 = (code >> 6) & 3,
+            j1 = (code >> 8) & 3, kmask = (code >> 10) & 15, kval = (code >> 14) & 15;
+  const int ng = (code >> 18) & 3;
+  if (type == OP_B1) {
+    if (cls == GC_X && ((code >> 21) & 1)) {
+      // X is its own adjoint and has no parameters: permute psi and lambda
+      const int jc = (code >> 22) & 3, cv = (code >> 24) & 1;
+      TFQG_CX(NA, a, ao);
+      TFQG_CX(NA, l, lo);
+      return;
     }
-  } else {
-    if (op.cls == GC_DIAG) {
-      TFQG_J6(b2_diag, a, l, m, dm, ng, kmask, kval, part);
+#define TFQG_B1_ALL(NG_, KM, KV)                                                   \
+    switch (cls) {                                                                 \
+      case GC_X: TFQG_B3(b1_x, NG_, a, l, ao, lo, m, dm, KM, KV, part); break;     \
+      case GC_DIAG: TFQG_B3(b1_diag, NG_, a, l, ao, lo, m, dm, KM, KV, part); break; \
+      case GC_REAL: TFQG_B3(b1_real, NG_, a, l, ao, lo, m, dm, KM, KV, part); break; \
+      default: TFQG_B3(b1_general, NG_, a, l, ao, lo, m, dm, KM, KV, part); break; \
+    }
+    if (kmask == 0) {
+      if (ng == 0) { TFQG_B1_ALL(0, 0, 0) }
+      else if (ng == 1) { TFQG_B1_ALL(1, 0, 0) }
+      else { TFQG_B1_ALL(2, 0, 0) }
     } else {
-      TFQG_J6(b2_general, a, l, m, dm, ng, kmask, kval, part);
+      if (ng == 0) { TFQG_B1_ALL(0, kmask, kval) }
+      else if (ng == 1) { TFQG_B1_ALL(1, kmask, kval) }
+      else { TFQG_B1_ALL(2, kmask, kval) }
     }
+#undef TFQG_B1_ALL
+  } else {
+#define TFQG_B2_ALL(NG_, KM, KV)                                                   \
+    if (cls == GC_DIAG) {                                                          \
+      TFQG_B6(b2_diag, NG_, a, l, ao, lo, m, dm, KM, KV, part);                    \
+    } else {                                                                       \
+      TFQG_B6(b2_general, NG_, a, l, ao, lo, m, dm, KM, KV, part);                 \
+    }
+    if (kmask == 0) {
+      if (ng == 0) { TFQG_B2_ALL(0, 0, 0) }
+      else if (ng == 1) { TFQG_B2_ALL(1, 0, 0) }
+      else { TFQG_B2_ALL(2, 0, 0) }
+    } else {
+      if (ng == 0) { TFQG_B2_ALL(0, kmask, kval) }
+      else if (ng == 1) { TFQG_B2_ALL(1, kmask, kval) }
+      else { TFQG_B2_ALL(2, kmask, kval) }
+    }
+#undef TFQG_B2_ALL
   }
 }
 
@@ -520,53 +629,113 @@ __device__ __forceinline__ uint32_t group_base(uint32_t g, uint32_t rbits, int r
   return g;
 }
 
+__device__ __forceinline__ bool op_active(const Stage* st, int i, uint32_t code,
+                                          uint32_t gb, uint32_t base) {
+  return !((code >> 20) & 1) ||
+         ((gb & st->lcmask[i]) == st->lcval[i] && (base & st->gcmask[i]) == st->gcval[i]);
+}
+
 // Forward sub-pass: each thread group loads the 16 amplitudes spanning the
-// register bits, applies the staged ops in registers, stores once.  Compiled
-// once and shared by every kernel mode.
-__device__ __noinline__ void exec_forward(float2* s, int T, uint32_t base,
-                                          const Stage* st, int nops,
+// register bits, applies the staged ops in registers (ping-pong between two
+// arrays), stores once.  Compiled once and shared by every kernel mode.
+__device__ __noinline__ void exec_forward(uint32_t s_off, int T, uint32_t base,
+                                          uint32_t st_off, int nops,
                                           uint32_t rbits) {
   constexpr int RB = kFwdRB, NA = 1 << RB;
-  uint32_t off[NA];
+  float2* s = reinterpret_cast<float2*>(smem_raw + s_off);
+  const Stage* st = reinterpret_cast<const Stage*>(smem_raw + st_off);
+  uint32_t soff[NA];
 #pragma unroll
   for (int k = 0; k < NA; ++k) {
     uint32_t o = 0;
 #pragma unroll
     for (int j = 0; j < RB; ++j)
       if (k >> j & 1) o |= 1u << ((rbits >> (8 * j)) & 0xFF);
-    off[k] = o;
+    soff[k] = swz(o);
   }
   const uint32_t ngroups = 1u << (T - RB);
   for (uint32_t g = threadIdx.x; g < ngroups; g += blockDim.x) {
     const uint32_t gb = group_base(g, rbits, RB);
-    float2 av[NA];
+    const uint32_t sgb = swz(gb);
+    float2 A[NA], B[NA];
 #pragma unroll
-    for (int k = 0; k < NA; ++k) av[k] = s[gb | off[k]];
-    for (int i = 0; i < nops; ++i) {
-      const DevOp& op = st->op[i];
-      if ((gb & op.lcmask) == op.lcval && (base & op.gcmask) == op.gcval)
-        apply_forward(op, av, st->mat[i]);
+    for (int k = 0; k < NA; ++k) A[k] = s[sgb ^ soff[k]];
+    int i = 0;
+    for (;;) {
+      if (i >= nops) {
+#pragma unroll
+        for (int k = 0; k < NA; ++k) s[sgb ^ soff[k]] = A[k];
+        break;
+      }
+      {
+        const uint32_t code = st->code[i];
+        if (op_active(st, i, code, gb, base)) apply_forward(code, A, B, st->mat[i]);
+        else copy_regs(A, B);
+      }
+      if (++i >= nops) {
+#pragma unroll
+        for (int k = 0; k < NA; ++k) s[sgb ^ soff[k]] = B[k];
+        break;
+      }
+      {
+        const uint32_t code = st->code[i];
+        if (op_active(st, i, code, gb, base)) apply_forward(code, B, A, st->mat[i]);
+        else copy_regs(B, A);
+      }
+      ++i;
     }
-#pragma unroll
-    for (int k = 0; k < NA; ++k) s[gb | off[k]] = av[k];
   }
 }
 
-// Adjoint sub-pass on psi (s) and lambda (l) with 3 register bits; per-op
-// gradient partials are warp-reduced into st->red[rbuf].
-__device__ __noinline__ void exec_backward(float2* s, float2* l, int T,
-                                           uint32_t base, Stage* st, int nops,
-                                           uint32_t rbits, int rbuf) {
-  constexpr int RB = kBwdRB, NA = 1 << RB;
+// One adjoint op of the sub-pass: (a, l) -> (ao, lo) plus warp-reduced
+// gradient partials into st->red.
+__device__ __forceinline__ void backward_op(Stage* st, int i, uint32_t gb,
+                                            uint32_t base, bool active, int it,
+                                            int rbuf, int& gi,
+                                            const float2 (&a)[1 << kBwdRB],
+                                            const float2 (&l)[1 << kBwdRB],
+                                            float2 (&ao)[1 << kBwdRB],
+                                            float2 (&lo)[1 << kBwdRB]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t off[NA];
+  const uint32_t code = st->code[i];
+  const bool on = active && op_active(st, i, code, gb, base);
+  const int ng = (code >> 18) & 3;
+  float part[2] = {0.f, 0.f};
+  if (on) {
+    apply_backward(code, a, l, ao, lo, st->mat[i], &st->dmat[i][0][0], part);
+  } else {
+    copy_regs(a, ao);
+    copy_regs(l, lo);
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    if (q < ng) {
+      float v = warp_sum(part[q]);
+      if (lane == 0) {
+        if (it == 0) st->red[rbuf][gi + q][warp] = v;
+        else st->red[rbuf][gi + q][warp] += v;
+      }
+    }
+  }
+  gi += ng;
+}
+
+// Adjoint sub-pass on psi (s) and lambda (l) with 3 register bits.
+__device__ __noinline__ void exec_backward(uint32_t s_off, uint32_t l_off, int T,
+                                           uint32_t base, uint32_t st_off,
+                                           int nops, uint32_t rbits, int rbuf) {
+  constexpr int RB = kBwdRB, NA = 1 << RB;
+  float2* s = reinterpret_cast<float2*>(smem_raw + s_off);
+  float2* l = reinterpret_cast<float2*>(smem_raw + l_off);
+  Stage* st = reinterpret_cast<Stage*>(smem_raw + st_off);
+  uint32_t soff[NA];
 #pragma unroll
   for (int k = 0; k < NA; ++k) {
     uint32_t o = 0;
 #pragma unroll
     for (int j = 0; j < RB; ++j)
       if (k >> j & 1) o |= 1u << ((rbits >> (8 * j)) & 0xFF);
-    off[k] = o;
+    soff[k] = swz(o);
   }
   const uint32_t ngroups = 1u << (T - RB);
   const uint32_t iters = (ngroups + blockDim.x - 1) / blockDim.x;
@@ -574,30 +743,34 @@ __device__ __noinline__ void exec_backward(float2* s, float2* l, int T,
     const uint32_t g = it * blockDim.x + threadIdx.x;
     const bool active = g < ngroups;
     const uint32_t gb = group_base(active ? g : 0u, rbits, RB);
-    float2 av[NA], lv[NA];
+    const uint32_t sgb = swz(gb);
+    float2 A[NA], LA[NA], B[NA], LB[NA];
     if (active) {
 #pragma unroll
-      for (int k = 0; k < NA; ++k) { av[k] = s[gb | off[k]]; lv[k] = l[gb | off[k]]; }
+      for (int k = 0; k < NA; ++k) { A[k] = s[sgb ^ soff[k]]; LA[k] = l[sgb ^ soff[k]]; }
+    } else {
+#pragma unroll
+      for (int k = 0; k < NA; ++k) { A[k] = make_float2(0.f, 0.f); LA[k] = A[k]; }
     }
-    int gi = 0;
-    for (int i = 0; i < nops; ++i) {
-      const DevOp& op = st->op[i];
-      const bool on = active && (gb & op.lcmask) == op.lcval &&
-                      (base & op.gcmask) == op.gcval;
-      float part[2] = {0.f, 0.f};
-      if (on) apply_backward(op, av, lv, st->mat[i], &st->dmat[i][0][0], part);
-      for (int q = 0; q < op.ngrad; ++q) {
-        float v = warp_sum(part[q]);
-        if (lane == 0) {
-          if (it == 0) st->red[rbuf][gi + q][warp] = v;
-          else st->red[rbuf][gi + q][warp] += v;
+    int gi = 0, i = 0;
+    for (;;) {
+      if (i >= nops) {
+        if (active) {
+#pragma unroll
+          for (int k = 0; k < NA; ++k) { s[sgb ^ soff[k]] = A[k]; l[sgb ^ soff[k]] = LA[k]; }
         }
+        break;
       }
-      gi += op.ngrad;
-    }
-    if (active) {
+      backward_op(st, i, gb, base, active, int(it), rbuf, gi, A, LA, B, LB);
+      if (++i >= nops) {
+        if (active) {
 #pragma unroll
-      for (int k = 0; k < NA; ++k) { s[gb | off[k]] = av[k]; l[gb | off[k]] = lv[k]; }
+          for (int k = 0; k < NA; ++k) { s[sgb ^ soff[k]] = B[k]; l[sgb ^ soff[k]] = LB[k]; }
+        }
+        break;
+      }
+      backward_op(st, i, gb, base, active, int(it), rbuf, gi, B, LB, A, LA);
+      ++i;
     }
   }
 }
@@ -619,7 +792,7 @@ __device__ void op_channel(float2* s, int T, int t0, const DevChannel& ch,
     float part[4] = {0.f, 0.f, 0.f, 0.f};
     for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
       uint32_t i0 = ins0(i, t0);
-      float2 a0 = s[i0], a1 = s[i0 | bit];
+      float2 a0 = s[swz(i0)], a1 = s[swz(i0 | bit)];
       for (int j = 0; j < ch.nk; ++j) {
         const float2* K = kraus + (ch.kraus + j) * 4;
         float2 z = make_float2(0.f, 0.f);
@@ -648,10 +821,10 @@ __device__ void op_channel(float2* s, int T, int t0, const DevChannel& ch,
   for (int j = 0; j < 4; ++j) g[j] = make_float2(K[j].x * scale, K[j].y * scale);
   for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
     uint32_t i0 = ins0(i, t0);
-    float2 a0 = s[i0], a1 = s[i0 | bit];
+    float2 a0 = s[swz(i0)], a1 = s[swz(i0 | bit)];
     float2 z = make_float2(0.f, 0.f);
-    s[i0] = cfma(g[1], a1, cfma(g[0], a0, z));
-    s[i0 | bit] = cfma(g[3], a1, cfma(g[2], a0, z));
+    s[swz(i0)] = cfma(g[1], a1, cfma(g[0], a0, z));
+    s[swz(i0 | bit)] = cfma(g[3], a1, cfma(g[2], a0, z));
   }
 }
 
@@ -687,11 +860,16 @@ __device__ void stage_subpass(const BatchDevice& b, const RunArgs& a,
         const float2* K = b.kraus + (ch.kraus + k) * 4;
         for (int j = 0; j < 4; ++j)
           st->mat[i][j] = make_float2(K[j].x * ch.scale[k], K[j].y * ch.scale[k]);
-        st->op[i] = o2;
+        st->code[i] = op_code(o2);
+        st->lcmask[i] = 0; st->lcval[i] = 0; st->gcmask[i] = 0; st->gcval[i] = 0;
       }
       continue;
     }
-    if (c == 0) st->op[i] = op;
+    if (c == 0) {
+      st->code[i] = op_code(op);
+      st->lcmask[i] = op.lcmask; st->lcval[i] = op.lcval;
+      st->gcmask[i] = op.gcmask; st->gcval[i] = op.gcval;
+    }
     if (c < 8) {
       reinterpret_cast<float4*>(st->mat[i])[c] =
           __ldg(reinterpret_cast<const float4*>(mats + int64_t(op.gate) * 16) + c);
@@ -737,10 +915,14 @@ __device__ void run_ops(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     const int nops = int(h.gate);
     stage_subpass<MODE>(b, a, rc, st, o + 1, nops, rbuf);
     __syncthreads();
-    if (MODE == kModeAdjoint && h.t0 == kBwdRB)
-      exec_backward(s, l, T, base, st, nops, h.lcmask, rbuf);
-    else
-      exec_forward(s, T, base, st, nops, h.lcmask);
+    const uint32_t so = uint32_t(reinterpret_cast<unsigned char*>(s) - smem_raw);
+    const uint32_t sto = uint32_t(reinterpret_cast<unsigned char*>(st) - smem_raw);
+    if (MODE == kModeAdjoint && h.t0 == kBwdRB) {
+      const uint32_t lo = uint32_t(reinterpret_cast<unsigned char*>(l) - smem_raw);
+      exec_backward(so, lo, T, base, sto, nops, h.lcmask, rbuf);
+    } else {
+      exec_forward(so, T, base, sto, nops, h.lcmask);
+    }
     __syncthreads();
     if (MODE == kModeAdjoint && int(threadIdx.x) < st->nred[rbuf]) {
       double acc = 0.0;
@@ -786,8 +968,9 @@ __device__ void tile_load(float2* dst, const float2* src, const uint32_t* hi,
   const uint32_t n2 = 1u << (kTile - 1);
   for (uint32_t k = threadIdx.x; k < n2; k += blockDim.x) {
     uint32_t g = tile_global(hi, 2 * k) | base;
-    reinterpret_cast<float4*>(dst)[k] =
-        __ldcg(reinterpret_cast<const float4*>(src + g));
+    float4 v = __ldcg(reinterpret_cast<const float4*>(src + g));
+    dst[swz(2 * k)] = make_float2(v.x, v.y);
+    dst[swz(2 * k + 1)] = make_float2(v.z, v.w);
   }
 }
 
@@ -796,12 +979,13 @@ __device__ void tile_store(float2* dst, const float2* src, const uint32_t* hi,
   const uint32_t n2 = 1u << (kTile - 1);
   for (uint32_t k = threadIdx.x; k < n2; k += blockDim.x) {
     uint32_t g = tile_global(hi, 2 * k) | base;
-    __stcg(reinterpret_cast<float4*>(dst + g),
-           reinterpret_cast<const float4*>(src)[k]);
+    float2 a = src[swz(2 * k)], c = src[swz(2 * k + 1)];
+    __stcg(reinterpret_cast<float4*>(dst + g), make_float4(a.x, a.y, c.x, c.y));
   }
 }
 
 __device__ void tile_zero(float2* dst, bool first_tile) {
+  // swz(0) == 0 and swz permutes the tile, so plain order is fine here
   const uint32_t n = 1u << kTile;
   for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
     dst[k] = make_float2(k == 0 && first_tile ? 1.f : 0.f, 0.f);
@@ -851,13 +1035,13 @@ __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
 // sum_x conj(psi_x) (P psi)_x accumulated per thread: float inner chunks,
 // double across chunks.
 __device__ void term_partial(const float2* psi, uint32_t N, const DevTerm& t,
-                             double* re, double* im) {
+                             bool shared, double* re, double* im) {
   double dre = 0.0, dim = 0.0;
   float fre = 0.f, fim = 0.f;
   int cnt = 0;
   for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
     uint32_t y = x ^ t.flip;
-    float2 av = psi[x], bv = psi[y];
+    float2 av = psi[sidx(x, shared)], bv = psi[sidx(y, shared)];
     float sg = (__popc(y & t.zy) & 1) ? -1.f : 1.f;
     fre = fmaf(sg, fmaf(av.x, bv.x, av.y * bv.y), fre);
     fim = fmaf(sg, fmaf(av.x, bv.y, -av.y * bv.x), fim);
@@ -873,8 +1057,9 @@ __device__ void term_partial(const float2* psi, uint32_t N, const DevTerm& t,
 // thread 0 once per term (in order) after the block reduction.
 template <class Sink>
 __device__ void measure_terms(const BatchDevice& b, const Smem& sm,
-                              const float2* psi, int n, uint32_t tb,
-                              uint32_t te, Sink&& sink, int& rbuf) {
+                              const float2* psi, bool shared, int n,
+                              uint32_t tb, uint32_t te, Sink&& sink,
+                              int& rbuf) {
   const uint32_t N = 1u << n;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (uint32_t ti = tb; ti < te; ++ti) {
@@ -884,7 +1069,7 @@ __device__ void measure_terms(const BatchDevice& b, const Smem& sm,
       continue;
     }
     double re, im;
-    term_partial(psi, N, t, &re, &im);
+    term_partial(psi, N, t, shared, &re, &im);
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
       re += __shfl_xor_sync(0xffffffffu, re, o);
@@ -914,13 +1099,13 @@ __device__ void measure_terms(const BatchDevice& b, const Smem& sm,
 // (AccumulateOperators, util_qsim.h:362-414).
 __device__ void init_lambda(const BatchDevice& b, const RunArgs& a,
                             const RowCtx& rc, const float2* psi, float2* lam,
-                            int n) {
+                            bool shared, int n) {
   const uint32_t N = 1u << n;
   const float* dg = a.dgrads + int64_t(rc.row) * b.num_ops;
   // tiny resident states are padded to 4 bits: the padding must be zero
   if (rc.p.resident)
     for (uint32_t x = N + threadIdx.x; x < (1u << kRB); x += blockDim.x)
-      lam[x] = make_float2(0.f, 0.f);
+      lam[swz(x)] = make_float2(0.f, 0.f);
   for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
     float2 v = make_float2(0.f, 0.f);
     for (uint32_t ti = rc.r.term_begin; ti < rc.r.term_end; ++ti) {
@@ -928,13 +1113,13 @@ __device__ void init_lambda(const BatchDevice& b, const RunArgs& a,
       float w = dg[t.op] * t.coef;
       if (fabsf(w) < 1e-5f) continue;
       if (t.identity) {
-        float2 p = psi[x];
+        float2 p = psi[sidx(x, shared)];
         v.x = fmaf(w, p.x, v.x);
         v.y = fmaf(w, p.y, v.y);
         continue;
       }
       uint32_t y = x ^ t.flip;
-      float2 p = psi[y];
+      float2 p = psi[sidx(y, shared)];
       if (__popc(y & t.zy) & 1) w = -w;
       switch (t.ny & 3) {  // multiply by i^ny
         case 1: p = make_float2(-p.y, p.x); break;
@@ -945,7 +1130,7 @@ __device__ void init_lambda(const BatchDevice& b, const RunArgs& a,
       v.x = fmaf(w, p.x, v.x);
       v.y = fmaf(w, p.y, v.y);
     }
-    lam[x] = v;
+    lam[sidx(x, shared)] = v;
   }
 }
 
@@ -953,7 +1138,7 @@ __device__ void init_lambda(const BatchDevice& b, const RunArgs& a,
 // (StateSpace::Sample semantics: index x with probability |psi_x|^2).
 __device__ void sample_state(const BatchDevice& b, const RunArgs& a,
                              const Smem& sm, const RowCtx& rc,
-                             const float2* psi) {
+                             const float2* psi, bool shared) {
   const int n = rc.p.n, maxn = b.max_n, S = a.num_samples;
   const uint32_t N = 1u << n;
   const uint32_t nch = N < kMaxChunks ? N : kMaxChunks;
@@ -962,7 +1147,7 @@ __device__ void sample_state(const BatchDevice& b, const RunArgs& a,
     double acc = 0.0;
     float f = 0.f;
     for (uint32_t j = 0; j < L; ++j) {
-      float2 v = psi[c * L + j];
+      float2 v = psi[sidx(c * L + j, shared)];
       f = fmaf(v.x, v.x, fmaf(v.y, v.y, f));
       if ((j & 31) == 31) { acc += f; f = 0.f; }
     }
@@ -993,7 +1178,7 @@ __device__ void sample_state(const BatchDevice& b, const RunArgs& a,
     uint32_t x = lo * L, last_nz = x;
     bool found = false;
     for (uint32_t j = 0; j < L; ++j) {
-      float2 v = psi[lo * L + j];
+      float2 v = psi[sidx(lo * L + j, shared)];
       double p = double(v.x) * v.x + double(v.y) * v.y;
       if (p > 0.0) last_nz = lo * L + j;
       acc += p;
@@ -1011,7 +1196,7 @@ __device__ void sample_state(const BatchDevice& b, const RunArgs& a,
 __device__ void init_resident(float2* s, int n) {
   const uint32_t N = 1u << (n < kRB ? kRB : n);
   for (uint32_t x = threadIdx.x; x < N; x += blockDim.x)
-    s[x] = make_float2(x == 0 ? 1.f : 0.f, 0.f);
+    s[x] = make_float2(x == 0 ? 1.f : 0.f, 0.f);  // swz(0) == 0
 }
 
 template <int MODE>
@@ -1066,6 +1251,7 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
   }
   __syncthreads();
   const float2* psi = rc.p.resident ? sm.psi : g_psi;
+  const bool shared = rc.p.resident;
 
   if (MODE == kModeExpect) {
     float* out = a.out_f + int64_t(row) * b.num_ops;
@@ -1073,7 +1259,7 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     __syncthreads();
     int cur = -1;
     double acc = 0.0;
-    measure_terms(b, sm, psi, n, rc.r.term_begin, rc.r.term_end,
+    measure_terms(b, sm, psi, shared, n, rc.r.term_begin, rc.r.term_end,
                   [&](int op, double v) {
                     if (op != cur) {
                       if (cur >= 0) out[cur] = float(acc);
@@ -1091,7 +1277,7 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     auto flush = [&]() {
       if (cur >= 0 && rc.traj < a.reps[base + cur]) atomicAdd(a.acc + base + cur, acc);
     };
-    measure_terms(b, sm, psi, n, rc.r.term_begin, rc.r.term_end,
+    measure_terms(b, sm, psi, shared, n, rc.r.term_begin, rc.r.term_end,
                   [&](int op, double v) {
                     if (op != cur) {
                       flush();
@@ -1106,15 +1292,15 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     float2* o = a.out_state + (int64_t(row) << b.max_n);
     const uint32_t N = 1u << n, M = 1u << b.max_n;
     if (rc.p.resident)
-      for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) o[x] = sm.psi[x];
+      for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) o[x] = sm.psi[swz(x)];
     for (uint32_t x = N + threadIdx.x; x < M; x += blockDim.x)
       o[x] = make_float2(-2.f, 0.f);
   } else if (MODE == kModeSample) {
-    sample_state(b, a, sm, rc, psi);
+    sample_state(b, a, sm, rc, psi, shared);
   } else if (MODE == kModeAdjoint) {
     for (int k = threadIdx.x; k < rc.p.num_grads; k += blockDim.x) sm.grad[k] = 0.0;
     float2* lam = rc.p.resident ? sm.lam : g_lam;
-    init_lambda(b, a, rc, psi, lam, n);
+    init_lambda(b, a, rc, psi, lam, shared, n);
     __syncthreads();
     run_passes<MODE>(b, a, sm, rc, rc.p.bwd_pass_begin, rc.p.bwd_pass_end,
                      rc.p.resident ? nullptr : g_psi,
@@ -1134,7 +1320,6 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
 template <int MODE>
 __global__ void __launch_bounds__(kSimThreads, 1)
 simulate_kernel(BatchDevice b, RunArgs a, int state_amps, int nstates) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem sm;
   sm.psi = reinterpret_cast<float2*>(smem_raw);
   sm.lam = sm.psi + state_amps;

@@ -32,6 +32,9 @@ cudaError_t plain_expect_adjoint(const PlainJob& j, cudaStream_t s,
 
 extern "C" {
 int64_t tfqg_internal_batch_table_bytes(void* batch);
+int tfqg_internal_batch_subpasses(void* batch, int32_t* fwd_subs,
+                                  int32_t* fwd_ops, int32_t* bwd_subs,
+                                  int32_t* bwd_ops);
 int tfqg_internal_batch_passes(void* batch, int32_t* fwd, int32_t* bwd,
                                int32_t* resident);
 // Expectation + adjoint gradient of a uniform batch by the plain path, all
