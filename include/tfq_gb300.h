@@ -110,6 +110,19 @@ int tfqg_batch_noisy_expectation(tfqg_batch* b, const float* symbol_values,
                                  float* expectations, int device_buffers,
                                  void* stream);
 
+/* Same result as tfqg_batch_expectation, for callers that must not let the
+ * library allocate device memory (for example a host framework whose caching
+ * allocator has already reserved nearly all device memory, so a plugin's own
+ * cudaMalloc can fail).  This entry point has no counterpart in the reference.
+ * symbol_values and expectations are DEVICE pointers; the call is
+ * asynchronous on `stream`.  All scratch (compiled tables, gate matrices,
+ * state slots) lives in one fixed 64 MiB device array owned by the library:
+ * larger batches fail with RESOURCE_EXHAUSTED.  Calls share that array, so
+ * calls that overlap on the GPU race; the first call on a device looks up the
+ * array's address and should come before any stream capture. */
+int tfqg_batch_expectation_noalloc(tfqg_batch* b, const float* symbol_values,
+                                   float* expectations, void* stream);
+
 /* ---------------------------------------------------------------------
  * One-shot entry points with the reference op signatures and HOST buffers
  * (what a TF CPU-side OpKernel::Compute holds).  They create a transient

@@ -1,0 +1,91 @@
+// Internal batch representation shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "host.h"
+#include "kernels.h"
+
+namespace tfqg {
+
+#define TFQG_CUDA(call)                                                    \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess)                                                 \
+      throw ::tfqg::Error(::tfqg::kInternal,                               \
+                          std::string("CUDA error: ") +                    \
+                              cudaGetErrorString(e_) + " at " #call);      \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int device = -1;
+  void reserve(size_t need, int dev) {
+    if (need <= bytes && dev == device) return;
+    release();
+    size_t sz = std::max<size_t>(need, 256);
+    TFQG_CUDA(cudaMalloc(&p, sz));
+    bytes = sz;
+    device = dev;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  ~DevBuf() { release(); }
+};
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Offsets of the device tables inside one packed blob.
+struct TableOffsets {
+  size_t prog, rows, gates, pass, ops, terms, chan, kraus, gc, order;
+};
+
+int set_last_error(int code, const std::string& msg);
+
+}  // namespace tfqg
+
+struct tfqg_batch {
+  int kind = 0;
+  int64_t B = 0, P = 0, n_ops = 0;
+  int max_n = 0;
+  int max_resident_n = -1;   // largest resident row (-1: none)
+  bool any_streamed = false;
+  int max_streamed_n = 0;
+  int max_grads = 0;
+  int64_t total_gates = 0, total_grads = 0;
+
+  // packed host copies of the device tables
+  std::vector<tfqg::DevProgram> programs;
+  std::vector<tfqg::DevRow> rows;
+  std::vector<tfqg::GateTemplate> gates;
+  std::vector<tfqg::DevPass> passes;
+  std::vector<tfqg::DevOp> ops;
+  std::vector<tfqg::DevTerm> terms;
+  std::vector<tfqg::DevChannel> channels;
+  std::vector<float2> kraus;
+  std::vector<int32_t> grad_cols;
+  std::vector<int32_t> order;
+
+  // device state
+  std::mutex mu;
+  int device = -1;
+  tfqg::DevBuf tables, mats, dmats, work, counter, values, out, aux, aux2;
+  tfqg::BatchDevice bd;
+};
+
+namespace tfqg {
+// Packs the batch's tables into `blob` (256-byte aligned sections).
+TableOffsets pack_tables(const tfqg_batch* b, std::vector<unsigned char>* blob);
+// Device-table view of a blob copied to `base`.
+BatchDevice table_view(const tfqg_batch* b, unsigned char* base,
+                       const TableOffsets& o);
+}  // namespace tfqg

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/tfq_gb300.h"
+#include "batch_internal.h"
 #include "host.h"
 #include "kernels.h"
 #include "plain.h"
@@ -27,66 +28,9 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
-#define TFQG_CUDA(call)                                                    \
-  do {                                                                     \
-    cudaError_t e_ = (call);                                               \
-    if (e_ != cudaSuccess)                                                 \
-      throw Error(kInternal, std::string("CUDA error: ") +                 \
-                                 cudaGetErrorString(e_) + " at " #call);   \
-  } while (0)
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  int device = -1;
-  void reserve(size_t need, int dev) {
-    if (need <= bytes && dev == device) return;
-    release();
-    size_t sz = std::max<size_t>(need, 256);
-    TFQG_CUDA(cudaMalloc(&p, sz));
-    bytes = sz;
-    device = dev;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-  ~DevBuf() { release(); }
-};
-
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
 }  // namespace
 
-struct tfqg_batch {
-  int kind = 0;
-  int64_t B = 0, P = 0, n_ops = 0;
-  int max_n = 0;
-  int max_resident_n = -1;   // largest resident row (-1: none)
-  bool any_streamed = false;
-  int max_streamed_n = 0;
-  int max_grads = 0;
-  int64_t total_gates = 0, total_grads = 0;
-
-  // packed host copies of the device tables
-  std::vector<DevProgram> programs;
-  std::vector<DevRow> rows;
-  std::vector<GateTemplate> gates;
-  std::vector<DevPass> passes;
-  std::vector<DevOp> ops;
-  std::vector<DevTerm> terms;
-  std::vector<DevChannel> channels;
-  std::vector<float2> kraus;
-  std::vector<int32_t> grad_cols;
-  std::vector<int32_t> order;
-
-  // device state
-  std::mutex mu;
-  int device = -1;
-  DevBuf tables, mats, dmats, work, counter, values, out, aux, aux2;
-  BatchDevice bd;
-};
+int tfqg::set_last_error(int code, const std::string& msg) { return fail(code, msg); }
 
 namespace {
 
@@ -306,35 +250,56 @@ void ensure_device(tfqg_batch* b, cudaStream_t s) {
   TFQG_CUDA(cudaGetDevice(&dev));
   if (b->device == dev && b->tables.p) return;
   std::vector<unsigned char> blob;
-  size_t o_prog = put(&blob, b->programs), o_rows = put(&blob, b->rows),
-         o_gates = put(&blob, b->gates), o_pass = put(&blob, b->passes),
-         o_ops = put(&blob, b->ops), o_terms = put(&blob, b->terms),
-         o_chan = put(&blob, b->channels), o_kraus = put(&blob, b->kraus),
-         o_gc = put(&blob, b->grad_cols), o_order = put(&blob, b->order);
+  TableOffsets o = pack_tables(b, &blob);
   b->tables.reserve(blob.size(), dev);
   TFQG_CUDA(cudaMemcpyAsync(b->tables.p, blob.data(), blob.size(),
                             cudaMemcpyHostToDevice, s));
   TFQG_CUDA(cudaStreamSynchronize(s));  // blob is a temporary
-  unsigned char* base = static_cast<unsigned char*>(b->tables.p);
-  BatchDevice& d = b->bd;
-  d.programs = reinterpret_cast<const DevProgram*>(base + o_prog);
-  d.rows = reinterpret_cast<const DevRow*>(base + o_rows);
-  d.gates = reinterpret_cast<const GateTemplate*>(base + o_gates);
-  d.passes = reinterpret_cast<const DevPass*>(base + o_pass);
-  d.ops = reinterpret_cast<const DevOp*>(base + o_ops);
-  d.terms = reinterpret_cast<const DevTerm*>(base + o_terms);
-  d.channels = reinterpret_cast<const DevChannel*>(base + o_chan);
-  d.kraus = reinterpret_cast<const float2*>(base + o_kraus);
-  d.grad_cols = reinterpret_cast<const int32_t*>(base + o_gc);
-  d.order = reinterpret_cast<const int32_t*>(base + o_order);
+  b->bd = table_view(b, static_cast<unsigned char*>(b->tables.p), o);
+  b->device = dev;
+}
+
+}  // namespace
+
+TableOffsets tfqg::pack_tables(const tfqg_batch* b, std::vector<unsigned char>* blob) {
+  TableOffsets o;
+  o.prog = put(blob, b->programs);
+  o.rows = put(blob, b->rows);
+  o.gates = put(blob, b->gates);
+  o.pass = put(blob, b->passes);
+  o.ops = put(blob, b->ops);
+  o.terms = put(blob, b->terms);
+  o.chan = put(blob, b->channels);
+  o.kraus = put(blob, b->kraus);
+  o.gc = put(blob, b->grad_cols);
+  o.order = put(blob, b->order);
+  blob->resize(align256(blob->size()));
+  return o;
+}
+
+BatchDevice tfqg::table_view(const tfqg_batch* b, unsigned char* base,
+                             const TableOffsets& o) {
+  BatchDevice d;
+  d.programs = reinterpret_cast<const DevProgram*>(base + o.prog);
+  d.rows = reinterpret_cast<const DevRow*>(base + o.rows);
+  d.gates = reinterpret_cast<const GateTemplate*>(base + o.gates);
+  d.passes = reinterpret_cast<const DevPass*>(base + o.pass);
+  d.ops = reinterpret_cast<const DevOp*>(base + o.ops);
+  d.terms = reinterpret_cast<const DevTerm*>(base + o.terms);
+  d.channels = reinterpret_cast<const DevChannel*>(base + o.chan);
+  d.kraus = reinterpret_cast<const float2*>(base + o.kraus);
+  d.grad_cols = reinterpret_cast<const int32_t*>(base + o.gc);
+  d.order = reinterpret_cast<const int32_t*>(base + o.order);
   d.num_rows = int32_t(b->B);
   d.num_ops = int32_t(b->n_ops);
   d.num_symbols = int32_t(b->P);
   d.max_n = b->max_n;
   d.total_gates = b->total_gates;
   d.total_grads = b->total_grads;
-  b->device = dev;
+  return d;
 }
+
+namespace {
 
 // Common preamble: device tables, symbol values on the device, matrices.
 const float* prepare(tfqg_batch* b, const float* values, int device_buffers,
