@@ -46,7 +46,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Offsets of the device tables inside one packed blob.
 struct TableOffsets {
-  size_t prog, rows, gates, pass, ops, terms, chan, kraus, gc, order;
+  size_t prog, rows, gates, pass, ops, terms, chan, kraus, gc, order, meas, mterms;
 };
 
 int set_last_error(int code, const std::string& msg);
@@ -74,6 +74,8 @@ struct tfqg_batch {
   std::vector<float2> kraus;
   std::vector<int32_t> grad_cols;
   std::vector<int32_t> order;
+  std::vector<tfqg::DevMeas> meas;
+  std::vector<tfqg::DevMeasTerm> meas_terms;
 
   // device state
   std::mutex mu;

@@ -187,7 +187,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
 
   // 6. rows: matrices, terms (deduplicated per distinct pauli-sum row)
   b->rows.resize(size_t(batch));
-  std::unordered_map<std::string, std::pair<uint32_t, uint32_t>> term_rows;
+  std::unordered_map<std::string, std::pair<uint32_t, uint32_t>> term_rows, meas_rows;
   int64_t mat = 0, dmat = 0;
   for (int64_t i = 0; i < batch; ++i) {
     DevRow& r = b->rows[i];
@@ -201,6 +201,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     dmat += b->programs[pid].num_grads;
     if (r.n == 0 || num_ops == 0) {
       r.term_begin = r.term_end = uint32_t(b->terms.size());
+      r.meas_begin = r.meas_end = uint32_t(b->meas.size());
       continue;
     }
     std::string key = std::to_string(pid) + ":";
@@ -210,6 +211,8 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     if (it != term_rows.end()) {
       r.term_begin = it->second.first;
       r.term_end = it->second.second;
+      r.meas_begin = meas_rows[key].first;
+      r.meas_end = meas_rows[key].second;
       continue;
     }
     r.term_begin = uint32_t(b->terms.size());
@@ -217,7 +220,12 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       lower_paulisum(psums[row_psum[i * num_ops + j]], index[pid], r.n, int(j),
                      &b->terms);
     r.term_end = uint32_t(b->terms.size());
+    r.meas_begin = uint32_t(b->meas.size());
+    plan_measurement(b->terms, r.term_begin, r.term_end, r.n,
+                     b->programs[pid].resident != 0, &b->meas, &b->meas_terms);
+    r.meas_end = uint32_t(b->meas.size());
     term_rows.emplace(key, std::make_pair(r.term_begin, r.term_end));
+    meas_rows.emplace(key, std::make_pair(r.meas_begin, r.meas_end));
   }
   b->total_gates = mat;
   b->total_grads = dmat;
@@ -273,6 +281,8 @@ TableOffsets tfqg::pack_tables(const tfqg_batch* b, std::vector<unsigned char>* 
   o.kraus = put(blob, b->kraus);
   o.gc = put(blob, b->grad_cols);
   o.order = put(blob, b->order);
+  o.meas = put(blob, b->meas);
+  o.mterms = put(blob, b->meas_terms);
   blob->resize(align256(blob->size()));
   return o;
 }
@@ -290,6 +300,8 @@ BatchDevice tfqg::table_view(const tfqg_batch* b, unsigned char* base,
   d.kraus = reinterpret_cast<const float2*>(base + o.kraus);
   d.grad_cols = reinterpret_cast<const int32_t*>(base + o.gc);
   d.order = reinterpret_cast<const int32_t*>(base + o.order);
+  d.meas = reinterpret_cast<const DevMeas*>(base + o.meas);
+  d.meas_terms = reinterpret_cast<const DevMeasTerm*>(base + o.mterms);
   d.num_rows = int32_t(b->B);
   d.num_ops = int32_t(b->n_ops);
   d.num_symbols = int32_t(b->P);

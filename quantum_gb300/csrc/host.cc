@@ -618,6 +618,8 @@ bool near(double a, double b) { return fabs(a - b) < 1e-9; }
 
 }  // namespace
 
+static uint32_t low_mask_bits(int k) { return k >= 32 ? 0xFFFFFFFFu : ((1u << k) - 1u); }
+
 // Chooses the cheapest exact arithmetic for a gate.  Constant gates are
 // classified from their matrix (fp32 parameter products, as the device
 // computes them); symbolic gates from their kind.
@@ -909,6 +911,62 @@ void plan_program(CompiledProgram* p, JobKind kind) {
   if (kind == kJobAdjoint) {
     std::vector<PlanItem> rev(items.rbegin(), items.rend());
     plan_sequence(*p, rev, tile_bits, true, chan_bits, &p->bwd_passes, &p->bwd_ops);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// measurement passes
+// ---------------------------------------------------------------------------
+void plan_measurement(const std::vector<DevTerm>& terms, uint32_t tb,
+                      uint32_t te, int n, bool resident,
+                      std::vector<DevMeas>* passes,
+                      std::vector<DevMeasTerm>* list) {
+  if (tb == te) return;
+  if (resident) {
+    // the tile is the whole state: local bits are global bits
+    for (uint32_t base = tb; base < te; base += kMaxMeasTerms) {
+      DevMeas m{low_mask_bits(n), uint32_t(list->size()), 0, 0};
+      for (uint32_t t = base; t < te && t < base + kMaxMeasTerms; ++t)
+        list->push_back(DevMeasTerm{t, terms[t].flip});
+      m.end = uint32_t(list->size());
+      passes->push_back(m);
+    }
+    return;
+  }
+  const uint32_t lanes = low_mask_bits(kLaneBits);
+  std::vector<uint32_t> remaining;
+  for (uint32_t t = tb; t < te; ++t) remaining.push_back(t);
+  while (!remaining.empty()) {
+    uint32_t S = lanes;
+    std::vector<uint32_t> taken, rest;
+    for (uint32_t t : remaining) {
+      uint32_t U = S | terms[t].flip;
+      if (__builtin_popcount(U) <= kStreamTileBits &&
+          taken.size() < size_t(kMaxMeasTerms)) {
+        S = U;
+        taken.push_back(t);
+      } else {
+        rest.push_back(t);
+      }
+    }
+    for (int b = 0; b < n && __builtin_popcount(S) < kStreamTileBits; ++b)
+      S |= 1u << b;
+    DevMeas m{S, uint32_t(list->size()), 0, 0};
+    for (uint32_t t : taken) {
+      // flip mask in tile-local bit positions
+      uint32_t lf = 0;
+      int j = 0;
+      for (int b = 0; b < 32; ++b)
+        if (S >> b & 1) {
+          if (terms[t].flip >> b & 1) lf |= 1u << j;
+          ++j;
+        }
+      list->push_back(DevMeasTerm{t, lf});
+    }
+    m.end = uint32_t(list->size());
+    passes->push_back(m);
+    if (taken.empty()) throw Error(kInternal, "measurement planner made no progress");
+    remaining.swap(rest);
   }
 }
 

@@ -110,6 +110,14 @@ uint8_t classify_gate(const GateTemplate& g);
 // Plans forward (and, for the adjoint, backward) passes.
 void plan_program(CompiledProgram* prog, JobKind kind);
 
+// Groups terms [tb, te) into measurement passes: each pass's tile holds the
+// flip bits of all its terms (resident rows: one pass over the whole state).
+constexpr int kMaxMeasTerms = 128;  // terms per measurement pass
+void plan_measurement(const std::vector<DevTerm>& terms, uint32_t tb,
+                      uint32_t te, int n, bool resident,
+                      std::vector<DevMeas>* passes,
+                      std::vector<DevMeasTerm>* list);
+
 // Pauli sum -> device terms for column `op` (bits relative to n qubits).
 void lower_paulisum(const PauliSumP& ps,
                     const std::unordered_map<std::string, int>& index, int n,

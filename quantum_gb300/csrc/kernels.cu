@@ -205,7 +205,12 @@ struct Smem {
   double* csum;       // sampler chunk prefix sums
   double* grad;       // adjoint accumulators
   Stage* st;
+  double* macc;       // [2 * kMaxMeasTerms] term sums (re, im)
+  struct MTerm { float w; uint32_t lflip, zy; uint16_t op; uint8_t ny, identity; }* mterm;
+  double* oacc;       // [kMaxOpsSmem] per-op sums (expectation mode)
 };
+constexpr int kMaxMeasTermsDev = 128;  // host kMaxMeasTerms
+constexpr int kMaxOpsSmem = 1024;
 
 __device__ __forceinline__ void warp_partials(double* red, int buf,
                                               const float* vals, int nv) {
@@ -1032,105 +1037,183 @@ __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
   }
 }
 
-// sum_x conj(psi_x) (P psi)_x accumulated per thread: float inner chunks,
-// double across chunks.
-__device__ void term_partial(const float2* psi, uint32_t N, const DevTerm& t,
-                             bool shared, double* re, double* im) {
-  double dre = 0.0, dim = 0.0;
-  float fre = 0.f, fim = 0.f;
-  int cnt = 0;
-  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
-    uint32_t y = x ^ t.flip;
-    float2 av = psi[sidx(x, shared)], bv = psi[sidx(y, shared)];
-    float sg = (__popc(y & t.zy) & 1) ? -1.f : 1.f;
-    fre = fmaf(sg, fmaf(av.x, bv.x, av.y * bv.y), fre);
-    fim = fmaf(sg, fmaf(av.x, bv.y, -av.y * bv.x), fim);
-    if (++cnt == 32) {
-      dre += fre; dim += fim; fre = fim = 0.f; cnt = 0;
+// Stages the terms of measurement pass M into shared memory; `w` is the
+// coefficient (expectation) or the AccumulateOperators weight g_j * c_t with
+// the reference's 1e-5 skip (lambda; util_qsim.h:378-383).
+__device__ void stage_terms(const BatchDevice& b, const RunArgs& a, const Smem& sm,
+                            const RowCtx& rc, const DevMeas& M, bool lambda) {
+  const int nt = int(M.end - M.begin);
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+    const DevMeasTerm mt = b.meas_terms[M.begin + i];
+    const DevTerm t = b.terms[mt.term];
+    float w = t.coef;
+    if (lambda) {
+      w = a.dgrads[int64_t(rc.row) * b.num_ops + t.op] * t.coef;
+      if (fabsf(w) < 1e-5f) w = 0.f;
     }
+    sm.mterm[i].w = w;
+    sm.mterm[i].lflip = mt.lflip;
+    sm.mterm[i].zy = t.zy;
+    sm.mterm[i].op = t.op;
+    sm.mterm[i].ny = t.ny;
+    sm.mterm[i].identity = t.identity;
   }
-  *re = dre + fre;
-  *im = dim + fim;
 }
 
-// Expectation of every term of the row; `sink(op, value)` is called by
-// thread 0 once per term (in order) after the block reduction.
+// Pauli-sum expectation by measurement passes (util_qsim.h:142-188): each
+// tile of the state is read once into shared memory and every term of the
+// pass whose flip bits lie in the tile is summed there.  Resident rows use
+// the state in shared memory as the single tile.  `sink(op, value)` is called
+// by thread 0 once per term.
 template <class Sink>
-__device__ void measure_terms(const BatchDevice& b, const Smem& sm,
-                              const float2* psi, bool shared, int n,
-                              uint32_t tb, uint32_t te, Sink&& sink,
-                              int& rbuf) {
-  const uint32_t N = 1u << n;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (uint32_t ti = tb; ti < te; ++ti) {
-    const DevTerm t = b.terms[ti];
-    if (t.identity) {
-      if (threadIdx.x == 0) sink(int(t.op), double(t.coef));
-      continue;
-    }
-    double re, im;
-    term_partial(psi, N, t, shared, &re, &im);
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      re += __shfl_xor_sync(0xffffffffu, re, o);
-      im += __shfl_xor_sync(0xffffffffu, im, o);
-    }
-    if (lane == 0) {
-      sm.red[(rbuf * 4 + 0) * kWarps + w] = re;
-      sm.red[(rbuf * 4 + 1) * kWarps + w] = im;
+__device__ void measure_passes(const BatchDevice& b, const RunArgs& a,
+                               const Smem& sm, const RowCtx& rc,
+                               const float2* g_psi, Sink&& sink) {
+  const int n = rc.p.n;
+  const bool resident = rc.p.resident;
+  const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+  const int lane = threadIdx.x & 31;
+  for (uint32_t mp = rc.r.meas_begin; mp < rc.r.meas_end; ++mp) {
+    const DevMeas M = b.meas[mp];
+    const int nt = int(M.end - M.begin);
+    stage_terms(b, a, sm, rc, M, false);
+    for (int i = threadIdx.x; i < 2 * nt; i += blockDim.x) sm.macc[i] = 0.0;
+    uint32_t ntiles = 1;
+    int Tl = n;
+    if (!resident) {
+      build_hi_table(sm.hi, M.tile_mask);
+      ntiles = 1u << (n - kTile);
+      Tl = kTile;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double sre = red_total(sm.red, rbuf, 0), sim = red_total(sm.red, rbuf, 1);
-      double v;
-      switch (t.ny & 3) {
-        case 0: v = sre; break;
-        case 1: v = -sim; break;
-        case 2: v = -sre; break;
-        default: v = sim; break;
+    const uint32_t outside = all & ~M.tile_mask;
+    const uint32_t N = 1u << Tl;
+    for (uint32_t tile = 0; tile < ntiles; ++tile) {
+      uint32_t base = 0;
+      if (!resident) {
+        base = deposit(tile, outside);
+        tile_load(sm.psi, g_psi, sm.hi, base);
+        __syncthreads();
       }
-      sink(int(t.op), double(t.coef) * v);
+      for (int i = 0; i < nt; ++i) {
+        if (sm.mterm[i].identity) continue;
+        const uint32_t lf = sm.mterm[i].lflip, zy = sm.mterm[i].zy;
+        float re = 0.f, im = 0.f;
+        for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+          const uint32_t y = x ^ lf;
+          const float2 av = sm.psi[swz(x)], bv = sm.psi[swz(y)];
+          const uint32_t yg = resident ? y : ((y & 31u) | sm.hi[y >> 5] | base);
+          const float sg = (__popc(yg & zy) & 1) ? -1.f : 1.f;
+          re = fmaf(sg, fmaf(av.x, bv.x, av.y * bv.y), re);
+          im = fmaf(sg, fmaf(av.x, bv.y, -av.y * bv.x), im);
+        }
+        re = warp_sum(re);
+        im = warp_sum(im);
+        if (lane == 0) {
+          atomicAdd(&sm.macc[2 * i], double(re));
+          atomicAdd(&sm.macc[2 * i + 1], double(im));
+        }
+      }
+      __syncthreads();  // before the next tile overwrites sm.psi
     }
-    rbuf ^= 1;
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < nt; ++i) {
+        double v;
+        if (sm.mterm[i].identity) {
+          v = 1.0;
+        } else {
+          const double sre = sm.macc[2 * i], sim = sm.macc[2 * i + 1];
+          switch (sm.mterm[i].ny & 3) {  // Re(i^ny * sum)
+            case 0: v = sre; break;
+            case 1: v = -sim; break;
+            case 2: v = -sre; break;
+            default: v = sim; break;
+          }
+        }
+        sink(int(sm.mterm[i].op), double(sm.mterm[i].w) * v);
+      }
+    }
+    __syncthreads();
   }
 }
 
-// lambda = sum_j g_j sum_t c_t P_t psi, skipping |g_j c_t| < 1e-5
-// (AccumulateOperators, util_qsim.h:362-414).
-__device__ void init_lambda(const BatchDevice& b, const RunArgs& a,
-                            const RowCtx& rc, const float2* psi, float2* lam,
-                            bool shared, int n) {
-  const uint32_t N = 1u << n;
-  const float* dg = a.dgrads + int64_t(rc.row) * b.num_ops;
-  // tiny resident states are padded to 4 bits: the padding must be zero
-  if (rc.p.resident)
-    for (uint32_t x = N + threadIdx.x; x < (1u << kRB); x += blockDim.x)
-      lam[swz(x)] = make_float2(0.f, 0.f);
-  for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
-    float2 v = make_float2(0.f, 0.f);
-    for (uint32_t ti = rc.r.term_begin; ti < rc.r.term_end; ++ti) {
-      const DevTerm t = b.terms[ti];
-      float w = dg[t.op] * t.coef;
-      if (fabsf(w) < 1e-5f) continue;
-      if (t.identity) {
-        float2 p = psi[sidx(x, shared)];
-        v.x = fmaf(w, p.x, v.x);
-        v.y = fmaf(w, p.y, v.y);
-        continue;
-      }
-      uint32_t y = x ^ t.flip;
-      float2 p = psi[sidx(y, shared)];
-      if (__popc(y & t.zy) & 1) w = -w;
-      switch (t.ny & 3) {  // multiply by i^ny
-        case 1: p = make_float2(-p.y, p.x); break;
-        case 2: p = make_float2(-p.x, -p.y); break;
-        case 3: p = make_float2(p.y, -p.x); break;
-        default: break;
-      }
-      v.x = fmaf(w, p.x, v.x);
-      v.y = fmaf(w, p.y, v.y);
+// lambda = sum_j g_j sum_t c_t P_t psi by measurement passes
+// (AccumulateOperators, util_qsim.h:362-414).  Streamed rows read psi tiles
+// and accumulate lambda tiles in their global slot.
+__device__ void lambda_passes(const BatchDevice& b, const RunArgs& a,
+                              const Smem& sm, const RowCtx& rc,
+                              float2* g_psi, float2* g_lam) {
+  const int n = rc.p.n;
+  const bool resident = rc.p.resident;
+  const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+  if (resident) {
+    // zero lambda (including the padding of tiny states) before accumulating
+    const uint32_t Np = 1u << (n < kRB ? kRB : n);
+    for (uint32_t x = threadIdx.x; x < Np; x += blockDim.x)
+      sm.lam[x] = make_float2(0.f, 0.f);
+    __syncthreads();
+  }
+  for (uint32_t mp = rc.r.meas_begin; mp < rc.r.meas_end; ++mp) {
+    const DevMeas M = b.meas[mp];
+    const int nt = int(M.end - M.begin);
+    const bool first = mp == rc.r.meas_begin;
+    stage_terms(b, a, sm, rc, M, true);
+    uint32_t ntiles = 1;
+    int Tl = n;
+    if (!resident) {
+      build_hi_table(sm.hi, M.tile_mask);
+      ntiles = 1u << (n - kTile);
+      Tl = kTile;
     }
-    lam[sidx(x, shared)] = v;
+    __syncthreads();
+    const uint32_t outside = all & ~M.tile_mask;
+    const uint32_t N = 1u << Tl;
+    for (uint32_t tile = 0; tile < ntiles; ++tile) {
+      uint32_t base = 0;
+      if (!resident) {
+        base = deposit(tile, outside);
+        tile_load(sm.psi, g_psi, sm.hi, base);
+        if (!first) tile_load(sm.lam, g_lam, sm.hi, base);
+        __syncthreads();
+      }
+      for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+        float2 v = (first && !resident) ? make_float2(0.f, 0.f) : sm.lam[swz(x)];
+        for (int i = 0; i < nt; ++i) {
+          float w = sm.mterm[i].w;
+          if (w == 0.f) continue;
+          if (sm.mterm[i].identity) {
+            const float2 p = sm.psi[swz(x)];
+            v.x = fmaf(w, p.x, v.x);
+            v.y = fmaf(w, p.y, v.y);
+            continue;
+          }
+          const uint32_t y = x ^ sm.mterm[i].lflip;
+          float2 p = sm.psi[swz(y)];
+          const uint32_t yg = resident ? y : ((y & 31u) | sm.hi[y >> 5] | base);
+          if (__popc(yg & sm.mterm[i].zy) & 1) w = -w;
+          switch (sm.mterm[i].ny & 3) {  // multiply by i^ny
+            case 1: p = make_float2(-p.y, p.x); break;
+            case 2: p = make_float2(-p.x, -p.y); break;
+            case 3: p = make_float2(p.y, -p.x); break;
+            default: break;
+          }
+          v.x = fmaf(w, p.x, v.x);
+          v.y = fmaf(w, p.y, v.y);
+        }
+        sm.lam[swz(x)] = v;
+      }
+      __syncthreads();
+      if (!resident) {
+        tile_store(g_lam, sm.lam, sm.hi, base);
+        __syncthreads();
+      }
+    }
+  }
+  if (rc.r.meas_begin == rc.r.meas_end && !resident) {
+    // no observable terms: lambda is zero
+    for (uint32_t x = threadIdx.x; x < (1u << n); x += blockDim.x)
+      g_lam[x] = make_float2(0.f, 0.f);
+    __syncthreads();
   }
 }
 
@@ -1255,39 +1338,23 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
 
   if (MODE == kModeExpect) {
     float* out = a.out_f + int64_t(row) * b.num_ops;
-    for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x) out[j] = 0.f;
+    const bool small = b.num_ops <= kMaxOpsSmem;
+    for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x) {
+      if (small) sm.oacc[j] = 0.0;
+      else out[j] = 0.f;
+    }
     __syncthreads();
-    int cur = -1;
-    double acc = 0.0;
-    measure_terms(b, sm, psi, shared, n, rc.r.term_begin, rc.r.term_end,
-                  [&](int op, double v) {
-                    if (op != cur) {
-                      if (cur >= 0) out[cur] = float(acc);
-                      cur = op;
-                      acc = 0.0;
-                    }
-                    acc += v;
-                  },
-                  rbuf);
-    if (threadIdx.x == 0 && cur >= 0) out[cur] = float(acc);
+    measure_passes(b, a, sm, rc, g_psi, [&](int op, double v) {
+      if (small) sm.oacc[op] += v;
+      else out[op] += float(v);
+    });
+    if (small)
+      for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x) out[j] = float(sm.oacc[j]);
   } else if (MODE == kModeNoisy) {
     const int64_t base = int64_t(row) * b.num_ops;
-    int cur = -1;
-    double acc = 0.0;
-    auto flush = [&]() {
-      if (cur >= 0 && rc.traj < a.reps[base + cur]) atomicAdd(a.acc + base + cur, acc);
-    };
-    measure_terms(b, sm, psi, shared, n, rc.r.term_begin, rc.r.term_end,
-                  [&](int op, double v) {
-                    if (op != cur) {
-                      flush();
-                      cur = op;
-                      acc = 0.0;
-                    }
-                    acc += v;
-                  },
-                  rbuf);
-    if (threadIdx.x == 0) flush();
+    measure_passes(b, a, sm, rc, g_psi, [&](int op, double v) {
+      if (rc.traj < a.reps[base + op]) atomicAdd(a.acc + base + op, v);
+    });
   } else if (MODE == kModeState) {
     float2* o = a.out_state + (int64_t(row) << b.max_n);
     const uint32_t N = 1u << n, M = 1u << b.max_n;
@@ -1299,8 +1366,7 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     sample_state(b, a, sm, rc, psi, shared);
   } else if (MODE == kModeAdjoint) {
     for (int k = threadIdx.x; k < rc.p.num_grads; k += blockDim.x) sm.grad[k] = 0.0;
-    float2* lam = rc.p.resident ? sm.lam : g_lam;
-    init_lambda(b, a, rc, psi, lam, shared, n);
+    lambda_passes(b, a, sm, rc, g_psi, g_lam);
     __syncthreads();
     run_passes<MODE>(b, a, sm, rc, rc.p.bwd_pass_begin, rc.p.bwd_pass_end,
                      rc.p.resident ? nullptr : g_psi,
@@ -1332,6 +1398,12 @@ simulate_kernel(BatchDevice b, RunArgs a, int state_amps, int nstates) {
   p += 2 * 4 * kWarps * sizeof(double);
   sm.csum = reinterpret_cast<double*>(p);
   if (MODE == kModeSample) p += kMaxChunks * sizeof(double);
+  sm.macc = reinterpret_cast<double*>(p);
+  p += 2 * kMaxMeasTermsDev * sizeof(double);
+  sm.mterm = reinterpret_cast<decltype(sm.mterm)>(p);
+  p += kMaxMeasTermsDev * 16;
+  sm.oacc = reinterpret_cast<double*>(p);
+  if (MODE == kModeExpect) p += kMaxOpsSmem * sizeof(double);
   sm.grad = reinterpret_cast<double*>(p);
 
   __shared__ int s_item;
@@ -1410,6 +1482,8 @@ size_t sim_smem_bytes(int mode, int max_resident_n, bool any_streamed,
   bytes += (1u << kHiBits) * sizeof(uint32_t);
   bytes += 2 * 4 * kWarps * sizeof(double);
   if (mode == kModeSample) bytes += kMaxChunks * sizeof(double);
+  bytes += 2 * kMaxMeasTermsDev * sizeof(double) + kMaxMeasTermsDev * 16;
+  if (mode == kModeExpect) bytes += kMaxOpsSmem * sizeof(double);
   if (mode == kModeAdjoint) bytes += size_t(max_grads) * sizeof(double);
   return bytes;
 }

@@ -21,6 +21,8 @@ struct BatchDevice {
   const float2* kraus = nullptr;
   const int32_t* grad_cols = nullptr;
   const int32_t* order = nullptr;  // rows, most expensive first
+  const DevMeas* meas = nullptr;
+  const DevMeasTerm* meas_terms = nullptr;
   int32_t num_rows = 0;
   int32_t num_ops = 0;       // pauli_sums columns
   int32_t num_symbols = 0;

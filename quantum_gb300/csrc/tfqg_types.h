@@ -124,11 +124,27 @@ struct DevProgram {
   int32_t num_channels;
 };
 
+// A measurement pass: the terms [begin, end) of the measurement list are
+// evaluated on tiles holding the index bits of tile_mask (each term's flip
+// bits lie inside the tile).
+struct DevMeas {
+  uint32_t tile_mask;
+  uint32_t begin, end;
+  uint32_t pad;
+};
+
+// Entry of the measurement list: a term and its flip mask in tile-local bits.
+struct DevMeasTerm {
+  uint32_t term;
+  uint32_t lflip;
+};
+
 // Per batch row.
 struct DevRow {
   int32_t program;       // index into DevProgram[]
   int32_t n;
   uint32_t term_begin, term_end;   // DevTerm range for this row's pauli_sums
+  uint32_t meas_begin, meas_end;   // DevMeas range (measurement passes)
   uint64_t mat_offset;   // first matrix slot (float2[16] each) of this row
   uint64_t dmat_offset;  // first derivative matrix slot of this row
 };
