@@ -337,6 +337,9 @@ def main():
     e2e_val = BATCH * world / e2e_s
 
     # ---- roofline of the dominant kernel (adjoint sweep)
+    nsig, spec_modes, spec_err = _native.batch_specialization(batch._h)
+    adj_kernel = ("tfqg_jit_adjoint (run-time specialized)" if "adjoint" in spec_modes
+                  else "simulate_adjoint_kernel (interpreter)")
     adj_mean_ms = float(np.mean(adj_ms))
     flop = flop_per_circuit(w)
     peaks = {}
@@ -365,11 +368,13 @@ def main():
                 "d2h_bytes_per_step": int(d2h),
                 "path": "tfqg_simulate_expectation + tfqg_adj_grad (one-shot C ABI: parse, upload, run, download)"},
         "gpu_launches": launches * args.steps,
-        "roofline": {"bound": "hbm", "kernel": "simulate_kernel<adjoint>",
+        "specialization": {"signatures": nsig, "modes": sorted(spec_modes),
+                           "error": spec_err or None},
+        "roofline": {"bound": "hbm", "kernel": adj_kernel,
                      "achieved": None, "peak": hbm_peak, "unit": "GB/s", "frac": None,
                      "traffic": None,
                      "note": "the 16-qubit adjoint sweep is FP32/shared-memory bound; see compute"},
-        "compute": {"kernel": "simulate_kernel<adjoint>", "ms_per_launch": adj_mean_ms,
+        "compute": {"kernel": adj_kernel, "ms_per_launch": adj_mean_ms,
                     "algorithmic_tflop_per_launch": adj_flop * BATCH / 1e12,
                     "achieved_tflops": achieved_tflops,
                     "fp32_peak_tflops_at_measured_clock": fp32_peak,

@@ -119,3 +119,39 @@ def string_array(items):
     ptrs = (ctypes.c_char_p * max(n, 1))(*bs) if n else (ctypes.c_char_p * 1)()
     lens = (ctypes.c_int64 * max(n, 1))(*[len(x) for x in bs])
     return ctypes.cast(ptrs, c_char_pp), ctypes.cast(lens, c_int64_p), (bs, ptrs, lens)
+
+
+# -- internal controls (tests and benchmarks) -------------------------------
+SIM_MODES = {"expect": 0, "state": 1, "sample": 2, "adjoint": 3, "noisy": 4}
+
+
+def batch_specialization(handle, mode=None):
+    """Run-time specialization state of a batch handle.
+
+    mode: None leaves it unchanged, -1 turns it off, 0 automatic, 1 forced.
+    Returns (signatures, active_modes, last_error): active_modes is the set
+    of SimMode names whose specialized module is loaded."""
+    L = lib()
+    f = L.tfqg_internal_batch_jit
+    f.argtypes = [c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int32),
+                  ctypes.POINTER(ctypes.c_int32), ctypes.c_char_p, ctypes.c_int64]
+    f.restype = ctypes.c_int
+    nsig, active = ctypes.c_int32(), ctypes.c_int32()
+    err = ctypes.create_string_buffer(4096)
+    check(f(handle, 2 if mode is None else int(mode), ctypes.byref(nsig),
+            ctypes.byref(active), err, 4096))
+    modes = {k for k, v in SIM_MODES.items() if active.value >> v & 1}
+    return nsig.value, modes, err.value.decode("utf-8", "replace")
+
+
+def specialization_compile_check(handle, mode):
+    """Generate and compile (no load, no GPU) the specialized module of
+    `mode` for a batch handle; raises with the compiler log on failure."""
+    L = lib()
+    f = L.tfqg_internal_jit_compile_check
+    f.argtypes = [c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int64]
+    f.restype = ctypes.c_int
+    err = ctypes.create_string_buffer(16384)
+    rc = f(handle, SIM_MODES[mode], err, 16384)
+    if rc != 0:
+        raise _ERRORS.get(rc, InternalError)(err.value.decode("utf-8", "replace"))

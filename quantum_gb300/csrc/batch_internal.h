@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -76,6 +77,13 @@ struct tfqg_batch {
   std::vector<int32_t> order;
   std::vector<tfqg::DevMeas> meas;
   std::vector<tfqg::DevMeasTerm> meas_terms;
+
+  // run-time specialization (jit.cc)
+  std::vector<std::vector<uint32_t>> jit_signatures;
+  int jit_mode = 0;            // -1 off, 0 automatic, 1 forced
+  bool jit_loaded[5] = {};     // compile attempted, per SimMode
+  std::shared_ptr<void> jit_module[5];
+  std::string jit_error;
 
   // device state
   std::mutex mu;

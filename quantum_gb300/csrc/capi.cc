@@ -14,6 +14,7 @@
 #include "../../include/tfq_gb300.h"
 #include "batch_internal.h"
 #include "host.h"
+#include "jit.h"
 #include "kernels.h"
 #include "plain.h"
 
@@ -238,6 +239,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   };
   std::stable_sort(b->order.begin(), b->order.end(),
                    [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
+  jit_assign_signatures(b);
   if (b->max_grads > 8192)
     throw Error(kResourceExhausted,
                 "A circuit has more than 8192 symbolic gate parameters; the "
@@ -344,7 +346,8 @@ int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
   size_t smem = sim_smem_bytes(mode, b->max_resident_n, b->any_streamed, max_grads);
   if (smem > 227 * 1024)
     throw Error(kResourceExhausted, "shared memory request too large");
-  int grid = sim_grid_size(mode, smem);
+  cudaKernel_t jk = jit_kernel(b, mode, b->device);
+  int grid = jk ? jit_grid(jk, smem, b->device) : sim_grid_size(mode, smem);
   int64_t units = mode == kModeNoisy ? a->total_traj : b->B;
   if (units < grid) grid = int(std::max<int64_t>(units, 1));
   if (b->any_streamed) {
@@ -356,6 +359,16 @@ int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
   }
   TFQG_CUDA(cudaMemsetAsync(a->counter, 0, sizeof(int), s));
   int state_amps = sim_state_amps(b->max_resident_n, b->any_streamed);
+  if (jk) {
+    cudaError_t e = jit_launch(jk, b->bd, *a, grid, smem, state_amps,
+                               mode == kModeAdjoint ? 2 : 1, s);
+    if (e == cudaSuccess) return grid;
+    // a rejected launch (nothing ran): record why, stop specializing this
+    // batch and run the interpreter instead
+    cudaGetLastError();
+    b->jit_error = std::string("specialized launch rejected: ") + cudaGetErrorString(e);
+    b->jit_mode = -1;
+  }
   TFQG_CUDA(launch_simulate(mode, b->bd, *a, grid, smem, state_amps, s));
   return grid;
 }
@@ -653,6 +666,40 @@ int tfqg_noisy_expectation(const char* const* programs,
   rc = tfqg_batch_noisy_expectation(b, symbol_values, num_samples, seed,
                                     expectations, 0, nullptr);
   tfqg_batch_destroy(b);
+  return rc;
+}
+
+// Run-time specialization control: mode -1 off, 0 automatic, 1 forced, any
+// other value leaves it unchanged.
+// Returns the number of sub-pass signatures; bit m of `active` is set when
+// the specialized module of SimMode m is loaded, `err` receives the last specialization error.
+int tfqg_internal_batch_jit(void* batch, int mode, int32_t* nsig, int32_t* active,
+                            char* err, int64_t err_size) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  if (!b) return kInvalidArgument;
+  if (mode >= -1 && mode <= 1) b->jit_mode = mode;
+  if (nsig) *nsig = int32_t(b->jit_signatures.size());
+  if (active) {
+    *active = 0;
+    for (int m = 0; m < 5; ++m)
+      if (b->jit_module[m]) *active |= 1 << m;
+  }
+  if (err && err_size > 0) {
+    strncpy(err, b->jit_error.c_str(), size_t(err_size - 1));
+    err[err_size - 1] = 0;
+  }
+  return 0;
+}
+
+// Generates and compiles the batch's specialized module on the host only.
+int tfqg_internal_jit_compile_check(void* batch, int mode, char* err, int64_t err_size) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  std::string log;
+  int rc = jit_compile_check(b, mode, &log);
+  if (err && err_size > 0) {
+    strncpy(err, log.c_str(), size_t(err_size - 1));
+    err[err_size - 1] = 0;
+  }
   return rc;
 }
 

@@ -1,7 +1,9 @@
 // Launch interface of the sm_103a kernels (kernels.cu), used by the C ABI.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
 #include <stdint.h>
+#endif
 
 #include "tfqg_types.h"
 
@@ -55,6 +57,7 @@ struct RunArgs {
 // Threads per CTA of the simulation kernel.
 constexpr int kSimThreads = 512;
 
+#ifndef __CUDACC_RTC__
 cudaError_t launch_build_matrices(const BatchDevice& b, const RunArgs& a,
                                   bool with_grads, cudaStream_t s);
 // Shared memory (bytes) the simulation kernel needs for this batch.
@@ -67,5 +70,19 @@ cudaError_t launch_simulate(int mode, const BatchDevice& b, const RunArgs& a,
                             cudaStream_t s);
 cudaError_t launch_noisy_finalize(const BatchDevice& b, const RunArgs& a,
                                   cudaStream_t s);
+
+// Per-mode interpreter kernels (sim_<mode>.cu): kernel address and launcher.
+#define TFQG_SIM_DECL(name)                                                     \
+  const void* sim_kernel_##name();                                              \
+  cudaError_t sim_launch_##name(const BatchDevice& b, const RunArgs& a, int grid, \
+                                size_t smem, int state_amps, int nstates,       \
+                                cudaStream_t s);
+TFQG_SIM_DECL(expect)
+TFQG_SIM_DECL(state)
+TFQG_SIM_DECL(sample)
+TFQG_SIM_DECL(adjoint)
+TFQG_SIM_DECL(noisy)
+#undef TFQG_SIM_DECL
+#endif  // __CUDACC_RTC__
 
 }  // namespace tfqg

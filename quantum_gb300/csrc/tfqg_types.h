@@ -6,7 +6,11 @@
 // first qubit is the most significant bit, circuit_parser_qsim.cc:161 maps
 // qubit q to simulator index n-q-1).  Bit positions below are these "bits".
 #pragma once
+#ifdef __CUDACC_RTC__
+#include "rtc_types.h"
+#else
 #include <stdint.h>
+#endif
 
 namespace tfqg {
 
@@ -148,5 +152,26 @@ struct DevRow {
   uint64_t mat_offset;   // first matrix slot (float2[16] each) of this row
   uint64_t dmat_offset;  // first derivative matrix slot of this row
 };
+
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+#define TFQG_TYPES_HD __host__ __device__ __forceinline__
+#else
+#define TFQG_TYPES_HD inline
+#endif
+
+// Packed op code (one 32-bit word per staged op):
+//   bits 0-2 type, 3-5 class, 6-7 j0, 8-9 j1, 10-13 kmask, 14-17 kval,
+//   18-19 ngrad, 20 has non-register controls, 21 single register control,
+//   22-23 that control's register bit, 24 its value.
+TFQG_TYPES_HD uint32_t op_code(const DevOp& op) {
+  uint32_t km = op.kmask & 15u, kv = op.kval & 15u;
+  uint32_t single = km && !(km & (km - 1u));
+  uint32_t jc = 0;
+  if (single) { while (!((km >> jc) & 1u)) ++jc; }
+  uint32_t cv = single ? ((kv >> jc) & 1u) : 0u;
+  return uint32_t(op.type & 7) | uint32_t(op.cls & 7) << 3 | uint32_t(op.t0 & 3) << 6 |
+         uint32_t(op.t1 & 3) << 8 | km << 10 | kv << 14 | uint32_t(op.ngrad & 3) << 18 |
+         uint32_t((op.lcmask | op.gcmask) != 0) << 20 | single << 21 | jc << 22 | cv << 24;
+}
 
 }  // namespace tfqg
