@@ -16,7 +16,6 @@ its own batch of 256 circuits (weak scaling, no collective on the data path).
 import argparse
 import ctypes
 import json
-import math
 import os
 import subprocess
 import sys
@@ -121,21 +120,31 @@ def workload(seed, batch=None):
     return workloads.adjoint_hea(batch or BATCH, NQ, DEPTH, seed=seed)
 
 
-def flop_per_circuit(w):
-    """Algorithmic flops of one step per circuit (dense 2^k gate matvecs):
-    expectation = forward + terms; adjoint = forward + 2x uncompute +
-    derivative matvec and inner product per parameter + lambda terms."""
+def adjoint_flop_per_circuit(w):
+    """Algorithmic flops of one adjoint launch per circuit: the forward
+    recompute the reference's gradient op also performs
+    (tfq_adj_grad_op.cc:199-214), the psi and lambda uncompute (2x forward),
+    one derivative matvec plus inner product per parameter gate, and the
+    lambda accumulation (16 * 2^n per term)."""
     N = 2 ** w["n"]
     n, d = w["n"], w["depth"]
     g1, g2 = 2 * n * d, (n - 1) * d
     f_fwd = (g1 * 8 * 2 + g2 * 8 * 4) * N
-    terms = 2 * n - 1
-    f_exp = f_fwd + terms * 8 * N
-    f_adj = 3 * f_fwd + g1 * (8 * 2 * N + 8 * N) + terms * 16 * N
-    return f_exp + f_adj
+    return 3 * f_fwd + g1 * (8 * 2 * N + 8 * N) + (2 * n - 1) * 16 * N
 
 
-def state_bytes_per_circuit(batch_obj_passes, n):
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "tfqg_jit_adjoint_adjoint_hea_16q.md")
+
+
+def profiled_traffic_per_circuit():
+    """DRAM bytes (read + write) per circuit of the adjoint launch, from the
+    committed ncu summary (a line `dram_bytes_per_circuit: <int>`)."""
+    try:
+        for ln in open(PROFILE_TRAFFIC):
+            if ln.strip().startswith("dram_bytes_per_circuit:"):
+                return int(ln.split(":", 1)[1].strip())
+    except OSError:
+        pass
     return None
 
 
@@ -341,23 +350,23 @@ def main():
     adj_kernel = ("tfqg_jit_adjoint (run-time specialized)" if "adjoint" in spec_modes
                   else "simulate_adjoint_kernel (interpreter)")
     adj_mean_ms = float(np.mean(adj_ms))
-    flop = flop_per_circuit(w)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    # state traffic the pass schedule moves per circuit between the per-CTA
-    # global slots and shared memory (read + write of psi, lambda)
-    sv = 8 * 2 ** NQ
-    passes = int(os.environ.get("TFQG_BENCH_PASSES", "0"))
+    hbm_peak = peaks.get("hbm_gbs")
+    hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else "fallback 6800 GB/s"
+    hbm_peak = hbm_peak or 6800.0
     props = torch.cuda.get_device_properties(dev)
-    sm_clock = clk.get("sm_mhz") or 1900.0
+    sm_clock = clk.get("sm_mhz") or peaks.get("sm_max_mhz") or 2070.0
+    # FP32 CUDA-core peak: 128 FMA lanes per SM, 2 flop per FMA
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_clock * 1e6 / 1e12
-    adj_flop = flop - ((2 * NQ * DEPTH * 8 * 2 + (NQ - 1) * DEPTH * 8 * 4) * 2 ** NQ + (2 * NQ - 1) * 8 * 2 ** NQ)
-    achieved_tflops = adj_flop * BATCH / (adj_mean_ms / 1e3) / 1e12
-    launches = 4
+    adj_flop = adjoint_flop_per_circuit(w) * BATCH
+    achieved_tflops = adj_flop / (adj_mean_ms / 1e3) / 1e12
+    tpc = profiled_traffic_per_circuit()
+    traffic = tpc * BATCH if tpc else None
+    launches = 4  # per step: build matrices + simulate, for each of the two ops
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
@@ -370,15 +379,25 @@ def main():
         "gpu_launches": launches * args.steps,
         "specialization": {"signatures": nsig, "modes": sorted(spec_modes),
                            "error": spec_err or None},
-        "roofline": {"bound": "hbm", "kernel": adj_kernel,
-                     "achieved": None, "peak": hbm_peak, "unit": "GB/s", "frac": None,
-                     "traffic": None,
-                     "note": "the 16-qubit adjoint sweep is FP32/shared-memory bound; see compute"},
-        "compute": {"kernel": adj_kernel, "ms_per_launch": adj_mean_ms,
-                    "algorithmic_tflop_per_launch": adj_flop * BATCH / 1e12,
-                    "achieved_tflops": achieved_tflops,
-                    "fp32_peak_tflops_at_measured_clock": fp32_peak,
-                    "frac": achieved_tflops / fp32_peak},
+        "roofline": {
+            "bound": "fp32", "kernel": adj_kernel,
+            "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": achieved_tflops / fp32_peak, "traffic": traffic,
+            "algorithmic": f"{adjoint_flop_per_circuit(w) / 1e9:.4f} GFLOP per circuit "
+                           f"x {BATCH} circuits per launch",
+            "peak_source": f"derived: {props.multi_processor_count} SMs x 128 FP32 lanes x 2 flop "
+                           f"x {sm_clock:.0f} MHz (median SM clock sampled in the timed region); "
+                           "MEASURED_PEAKS.json holds no FP32 CUDA-core figure",
+            "why_not_hbm_or_tensor": "the 512 KB state of a 16-qubit circuit is streamed "
+                                     "between a per-CTA slot and shared memory; DRAM "
+                                     "traffic is small (see hbm) and complex64 gate "
+                                     "arithmetic runs on the FP32 pipe",
+            "hbm": {"achieved": (traffic / (adj_mean_ms / 1e3) / 1e9) if traffic else None,
+                    "peak": hbm_peak, "unit": "GB/s",
+                    "frac": (traffic / (adj_mean_ms / 1e3) / 1e9 / hbm_peak) if traffic else None,
+                    "peak_source": hbm_src,
+                    "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                                      "per circuit, scaled to the launch"}},
         "expectation_ms": float(np.mean(exp_ms)), "adjoint_ms": adj_mean_ms,
         "clocks": clk, "accuracy": err, "plain_gpu": plain,
         "wall_s_timed": wall,
@@ -386,7 +405,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import cpu_port
         threads = cpu_port.num_threads()
-        sample = 2 * threads
+        sample = min(BATCH, 16 * threads)  # about 10 s of host work
         flat = cpu_port.Flat(w["programs"][:sample], w["symbol_names"],
                              w["symbol_values"][:sample], w["pauli_sums"][:sample])
         t0 = time.perf_counter()
