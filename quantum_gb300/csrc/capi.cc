@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -705,6 +706,17 @@ int tfqg_internal_jit_compile_check(void* batch, int mode, char* err, int64_t er
 
 // Bytes of compiled tables uploaded to the device per batch (benchmark
 // accounting of host->device traffic).
+int tfqg_internal_batch_row_costs(void* batch, double* costs) {
+  const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
+  if (!b || (b->B > 0 && !costs)) return kInvalidArgument;
+  for (int64_t i = 0; i < b->B; ++i) {
+    const DevRow& r = b->rows[size_t(i)];
+    const DevProgram& p = b->programs[r.program];
+    costs[i] = r.n > 0 ? double(p.num_gates + 1) * std::ldexp(1.0, r.n) : 0.0;
+  }
+  return 0;
+}
+
 int64_t tfqg_internal_batch_table_bytes(void* batch) {
   tfqg_batch* b = static_cast<tfqg_batch*>(batch);
   size_t bytes = 0;
