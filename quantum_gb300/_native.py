@@ -122,7 +122,8 @@ def string_array(items):
 
 
 # -- internal controls (tests and benchmarks) -------------------------------
-SIM_MODES = {"expect": 0, "state": 1, "sample": 2, "adjoint": 3, "noisy": 4}
+SIM_MODES = {"expect": 0, "state": 1, "sample": 2, "adjoint": 3, "noisy": 4,
+             "wide": 5}
 
 
 def batch_specialization(handle, mode=None):
@@ -130,7 +131,8 @@ def batch_specialization(handle, mode=None):
 
     mode: None leaves it unchanged, -1 turns it off, 0 automatic, 1 forced.
     Returns (signatures, active_modes, last_error): active_modes is the set
-    of SimMode names whose specialized module is loaded."""
+    of module names ("expect" ... "noisy", "wide" for the wide-row pass)
+    whose specialized module is loaded."""
     L = lib()
     f = L.tfqg_internal_batch_jit
     f.argtypes = [c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int32),
@@ -155,3 +157,20 @@ def specialization_compile_check(handle, mode):
     rc = f(handle, SIM_MODES[mode], err, 16384)
     if rc != 0:
         raise _ERRORS.get(rc, InternalError)(err.value.decode("utf-8", "replace"))
+
+
+def set_wide_min_qubits(n):
+    """Qubit count from which forward-mode rows of batches created from now
+    on run as wide rows (the whole grid on one state); returns the previous
+    value."""
+    f = lib().tfqg_internal_set_wide_min_qubits
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return f(int(n))
+
+
+def batch_wide_rows(handle):
+    f = lib().tfqg_internal_batch_wide_rows
+    f.argtypes = [c_void_p]
+    f.restype = ctypes.c_int
+    return f(handle)

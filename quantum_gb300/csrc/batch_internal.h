@@ -47,7 +47,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Offsets of the device tables inside one packed blob.
 struct TableOffsets {
-  size_t prog, rows, gates, pass, ops, terms, chan, kraus, gc, order, meas, mterms;
+  size_t prog, rows, gates, pass, ops, terms, chan, kraus, gc, order, order_fwd, meas, mterms;
 };
 
 int set_last_error(int code, const std::string& msg);
@@ -61,6 +61,12 @@ struct tfqg_batch {
   int max_resident_n = -1;   // largest resident row (-1: none)
   bool any_streamed = false;
   int max_streamed_n = 0;
+  // forward modes run wide rows (n >= kWideMinQubits) on the whole grid and
+  // the other rows through the persistent kernel's queue (order_fwd)
+  std::vector<int32_t> wide_rows;
+  int max_wide_n = 0;
+  bool any_streamed_fwd = false;
+  int max_streamed_n_fwd = 0;
   int max_grads = 0;
   int64_t total_gates = 0, total_grads = 0;
 
@@ -75,21 +81,24 @@ struct tfqg_batch {
   std::vector<float2> kraus;
   std::vector<int32_t> grad_cols;
   std::vector<int32_t> order;
+  std::vector<int32_t> order_fwd;
   std::vector<tfqg::DevMeas> meas;
   std::vector<tfqg::DevMeasTerm> meas_terms;
 
   // run-time specialization (jit.cc)
   std::vector<std::vector<uint32_t>> jit_signatures;
   int jit_mode = 0;            // -1 off, 0 automatic, 1 forced
-  bool jit_loaded[5] = {};     // compile attempted, per SimMode
-  std::shared_ptr<void> jit_module[5];
+  bool jit_loaded[6] = {};     // compile attempted, per SimMode and wide pass
+  std::shared_ptr<void> jit_module[6];
   std::string jit_error;
 
   // device state
   std::mutex mu;
   int device = -1;
   tfqg::DevBuf tables, mats, dmats, work, counter, values, out, aux, aux2;
+  tfqg::DevBuf wide_state, wide_acc;
   tfqg::BatchDevice bd;
+  const int32_t* d_order_fwd = nullptr;
 };
 
 namespace tfqg {

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <memory>
 #include <mutex>
@@ -33,6 +34,14 @@ int fail(int code, const std::string& msg) {
 }  // namespace
 
 int tfqg::set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+
+namespace {
+
+std::atomic<int> g_wide_min_qubits{kWideMinQubits};
+
+int wide_min_qubits() { return g_wide_min_qubits.load(); }
+
+}  // namespace
 
 namespace {
 
@@ -240,6 +249,26 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   };
   std::stable_sort(b->order.begin(), b->order.end(),
                    [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
+  // wide rows: in the forward modes the whole grid simulates them one by one
+  const int wide_min = std::max(wide_min_qubits(), kStreamTileBits + 2);
+  auto is_wide = [&](const DevProgram& p) {
+    return p.n >= wide_min && !p.resident && p.fwd_pass_begin != p.fwd_pass_end;
+  };
+  for (const int32_t i : b->order) {
+    const DevProgram& p = b->programs[b->rows[i].program];
+    if (is_wide(p)) continue;
+    b->order_fwd.push_back(i);
+    if (p.n > 0 && !p.resident) {
+      b->any_streamed_fwd = true;
+      b->max_streamed_n_fwd = std::max(b->max_streamed_n_fwd, int(p.n));
+    }
+  }
+  for (int64_t i = 0; i < batch; ++i) {
+    const DevProgram& p = b->programs[b->rows[i].program];
+    if (!is_wide(p)) continue;
+    b->wide_rows.push_back(int32_t(i));
+    b->max_wide_n = std::max(b->max_wide_n, int(p.n));
+  }
   jit_assign_signatures(b);
   if (b->max_grads > 8192)
     throw Error(kResourceExhausted,
@@ -267,6 +296,8 @@ void ensure_device(tfqg_batch* b, cudaStream_t s) {
                             cudaMemcpyHostToDevice, s));
   TFQG_CUDA(cudaStreamSynchronize(s));  // blob is a temporary
   b->bd = table_view(b, static_cast<unsigned char*>(b->tables.p), o);
+  b->d_order_fwd = reinterpret_cast<const int32_t*>(
+      static_cast<unsigned char*>(b->tables.p) + o.order_fwd);
   b->device = dev;
 }
 
@@ -284,6 +315,7 @@ TableOffsets tfqg::pack_tables(const tfqg_batch* b, std::vector<unsigned char>* 
   o.kraus = put(blob, b->kraus);
   o.gc = put(blob, b->grad_cols);
   o.order = put(blob, b->order);
+  o.order_fwd = put(blob, b->order_fwd);
   o.meas = put(blob, b->meas);
   o.mterms = put(blob, b->meas_terms);
   blob->resize(align256(blob->size()));
@@ -306,6 +338,7 @@ BatchDevice tfqg::table_view(const tfqg_batch* b, unsigned char* base,
   d.meas = reinterpret_cast<const DevMeas*>(base + o.meas);
   d.meas_terms = reinterpret_cast<const DevMeasTerm*>(base + o.mterms);
   d.num_rows = int32_t(b->B);
+  d.num_queue = int32_t(b->B);
   d.num_ops = int32_t(b->n_ops);
   d.num_symbols = int32_t(b->P);
   d.max_n = b->max_n;
@@ -342,35 +375,129 @@ const float* prepare(tfqg_batch* b, const float* values, int device_buffers,
   return dvals;
 }
 
+// Grid of a kernel with `threads` per CTA: resident CTAs per SM x SMs.
+int occupancy_grid(const void* k, int threads, size_t smem, int dev) {
+  int sms = 0, per_sm = 0;
+  TFQG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  TFQG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  TFQG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem));
+  return sms * std::max(per_sm, 1);
+}
+
+// Forward-mode work of the wide rows, one row after another on stream s:
+// every pass of a row is one launch over all SMs, then the row's
+// measurement, state padding or sampling.
+void run_wide(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a,
+              cudaStream_t s) {
+  const int dev = b->device;
+  const int state_amps = 1 << kStreamTileBits;
+  const size_t smem = sim_smem_bytes(kModeState, -1, true, 0);
+  cudaKernel_t jk = jit_kernel(b, kJitWide, dev);
+  int grid = jk ? jit_grid(jk, smem, dev, kWideThreads)
+                : occupancy_grid(sim_kernel_wide(), kWideThreads, smem, dev);
+  const int mgrid = occupancy_grid(wide_measure_kernel_ptr(), kWideThreads, smem, dev);
+  int sms = 0;
+  TFQG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  for (const int32_t row : b->wide_rows) {
+    const DevRow& r = b->rows[size_t(row)];
+    const DevProgram& p = b->programs[r.program];
+    const int n = p.n;
+    float2* psi;
+    if (mode == kModeState) {
+      psi = a->out_state + (int64_t(row) << b->max_n);
+    } else {
+      b->wide_state.reserve((size_t(1) << b->max_wide_n) * sizeof(float2), dev);
+      psi = static_cast<float2*>(b->wide_state.p);
+    }
+    for (uint32_t q = p.fwd_pass_begin; q < p.fwd_pass_end; ++q) {
+      const int init = q == p.fwd_pass_begin ? 1 : 0;
+      if (jk) {
+        cudaError_t e = jit_launch_wide(jk, bd, *a, row, int(q), init, psi, grid, smem,
+                                        state_amps, s);
+        if (e == cudaSuccess) continue;
+        // a rejected launch (nothing ran): interpreter from here on
+        cudaGetLastError();
+        b->jit_error = std::string("specialized launch rejected: ") + cudaGetErrorString(e);
+        b->jit_mode = -1;
+        jk = nullptr;
+        grid = occupancy_grid(sim_kernel_wide(), kWideThreads, smem, dev);
+      }
+      TFQG_CUDA(sim_launch_wide(bd, *a, row, int(q), init, psi, grid, smem, state_amps, s));
+    }
+    if (mode == kModeExpect) {
+      int term0 = 0, term1 = 0;
+      if (r.meas_begin != r.meas_end) {
+        term0 = int(b->meas[r.meas_begin].begin);
+        term1 = int(b->meas[r.meas_end - 1].end);
+      }
+      const size_t nacc = 2 * size_t(term1 - term0);
+      b->wide_acc.reserve((nacc + size_t(b->n_ops)) * sizeof(double), dev);
+      double* wacc = static_cast<double*>(b->wide_acc.p);
+      if (nacc) TFQG_CUDA(cudaMemsetAsync(wacc, 0, nacc * sizeof(double), s));
+      for (uint32_t mp = r.meas_begin; mp < r.meas_end; ++mp)
+        TFQG_CUDA(launch_wide_measure(bd, *a, row, int(mp), psi, wacc, term0, mgrid, smem,
+                                      state_amps, s));
+      TFQG_CUDA(launch_wide_expect_finalize(bd, *a, row, wacc, term0, wacc + nacc, s));
+    } else if (mode == kModeState) {
+      const int64_t N = int64_t(1) << n, M = int64_t(1) << b->max_n;
+      const float2 pad = make_float2(-2.f, 0.f);
+      TFQG_CUDA(launch_fill(psi + N, M - N, pad, pad, sms * 4, s));
+    } else {
+      const size_t nch = size_t(1) << (n - kStreamTileBits);
+      b->wide_acc.reserve(nch * sizeof(double), dev);
+      double* csum = static_cast<double*>(b->wide_acc.p);
+      TFQG_CUDA(launch_wide_chunk_sums(psi, n, csum, sms * 4, s));
+      TFQG_CUDA(launch_wide_sample(bd, *a, row, psi, n, csum, s));
+    }
+  }
+}
+
 int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
-  const int max_grads = mode == kModeAdjoint ? b->max_grads : 0;
-  size_t smem = sim_smem_bytes(mode, b->max_resident_n, b->any_streamed, max_grads);
-  if (smem > 227 * 1024)
-    throw Error(kResourceExhausted, "shared memory request too large");
-  cudaKernel_t jk = jit_kernel(b, mode, b->device);
-  int grid = jk ? jit_grid(jk, smem, b->device) : sim_grid_size(mode, smem);
-  int64_t units = mode == kModeNoisy ? a->total_traj : b->B;
-  if (units < grid) grid = int(std::max<int64_t>(units, 1));
-  if (b->any_streamed) {
-    int64_t per = int64_t(1) << b->max_streamed_n;
-    if (mode == kModeAdjoint) per *= 2;
-    a->slot_amps = per;
-    b->work.reserve(size_t(per) * grid * sizeof(float2), b->device);
-    a->work = static_cast<float2*>(b->work.p);
+  // forward modes: wide rows run on the whole grid, the rest in the queue
+  const bool fwd = mode == kModeExpect || mode == kModeState || mode == kModeSample;
+  const bool split = fwd && !b->wide_rows.empty();
+  BatchDevice bd = b->bd;
+  if (split) {
+    bd.order = b->d_order_fwd;
+    bd.num_queue = int32_t(b->order_fwd.size());
   }
-  TFQG_CUDA(cudaMemsetAsync(a->counter, 0, sizeof(int), s));
-  int state_amps = sim_state_amps(b->max_resident_n, b->any_streamed);
-  if (jk) {
-    cudaError_t e = jit_launch(jk, b->bd, *a, grid, smem, state_amps,
-                               mode == kModeAdjoint ? 2 : 1, s);
-    if (e == cudaSuccess) return grid;
-    // a rejected launch (nothing ran): record why, stop specializing this
-    // batch and run the interpreter instead
-    cudaGetLastError();
-    b->jit_error = std::string("specialized launch rejected: ") + cudaGetErrorString(e);
-    b->jit_mode = -1;
+  const bool any_streamed = split ? b->any_streamed_fwd : b->any_streamed;
+  const int max_streamed_n = split ? b->max_streamed_n_fwd : b->max_streamed_n;
+  int grid = 0;
+  if (mode == kModeNoisy || bd.num_queue > 0) {
+    const int max_grads = mode == kModeAdjoint ? b->max_grads : 0;
+    size_t smem = sim_smem_bytes(mode, b->max_resident_n, any_streamed, max_grads);
+    if (smem > 227 * 1024)
+      throw Error(kResourceExhausted, "shared memory request too large");
+    cudaKernel_t jk = jit_kernel(b, mode, b->device);
+    grid = jk ? jit_grid(jk, smem, b->device, kSimThreads) : sim_grid_size(mode, smem);
+    int64_t units = mode == kModeNoisy ? a->total_traj : bd.num_queue;
+    if (units < grid) grid = int(std::max<int64_t>(units, 1));
+    if (any_streamed) {
+      int64_t per = int64_t(1) << max_streamed_n;
+      if (mode == kModeAdjoint) per *= 2;
+      a->slot_amps = per;
+      b->work.reserve(size_t(per) * grid * sizeof(float2), b->device);
+      a->work = static_cast<float2*>(b->work.p);
+    }
+    TFQG_CUDA(cudaMemsetAsync(a->counter, 0, sizeof(int), s));
+    int state_amps = sim_state_amps(b->max_resident_n, any_streamed);
+    bool launched = false;
+    if (jk) {
+      cudaError_t e = jit_launch(jk, bd, *a, grid, smem, state_amps,
+                                 mode == kModeAdjoint ? 2 : 1, s);
+      launched = e == cudaSuccess;
+      if (!launched) {
+        // a rejected launch (nothing ran): record why, stop specializing
+        // this batch and run the interpreter instead
+        cudaGetLastError();
+        b->jit_error = std::string("specialized launch rejected: ") + cudaGetErrorString(e);
+        b->jit_mode = -1;
+      }
+    }
+    if (!launched) TFQG_CUDA(launch_simulate(mode, bd, *a, grid, smem, state_amps, s));
   }
-  TFQG_CUDA(launch_simulate(mode, b->bd, *a, grid, smem, state_amps, s));
+  if (split) run_wide(b, mode, bd, a, s);
   return grid;
 }
 
@@ -682,7 +809,7 @@ int tfqg_internal_batch_jit(void* batch, int mode, int32_t* nsig, int32_t* activ
   if (nsig) *nsig = int32_t(b->jit_signatures.size());
   if (active) {
     *active = 0;
-    for (int m = 0; m < 5; ++m)
+    for (int m = 0; m < kJitModes; ++m)
       if (b->jit_module[m]) *active |= 1 << m;
   }
   if (err && err_size > 0) {
@@ -706,6 +833,19 @@ int tfqg_internal_jit_compile_check(void* batch, int mode, char* err, int64_t er
 
 // Bytes of compiled tables uploaded to the device per batch (benchmark
 // accounting of host->device traffic).
+// Qubit count from which forward-mode rows run as wide rows, for batches
+// created after the call (clamped to at least the streamed tile + 2);
+// returns the previous value.
+int tfqg_internal_set_wide_min_qubits(int n) {
+  return g_wide_min_qubits.exchange(n);
+}
+
+// Number of wide rows of a batch (forward modes).
+int tfqg_internal_batch_wide_rows(void* batch) {
+  const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
+  return b ? int(b->wide_rows.size()) : -1;
+}
+
 int tfqg_internal_batch_row_costs(void* batch, double* costs) {
   const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
   if (!b || (b->B > 0 && !costs)) return kInvalidArgument;

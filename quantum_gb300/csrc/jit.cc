@@ -40,9 +40,10 @@ namespace {
 
 constexpr int kMaxSignatures = 512;
 
-const char* kModeNames[5] = {"tfqg_jit_expect", "tfqg_jit_state",
-                             "tfqg_jit_sample", "tfqg_jit_adjoint",
-                             "tfqg_jit_noisy"};
+// kernel names per SimMode, then the wide-row forward pass
+const char* kModeNames[kJitModes] = {"tfqg_jit_expect", "tfqg_jit_state",
+                                     "tfqg_jit_sample", "tfqg_jit_adjoint",
+                                     "tfqg_jit_noisy", "tfqg_jit_wide"};
 const char* kModeEnums[5] = {"kModeExpect", "kModeState", "kModeSample",
                              "kModeAdjoint", "kModeNoisy"};
 
@@ -384,10 +385,16 @@ std::string jit_source(const tfqg_batch* b, int mode) {
       o << "      case " << id << ": jit_sub_" << id
         << "(so, lo, T, base, sto, rbits, rbuf); break;\n";
   o << "      default: break;\n    }\n    (void)nops;\n  }\n};\n\n}  // namespace\n\n";
-  o << "extern \"C\" __global__ void __launch_bounds__(kSimThreads, 1) " << kModeNames[mode]
-    << "(BatchDevice b, RunArgs a, int state_amps, int nstates) {\n"
-       "  simulate_body<"
-    << kModeEnums[mode] << ", JitExec>(b, a, state_amps, nstates);\n}\n";
+  if (mode == kJitWide)
+    o << "extern \"C\" __global__ void __launch_bounds__(kWideThreads, 2) " << kModeNames[mode]
+      << "(BatchDevice b, RunArgs a, int row, int pass, int init, float2* psi,"
+         " int state_amps) {\n"
+         "  wide_pass_body<JitExec>(b, a, row, pass, init, psi, state_amps);\n}\n";
+  else
+    o << "extern \"C\" __global__ void __launch_bounds__(kSimThreads, 1) " << kModeNames[mode]
+      << "(BatchDevice b, RunArgs a, int state_amps, int nstates) {\n"
+         "  simulate_body<"
+      << kModeEnums[mode] << ", JitExec>(b, a, state_amps, nstates);\n}\n";
   o << "}  // namespace tfqg\n";
   return o.str();
 }
@@ -409,7 +416,8 @@ bool jit_enabled_for(const tfqg_batch* b) {
 // batch's module on first use; nullptr when specialization is off or fails
 // (the caller then uses the interpreter).
 cudaKernel_t jit_kernel(tfqg_batch* b, int mode, int dev) {
-  if (!jit_enabled_for(b) || dev < 0 || dev >= 64 || mode < 0 || mode > 4) return nullptr;
+  if (!jit_enabled_for(b) || dev < 0 || dev >= 64 || mode < 0 || mode >= kJitModes)
+    return nullptr;
   if (!b->jit_loaded[mode]) {
     b->jit_loaded[mode] = true;  // one attempt per batch and mode
     try {
@@ -472,7 +480,7 @@ cudaKernel_t jit_kernel(tfqg_batch* b, int mode, int dev) {
 // Generates and compiles the batch's specialized source without loading it
 // (no GPU needed).  Returns 0 on success; `log` receives the error text.
 int jit_compile_check(tfqg_batch* b, int mode, std::string* log) {
-  if (mode < 0 || mode > 4) return kInvalidArgument;
+  if (mode < 0 || mode >= kJitModes) return kInvalidArgument;
   try {
     std::vector<char> cubin = nvrtc_compile(jit_source(b, mode));
     return cubin.empty() ? kInternal : 0;
@@ -482,13 +490,13 @@ int jit_compile_check(tfqg_batch* b, int mode, std::string* log) {
   }
 }
 
-int jit_grid(cudaKernel_t k, size_t smem, int dev) {
+int jit_grid(cudaKernel_t k, size_t smem, int dev, int threads) {
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       int(smem), dev) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per_sm, reinterpret_cast<const void*>(k), kSimThreads, smem) != cudaSuccess) {
+          &per_sm, reinterpret_cast<const void*>(k), threads, smem) != cudaSuccess) {
     cudaGetLastError();
     per_sm = 1;
   }
@@ -504,6 +512,16 @@ cudaError_t jit_launch(cudaKernel_t k, const BatchDevice& bd, const RunArgs& a,
   void* args[] = {&b, &ra, &state_amps, &nstates};
   return cudaLaunchKernel(reinterpret_cast<const void*>(k), dim3(grid),
                           dim3(kSimThreads), args, smem, s);
+}
+
+cudaError_t jit_launch_wide(cudaKernel_t k, const BatchDevice& bd, const RunArgs& a,
+                            int row, int pass, int init, float2* psi, int grid,
+                            size_t smem, int state_amps, cudaStream_t s) {
+  BatchDevice b = bd;
+  RunArgs ra = a;
+  void* args[] = {&b, &ra, &row, &pass, &init, &psi, &state_amps};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(k), dim3(grid),
+                          dim3(kWideThreads), args, smem, s);
 }
 
 }  // namespace tfqg

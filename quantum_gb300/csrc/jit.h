@@ -10,6 +10,10 @@ struct tfqg_batch;
 
 namespace tfqg {
 
+// Specialized modules: one per SimMode (0..4), plus the wide-row forward pass.
+constexpr int kJitWide = 5;
+constexpr int kJitModes = 6;
+
 // Records each sub-pass header's signature id (host only; cheap).
 void jit_assign_signatures(tfqg_batch* b);
 // Generated CUDA source of the batch's executors and kernels.
@@ -18,9 +22,12 @@ bool jit_enabled_for(const tfqg_batch* b);
 // Specialized kernel for `mode` on device `dev`, or nullptr (interpreter).
 cudaKernel_t jit_kernel(tfqg_batch* b, int mode, int dev);
 int jit_compile_check(tfqg_batch* b, int mode, std::string* log);
-int jit_grid(cudaKernel_t k, size_t smem, int dev);
+int jit_grid(cudaKernel_t k, size_t smem, int dev, int threads);
 cudaError_t jit_launch(cudaKernel_t k, const BatchDevice& bd, const RunArgs& a,
                        int grid, size_t smem, int state_amps, int nstates,
                        cudaStream_t s);
+cudaError_t jit_launch_wide(cudaKernel_t k, const BatchDevice& bd, const RunArgs& a,
+                            int row, int pass, int init, float2* psi, int grid,
+                            size_t smem, int state_amps, cudaStream_t s);
 
 }  // namespace tfqg

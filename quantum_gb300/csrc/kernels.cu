@@ -8,6 +8,11 @@
 //  simulate_<mode>_kernel  the simulation kernels, one translation unit per
 //                          mode (sim_mode.cuh, sim_<mode>.cu).
 //  noisy_finalize_kernel   divides the trajectory sums by their counts.
+//  wide_*                  rows too large for one CTA (kWideMinQubits and
+//                          up): measurement passes, expectation finalize,
+//                          probability chunk sums and sampling over a state
+//                          in global memory that every CTA works on (the
+//                          forward passes are sim_wide.cu).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -100,6 +105,139 @@ __global__ void noisy_finalize_kernel(BatchDevice b, RunArgs a) {
   a.out_f[t] = reps > 0 ? float(a.acc[t] / double(reps)) : 0.f;
 }
 
+// ---- wide rows --------------------------------------------------------------
+
+__global__ void __launch_bounds__(kWideThreads, 2)
+wide_measure_kernel(BatchDevice b, RunArgs a, int row, int mp, const float2* psi,
+                    double* wacc, int term0, int state_amps) {
+  wide_measure_body(b, a, row, mp, psi, wacc, term0, state_amps);
+}
+
+// Combines the term sums of a wide row into out_f[row, :] in double, with the
+// measure_passes rules: Re(i^ny * sum) times the coefficient, identity terms
+// contribute their coefficient (util_qsim.h:152-186).
+__global__ void wide_expect_finalize_kernel(BatchDevice b, RunArgs a, int row,
+                                            const double* wacc, int term0,
+                                            double* acc) {
+  const DevRow r = b.rows[row];
+  for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x) acc[j] = 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (uint32_t mp = r.meas_begin; mp < r.meas_end; ++mp) {
+      const DevMeas M = b.meas[mp];
+      for (uint32_t i = M.begin; i < M.end; ++i) {
+        const DevTerm t = b.terms[b.meas_terms[i].term];
+        double v = 1.0;
+        if (!t.identity) {
+          const double sre = wacc[2 * (int64_t(i) - term0)];
+          const double sim = wacc[2 * (int64_t(i) - term0) + 1];
+          switch (t.ny & 3) {
+            case 0: v = sre; break;
+            case 1: v = -sim; break;
+            case 2: v = -sre; break;
+            default: v = sim; break;
+          }
+        }
+        acc[t.op] += double(t.coef) * v;
+      }
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x)
+    a.out_f[int64_t(row) * b.num_ops + j] = float(acc[j]);
+}
+
+__global__ void __launch_bounds__(256)
+wide_chunk_sums_kernel(const float2* psi, int n, double* csum) {
+  __shared__ double part[8];
+  const uint32_t nch = 1u << (n - kTile);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
+    const float4* p = reinterpret_cast<const float4*>(psi + (size_t(c) << kTile));
+    float f = 0.f;
+    for (uint32_t k = threadIdx.x; k < (1u << (kTile - 1)); k += blockDim.x) {
+      const float4 v = __ldcg(p + k);
+      f = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, f))));
+    }
+    double d = f;
+    for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) part[w] = d;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int i = 0; i < int(blockDim.x >> 5); ++i) t += part[i];
+      csum[c] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// One CTA: inclusive scan of the chunk sums, then one thread per sample finds
+// its chunk by binary search and its index by a scan inside the chunk
+// (StateSpace::Sample semantics: index x with probability |psi_x|^2; bit k
+// of x goes to column max_n - k - 1, tfq_simulate_samples_op.cc:226-243).
+__global__ void __launch_bounds__(512)
+wide_sample_kernel(BatchDevice b, RunArgs a, int row, const float2* psi, int n,
+                   double* csum) {
+  __shared__ double seg[512];
+  const uint32_t nch = 1u << (n - kTile);
+  const uint32_t per = (nch + blockDim.x - 1) / blockDim.x;
+  const uint32_t lo = min(threadIdx.x * per, nch), hi = min(lo + per, nch);
+  double run = 0.0;
+  for (uint32_t i = lo; i < hi; ++i) {
+    run += csum[i];
+    csum[i] = run;
+  }
+  seg[threadIdx.x] = run;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double off = 0.0;
+    for (uint32_t t = 0; t < blockDim.x; ++t) {
+      const double v = seg[t];
+      seg[t] = off;
+      off += v;
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = lo; i < hi; ++i) csum[i] += seg[threadIdx.x];
+  __syncthreads();
+  const double total = csum[nch - 1];
+  const int maxn = b.max_n, S = a.num_samples;
+  const uint32_t L = 1u << kTile;
+  int8_t* out = a.out_samples + int64_t(row) * S * maxn;
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    const double u = uniform01(a.seed, uint32_t(row), uint32_t(s), 0x5A3Fu) * total;
+    uint32_t c0 = 0, c1 = nch - 1;
+    while (c0 < c1) {
+      const uint32_t mid = (c0 + c1) >> 1;
+      if (csum[mid] > u) c1 = mid; else c0 = mid + 1;
+    }
+    double acc = c0 ? csum[c0 - 1] : 0.0;
+    const size_t first = size_t(c0) * L;
+    size_t x = first, last_nz = first;
+    bool found = false;
+    for (uint32_t j = 0; j < L; ++j) {
+      const float2 v = psi[first + j];
+      const double p = double(v.x) * v.x + double(v.y) * v.y;
+      if (p > 0.0) last_nz = first + j;
+      acc += p;
+      if (acc > u && p > 0.0) { x = first + j; found = true; break; }
+    }
+    if (!found) x = last_nz;
+    int8_t* o = out + int64_t(s) * maxn;
+    for (int c = 0; c < maxn; ++c) {
+      const int k = maxn - 1 - c;
+      o[c] = k >= n ? int8_t(-2) : int8_t((x >> k) & 1);
+    }
+  }
+}
+
+__global__ void fill_kernel(float2* p, int64_t count, float2 first, float2 rest) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
+       i += int64_t(gridDim.x) * blockDim.x)
+    p[i] = i == 0 ? first : rest;
+}
+
 const void* kernel_for(int mode) {
   switch (mode) {
     case kModeExpect: return sim_kernel_expect();
@@ -171,6 +309,44 @@ cudaError_t launch_noisy_finalize(const BatchDevice& b, const RunArgs& a,
   int64_t total = int64_t(b.num_rows) * b.num_ops;
   if (total == 0) return cudaSuccess;
   noisy_finalize_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(b, a);
+  return cudaGetLastError();
+}
+
+const void* wide_measure_kernel_ptr() {
+  return reinterpret_cast<const void*>(&wide_measure_kernel);
+}
+
+cudaError_t launch_wide_measure(const BatchDevice& b, const RunArgs& a, int row, int mp,
+                                const float2* psi, double* wacc, int term0, int grid,
+                                size_t smem, int state_amps, cudaStream_t s) {
+  wide_measure_kernel<<<grid, kWideThreads, smem, s>>>(b, a, row, mp, psi, wacc, term0,
+                                                      state_amps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wide_expect_finalize(const BatchDevice& b, const RunArgs& a, int row,
+                                        const double* wacc, int term0, double* scratch,
+                                        cudaStream_t s) {
+  wide_expect_finalize_kernel<<<1, 256, 0, s>>>(b, a, row, wacc, term0, scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wide_chunk_sums(const float2* psi, int n, double* csum, int grid,
+                                   cudaStream_t s) {
+  wide_chunk_sums_kernel<<<grid, 256, 0, s>>>(psi, n, csum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wide_sample(const BatchDevice& b, const RunArgs& a, int row,
+                               const float2* psi, int n, double* csum, cudaStream_t s) {
+  wide_sample_kernel<<<1, 512, 0, s>>>(b, a, row, psi, n, csum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill(float2* p, int64_t count, float2 first, float2 rest, int grid,
+                        cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  fill_kernel<<<grid, 256, 0, s>>>(p, count, first, rest);
   return cudaGetLastError();
 }
 

@@ -22,10 +22,12 @@ struct BatchDevice {
   const DevChannel* channels = nullptr;
   const float2* kraus = nullptr;
   const int32_t* grad_cols = nullptr;
-  const int32_t* order = nullptr;  // rows, most expensive first
+  const int32_t* order = nullptr;  // rows the persistent kernel takes, most
+                                   // expensive first (num_queue of them)
   const DevMeas* meas = nullptr;
   const DevMeasTerm* meas_terms = nullptr;
   int32_t num_rows = 0;
+  int32_t num_queue = 0;     // entries of `order` the persistent kernel runs
   int32_t num_ops = 0;       // pauli_sums columns
   int32_t num_symbols = 0;
   int32_t max_n = 0;
@@ -56,6 +58,12 @@ struct RunArgs {
 
 // Threads per CTA of the simulation kernel.
 constexpr int kSimThreads = 512;
+// Threads per CTA of the wide-row kernels (two CTAs per SM, so that one
+// CTA's tile loads and stores overlap the other's arithmetic).
+constexpr int kWideThreads = 256;
+// Rows of at least this many qubits run as wide rows in the forward modes:
+// the whole grid works on one state, one launch per pass.
+constexpr int kWideMinQubits = 22;
 
 #ifndef __CUDACC_RTC__
 cudaError_t launch_build_matrices(const BatchDevice& b, const RunArgs& a,
@@ -83,6 +91,31 @@ TFQG_SIM_DECL(sample)
 TFQG_SIM_DECL(adjoint)
 TFQG_SIM_DECL(noisy)
 #undef TFQG_SIM_DECL
+
+// Wide rows (kernels.cu, sim_wide.cu).  `psi` is the row's 2^n state in
+// global memory; grids are multiples of the SM count.
+const void* sim_kernel_wide();
+cudaError_t sim_launch_wide(const BatchDevice& b, const RunArgs& a, int row, int pass,
+                            int init, float2* psi, int grid, size_t smem,
+                            int state_amps, cudaStream_t s);
+const void* wide_measure_kernel_ptr();
+cudaError_t launch_wide_measure(const BatchDevice& b, const RunArgs& a, int row, int mp,
+                                const float2* psi, double* wacc, int term0, int grid,
+                                size_t smem, int state_amps, cudaStream_t s);
+// out_f[row, :] from the term sums; `scratch` holds num_ops doubles.
+cudaError_t launch_wide_expect_finalize(const BatchDevice& b, const RunArgs& a, int row,
+                                        const double* wacc, int term0, double* scratch,
+                                        cudaStream_t s);
+// csum[c] = sum of |psi|^2 over amplitudes [c * 2^13, (c + 1) * 2^13).
+cudaError_t launch_wide_chunk_sums(const float2* psi, int n, double* csum, int grid,
+                                   cudaStream_t s);
+// Draws a.num_samples samples of row `row` from psi using the chunk sums
+// (scanned in place) and writes them in the reference bit layout.
+cudaError_t launch_wide_sample(const BatchDevice& b, const RunArgs& a, int row,
+                               const float2* psi, int n, double* csum, cudaStream_t s);
+// p[i] = (i == 0 ? first : rest) for i in [0, count).
+cudaError_t launch_fill(float2* p, int64_t count, float2 first, float2 rest, int grid,
+                        cudaStream_t s);
 #endif  // __CUDACC_RTC__
 
 }  // namespace tfqg

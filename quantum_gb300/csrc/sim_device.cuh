@@ -128,7 +128,8 @@ __device__ __forceinline__ void warp_partials(double* red, int buf,
 
 __device__ __forceinline__ double red_total(const double* red, int buf, int v) {
   double s = 0.0;
-  for (int w = 0; w < kWarps; ++w) s += red[(buf * 4 + v) * kWarps + w];
+  const int nw = int(blockDim.x >> 5);  // kernels run with <= kWarps warps
+  for (int w = 0; w < nw; ++w) s += red[(buf * 4 + v) * kWarps + w];
   return s;
 }
 
@@ -842,7 +843,7 @@ __device__ void run_ops(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     __syncthreads();
     if (MODE == kModeAdjoint && int(threadIdx.x) < st->nred[rbuf]) {
       double acc = 0.0;
-      for (int w = 0; w < kWarps; ++w) acc += st->red[rbuf][threadIdx.x][w];
+      for (int w = 0; w < int(blockDim.x >> 5); ++w) acc += st->red[rbuf][threadIdx.x][w];
       sm.grad[st->red_slot[rbuf][threadIdx.x]] += acc;
     }
     if (MODE == kModeAdjoint) rbuf ^= 1;
@@ -915,7 +916,8 @@ template <int MODE, class Exec>
 __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
                            const Smem& sm, const RowCtx& rc, uint32_t pb,
                            uint32_t pe, float2* g_psi, float2* g_lam,
-                           bool init, int& rbuf) {
+                           bool init, int& rbuf, uint32_t t0 = 0,
+                           uint32_t tstride = 1) {
   const int n = rc.p.n;
   if (rc.p.resident) {
     const int T = n < kRB ? kRB : n;  // tiny states are padded to 4 bits
@@ -933,7 +935,7 @@ __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
     __syncthreads();
     const uint32_t outside = all & ~ps.tile_mask;
     const uint32_t ntiles = 1u << (n - kTile);
-    for (uint32_t t = 0; t < ntiles; ++t) {
+    for (uint32_t t = t0; t < ntiles; t += tstride) {
       const uint32_t base = deposit(t, outside);
       if (init && p == pb) tile_zero(sm.psi, base == 0);
       else tile_load(sm.psi, g_psi, sm.hi, base);
@@ -971,6 +973,32 @@ __device__ void stage_terms(const BatchDevice& b, const RunArgs& a, const Smem& 
   }
 }
 
+// Adds <psi| P_t |psi> over one tile in shared memory (N amplitudes, fixed
+// global bits `base`) to the term sums sm.macc, for the nt staged terms.
+__device__ void measure_tile(const Smem& sm, int nt, uint32_t N, uint32_t base,
+                             bool resident) {
+  const int lane = threadIdx.x & 31;
+  for (int i = 0; i < nt; ++i) {
+    if (sm.mterm[i].identity) continue;
+    const uint32_t lf = sm.mterm[i].lflip, zy = sm.mterm[i].zy;
+    float re = 0.f, im = 0.f;
+    for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+      const uint32_t y = x ^ lf;
+      const float2 av = sm.psi[swz(x)], bv = sm.psi[swz(y)];
+      const uint32_t yg = resident ? y : ((y & 31u) | sm.hi[y >> 5] | base);
+      const float sg = (__popc(yg & zy) & 1) ? -1.f : 1.f;
+      re = fmaf(sg, fmaf(av.x, bv.x, av.y * bv.y), re);
+      im = fmaf(sg, fmaf(av.x, bv.y, -av.y * bv.x), im);
+    }
+    re = warp_sum(re);
+    im = warp_sum(im);
+    if (lane == 0) {
+      atomicAdd(&sm.macc[2 * i], double(re));
+      atomicAdd(&sm.macc[2 * i + 1], double(im));
+    }
+  }
+}
+
 // Pauli-sum expectation by measurement passes (util_qsim.h:142-188): each
 // tile of the state is read once into shared memory and every term of the
 // pass whose flip bits lie in the tile is summed there.  Resident rows use
@@ -983,7 +1011,6 @@ __device__ void measure_passes(const BatchDevice& b, const RunArgs& a,
   const int n = rc.p.n;
   const bool resident = rc.p.resident;
   const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
-  const int lane = threadIdx.x & 31;
   for (uint32_t mp = rc.r.meas_begin; mp < rc.r.meas_end; ++mp) {
     const DevMeas M = b.meas[mp];
     const int nt = int(M.end - M.begin);
@@ -1006,25 +1033,7 @@ __device__ void measure_passes(const BatchDevice& b, const RunArgs& a,
         tile_load(sm.psi, g_psi, sm.hi, base);
         __syncthreads();
       }
-      for (int i = 0; i < nt; ++i) {
-        if (sm.mterm[i].identity) continue;
-        const uint32_t lf = sm.mterm[i].lflip, zy = sm.mterm[i].zy;
-        float re = 0.f, im = 0.f;
-        for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
-          const uint32_t y = x ^ lf;
-          const float2 av = sm.psi[swz(x)], bv = sm.psi[swz(y)];
-          const uint32_t yg = resident ? y : ((y & 31u) | sm.hi[y >> 5] | base);
-          const float sg = (__popc(yg & zy) & 1) ? -1.f : 1.f;
-          re = fmaf(sg, fmaf(av.x, bv.x, av.y * bv.y), re);
-          im = fmaf(sg, fmaf(av.x, bv.y, -av.y * bv.x), im);
-        }
-        re = warp_sum(re);
-        im = warp_sum(im);
-        if (lane == 0) {
-          atomicAdd(&sm.macc[2 * i], double(re));
-          atomicAdd(&sm.macc[2 * i + 1], double(im));
-        }
-      }
+      measure_tile(sm, nt, N, base, resident);
       __syncthreads();  // before the next tile overwrites sm.psi
     }
     if (threadIdx.x == 0) {
@@ -1294,12 +1303,9 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
   __syncthreads();
 }
 
-// Body of the persistent simulation kernel: lays out dynamic shared memory
-// and pulls rows (or trajectories) from the work queue.  `Exec` executes
-// sub-passes (the interpreter, or code specialized for one batch).
-template <int MODE, class Exec>
-__device__ __forceinline__ void simulate_body(BatchDevice b, RunArgs a,
-                                              int state_amps, int nstates) {
+// Dynamic shared memory layout of a simulation CTA.
+template <int MODE>
+__device__ __forceinline__ Smem carve_smem(int state_amps, int nstates) {
   Smem sm;
   sm.psi = reinterpret_cast<float2*>(smem_raw);
   sm.lam = sm.psi + state_amps;
@@ -1319,9 +1325,19 @@ __device__ __forceinline__ void simulate_body(BatchDevice b, RunArgs a,
   sm.oacc = reinterpret_cast<double*>(p);
   if (MODE == kModeExpect) p += kMaxOpsSmem * sizeof(double);
   sm.grad = reinterpret_cast<double*>(p);
+  return sm;
+}
+
+// Body of the persistent simulation kernel: lays out dynamic shared memory
+// and pulls rows (or trajectories) from the work queue.  `Exec` executes
+// sub-passes (the interpreter, or code specialized for one batch).
+template <int MODE, class Exec>
+__device__ __forceinline__ void simulate_body(BatchDevice b, RunArgs a,
+                                              int state_amps, int nstates) {
+  const Smem sm = carve_smem<MODE>(state_amps, nstates);
 
   __shared__ int s_item;
-  const int64_t total = MODE == kModeNoisy ? a.total_traj : b.num_rows;
+  const int64_t total = MODE == kModeNoisy ? a.total_traj : b.num_queue;
   while (true) {
     if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
     __syncthreads();
@@ -1340,6 +1356,80 @@ __device__ __forceinline__ void simulate_body(BatchDevice b, RunArgs a,
     }
   }
 }
+
+
+// ---------------------------------------------------------------------------
+// wide rows: one large state, every CTA of the grid works on it
+// ---------------------------------------------------------------------------
+// A wide row's state lives in global memory and each forward pass is one
+// launch: CTA c takes tiles c, c + gridDim.x, ... of the pass (tiles of one
+// pass are independent; the launch boundary orders the passes).
+
+// Forward pass `pass` of wide row `row` over the state `psi` (2^n amplitudes).
+template <class Exec>
+__device__ __forceinline__ void wide_pass_body(const BatchDevice& b, const RunArgs& a,
+                                               int row, int pass, int init, float2* psi,
+                                               int state_amps) {
+  const Smem sm = carve_smem<kModeState>(state_amps, 1);
+  RowCtx rc;
+  rc.row = row;
+  rc.traj = 0;
+  rc.r = b.rows[row];
+  rc.p = b.programs[rc.r.program];
+  int rbuf = 0;
+  run_passes<kModeState, Exec>(b, a, sm, rc, uint32_t(pass), uint32_t(pass) + 1, psi,
+                               nullptr, init != 0, rbuf, blockIdx.x, gridDim.x);
+}
+
+// Measurement pass `mp` of wide row `row`: this CTA's tiles add their term
+// sums (re, im) to wacc[2 * (term - term0) + {0, 1}] (double atomics).
+__device__ __forceinline__ void wide_measure_body(const BatchDevice& b, const RunArgs& a,
+                                                  int row, int mp, const float2* psi,
+                                                  double* wacc, int term0, int state_amps) {
+  const Smem sm = carve_smem<kModeState>(state_amps, 1);
+  RowCtx rc;
+  rc.row = row;
+  rc.traj = 0;
+  rc.r = b.rows[row];
+  rc.p = b.programs[rc.r.program];
+  const int n = rc.p.n;
+  const DevMeas M = b.meas[mp];
+  const int nt = int(M.end - M.begin);
+  stage_terms(b, a, sm, rc, M, false);
+  for (int i = threadIdx.x; i < 2 * nt; i += blockDim.x) sm.macc[i] = 0.0;
+  build_hi_table(sm.hi, M.tile_mask);
+  __syncthreads();
+  const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+  const uint32_t outside = all & ~M.tile_mask;
+  const uint32_t ntiles = 1u << (n - kTile);
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t base = deposit(t, outside);
+    tile_load(sm.psi, psi, sm.hi, base);
+    __syncthreads();
+    measure_tile(sm, nt, 1u << kTile, base, false);
+    __syncthreads();
+  }
+  double* dst = wacc + 2 * (int64_t(M.begin) - term0);
+  for (int i = threadIdx.x; i < 2 * nt; i += blockDim.x)
+    if (sm.macc[i] != 0.0) atomicAdd(dst + i, sm.macc[i]);
+}
+
+#ifndef TFQG_JIT
+// Sub-passes run by the precompiled interpreter.
+struct InterpExec {
+  static __device__ __forceinline__ void forward(uint32_t so, int T, uint32_t base,
+                                                 uint32_t sto, int nops,
+                                                 uint32_t rbits, int sig) {
+    exec_forward(so, T, base, sto, nops, rbits);
+  }
+  static __device__ __forceinline__ void backward(uint32_t so, uint32_t lo, int T,
+                                                  uint32_t base, uint32_t sto,
+                                                  int nops, uint32_t rbits,
+                                                  int rbuf, int sig) {
+    exec_backward(so, lo, T, base, sto, nops, rbits, rbuf);
+  }
+};
+#endif  // TFQG_JIT
 
 }  // namespace
 }  // namespace tfqg

@@ -23,24 +23,6 @@
 #define TFQG_CAT(a, b) TFQG_CAT2(a, b)
 
 namespace tfqg {
-namespace {
-
-// Sub-passes run by the precompiled interpreter.
-struct InterpExec {
-  static __device__ __forceinline__ void forward(uint32_t so, int T, uint32_t base,
-                                                 uint32_t sto, int nops,
-                                                 uint32_t rbits, int sig) {
-    exec_forward(so, T, base, sto, nops, rbits);
-  }
-  static __device__ __forceinline__ void backward(uint32_t so, uint32_t lo, int T,
-                                                  uint32_t base, uint32_t sto,
-                                                  int nops, uint32_t rbits,
-                                                  int rbuf, int sig) {
-    exec_backward(so, lo, T, base, sto, nops, rbits, rbuf);
-  }
-};
-
-}  // namespace
 
 __global__ void __launch_bounds__(kSimThreads, 1)
 TFQG_CAT(TFQG_CAT(simulate_, TFQG_SIM_NAME), _kernel)(BatchDevice b, RunArgs a,

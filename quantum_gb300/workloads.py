@@ -135,3 +135,43 @@ def noisy_brickwall(batch=64, n=14, depth=15, p=0.01, seed=1):
     return dict(programs=programs, symbol_names=[],
                 symbol_values=np.zeros((batch, 0), np.float32),
                 pauli_sums=[[ps] for _ in range(batch)])
+
+
+def grid_fsim(rows=5, cols=6, depth=24, seed=1):
+    """One random circuit on a rows x cols GridQubit array (30 qubits at the
+    default size). Each layer applies one of {sqrt(X), sqrt(Y), sqrt(W)} to
+    every qubit, never the gate that qubit had in the previous layer, where
+    sqrt(W) = PhasedXPow(0.25, 0.5). Then fSim(theta ~ U[1.4, 1.7],
+    phi ~ U[0.4, 0.6]) runs on one of four coupler patterns, cycled:
+    horizontal pairs at even / odd columns, then vertical pairs at even /
+    odd rows. Observable sum_i Z_i."""
+    rng = np.random.default_rng(seed)
+    qs = [S.GridQubit(r, c) for r in range(rows) for c in range(cols)]
+    at = {(q.row, q.col): q for q in qs}
+    last = [-1] * len(qs)
+    moments = []
+    for layer in range(depth):
+        one = []
+        for i, q in enumerate(qs):
+            g = int(rng.integers(3))
+            if g == last[i]:
+                g = (g + 1 + int(rng.integers(2))) % 3
+            last[i] = g
+            one.append(S.XPow(q, 0.5) if g == 0 else S.YPow(q, 0.5) if g == 1
+                       else S.PhasedXPow(q, 0.25, 0.5))
+        moments.append(one)
+        pattern = layer % 4
+        pairs = []
+        for r in range(rows):
+            for c in range(cols):
+                if pattern < 2 and c % 2 == pattern and c + 1 < cols:
+                    pairs.append((at[r, c], at[r, c + 1]))
+                if pattern >= 2 and r % 2 == pattern - 2 and r + 1 < rows:
+                    pairs.append((at[r, c], at[r + 1, c]))
+        moments.append([S.FSim(a, b, float(rng.uniform(1.4, 1.7)),
+                               float(rng.uniform(0.4, 0.6))) for a, b in pairs])
+    prog = S.serialize_circuit(S.Circuit(moments))
+    ps = S.serialize_paulisum([(1.0, [(q, "Z")]) for q in qs])
+    return dict(programs=[prog], symbol_names=[],
+                symbol_values=np.zeros((1, 0), np.float32), pauli_sums=[[ps]],
+                n=len(qs), depth=depth)

@@ -1,0 +1,110 @@
+"""Wide rows: states too large for one CTA, simulated by the whole grid one
+launch per pass (forward modes). The wide threshold is lowered here so that
+15..18-qubit rows take the path at oracle-checkable sizes. Narrow rows of
+the same batch still go through the persistent kernel. One 22-qubit row
+checks the default threshold. Tolerances as in test_gpu_parity.py."""
+
+import numpy as np
+import pytest
+from scipy import stats
+
+from oracle import tfq_oracle as O
+from quantum_gb300 import _native, ops
+from quantum_gb300 import serialize as S
+from tests.circuits import random_circuit, random_paulisum
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def wide_from_15():
+    old = _native.set_wide_min_qubits(15)
+    yield
+    _native.set_wide_min_qubits(old)
+
+
+def _inputs(rng, nqs, n_moments=5, n_ops=2, n_symbols=4):
+    names = [f"s{i}" for i in range(n_symbols)]
+    programs, psums = [], []
+    for n in nqs:
+        qs = S.GridQubit.rect(1, n)
+        programs.append(S.serialize_circuit(random_circuit(qs, n_moments, rng, names,
+                                                           p_control=0.3)))
+        psums.append([random_paulisum(qs, rng, n_terms=6) for _ in range(n_ops)])
+    values = rng.uniform(-2, 2, size=(len(nqs), n_symbols)).astype(np.float32)
+    return programs, names, values, psums
+
+
+@pytest.mark.parametrize("jit", [-1, 1])
+def test_expectation_mixed_wide_and_narrow(wide_from_15, jit):
+    rng = np.random.default_rng(12 + jit)
+    nqs = [16, 5, 17, 15, 12]
+    programs, names, values, psums = _inputs(rng, nqs)
+    b = ops.Batch(programs, names, psums)
+    assert _native.batch_wide_rows(b._h) == 3
+    _native.batch_specialization(b._h, jit)
+    got = b.expectation(values)
+    if jit == 1:
+        _, active, err = _native.batch_specialization(b._h)
+        assert "wide" in active, err
+    want = O.simulate_expectation(programs, names, values, psums)
+    np.testing.assert_allclose(got, want, atol=8e-5, rtol=0)
+
+
+def test_adjoint_batch_runs_wide_forward_and_queued_gradient(wide_from_15):
+    rng = np.random.default_rng(3)
+    programs, names, values, psums = _inputs(rng, [16, 4], n_moments=4)
+    b = ops.Batch(programs, names, psums, kind=ops.KIND_ADJOINT)
+    assert _native.batch_wide_rows(b._h) == 1
+    np.testing.assert_allclose(b.expectation(values),
+                               O.simulate_expectation(programs, names, values, psums),
+                               atol=8e-5, rtol=0)
+    dg = rng.normal(size=(2, 2)).astype(np.float32)
+    want = O.adj_grad(programs, names, values, psums, dg)
+    np.testing.assert_allclose(b.adj_grad(values, dg), want,
+                               atol=2e-5 * max(1.0, np.abs(want).max()), rtol=0)
+
+
+def test_state_with_padding(wide_from_15):
+    rng = np.random.default_rng(8)
+    programs, names, values, _ = _inputs(rng, [15, 3, 16], n_ops=0)
+    b = ops.Batch(programs, names, None)
+    assert _native.batch_wide_rows(b._h) == 2
+    got = b.state(values)
+    want = O.simulate_state(programs, names, values)
+    assert got.shape == want.shape == (3, 2 ** 16)
+    np.testing.assert_allclose(got, want, atol=1e-5, rtol=0)
+
+
+def test_samples_distribution_and_layout(wide_from_15):
+    q = S.GridQubit.rect(1, 16)
+    ops_ = [S.X(q[0]), S.X(q[3]), S.X(q[7]), S.H(q[2]), S.H(q[12])]
+    ops_ += [S.I(x) for i, x in enumerate(q) if i not in (0, 2, 3, 7, 12)]
+    wide = S.serialize_circuit(S.Circuit([ops_]))
+    small = S.serialize_circuit(S.Circuit([[S.X(S.GridQubit(0, 0)), S.I(S.GridQubit(0, 1))]]))
+    b = ops.Batch([wide, small], [], None)
+    assert _native.batch_wide_rows(b._h) == 1
+    shots = 4000
+    res = b.samples(np.zeros((2, 0), np.float32), shots, seed=11)
+    assert res.shape == (2, shots, 16)
+    # narrow row: 2 qubits, 14 leading -2 columns, then bits (q0 = 1, q1 = 0)
+    assert (res[1, :, :14] == -2).all()
+    assert (res[1, :, 14:] == np.array([1, 0])).all()
+    bits = res[0].astype(np.int64)
+    idx = (bits[:, ::-1] << np.arange(16)).sum(axis=1)  # column 15 - k holds bit k
+    (n, probs), _ = O.final_probabilities([wide, small], [], np.zeros((2, 0)))
+    support = np.nonzero(probs > 1e-6)[0]
+    assert len(support) == 4 and set(np.unique(idx)) <= set(support)
+    counts = np.array([(idx == s).sum() for s in support])
+    p = stats.chisquare(counts, probs[support] / probs[support].sum() * shots).pvalue
+    assert p > 1e-3, (counts, p)
+
+
+def test_default_threshold_22_qubits():
+    rng = np.random.default_rng(22)
+    programs, names, values, psums = _inputs(rng, [22], n_moments=2, n_ops=1)
+    b = ops.Batch(programs, names, psums)
+    assert _native.batch_wide_rows(b._h) == 1
+    np.testing.assert_allclose(b.expectation(values),
+                               O.simulate_expectation(programs, names, values, psums),
+                               atol=8e-5, rtol=0)

@@ -26,7 +26,7 @@ def _batch(kind, nqs, channels=()):
 
 
 @pytest.mark.parametrize("kind,modes", [
-    (ops.KIND_FORWARD, ["expect", "state", "sample"]),
+    (ops.KIND_FORWARD, ["expect", "state", "sample", "wide"]),
     (ops.KIND_ADJOINT, ["expect", "adjoint"]),
 ])
 def test_generated_source_compiles(kind, modes):
