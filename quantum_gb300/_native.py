@@ -148,7 +148,8 @@ def batch_specialization(handle, mode=None):
 
 def specialization_compile_check(handle, mode):
     """Generate and compile (no load, no GPU) the specialized module of
-    `mode` for a batch handle; raises with the compiler log on failure."""
+    `mode` for a batch handle. Raises with the compiler log on failure;
+    returns the log (ptxas resource usage) on success."""
     L = lib()
     f = L.tfqg_internal_jit_compile_check
     f.argtypes = [c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int64]
@@ -157,6 +158,7 @@ def specialization_compile_check(handle, mode):
     rc = f(handle, SIM_MODES[mode], err, 16384)
     if rc != 0:
         raise _ERRORS.get(rc, InternalError)(err.value.decode("utf-8", "replace"))
+    return err.value.decode("utf-8", "replace")
 
 
 def set_wide_min_qubits(n):

@@ -270,9 +270,9 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     b->max_wide_n = std::max(b->max_wide_n, int(p.n));
   }
   jit_assign_signatures(b);
-  if (b->max_grads > 8192)
+  if (b->max_grads > 6144)
     throw Error(kResourceExhausted,
-                "A circuit has more than 8192 symbolic gate parameters; the "
+                "A circuit has more than 6144 symbolic gate parameters; the "
                 "adjoint kernel keeps one accumulator per parameter in shared "
                 "memory.");
 }
@@ -470,7 +470,7 @@ int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
     if (smem > 227 * 1024)
       throw Error(kResourceExhausted, "shared memory request too large");
     cudaKernel_t jk = jit_kernel(b, mode, b->device);
-    grid = jk ? jit_grid(jk, smem, b->device, kSimThreads) : sim_grid_size(mode, smem);
+    grid = jk ? jit_grid(jk, smem, b->device, jit_threads(mode)) : sim_grid_size(mode, smem);
     int64_t units = mode == kModeNoisy ? a->total_traj : bd.num_queue;
     if (units < grid) grid = int(std::max<int64_t>(units, 1));
     if (any_streamed) {
@@ -485,7 +485,7 @@ int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
     bool launched = false;
     if (jk) {
       cudaError_t e = jit_launch(jk, bd, *a, grid, smem, state_amps,
-                                 mode == kModeAdjoint ? 2 : 1, s);
+                                 mode == kModeAdjoint ? 2 : 1, s, jit_threads(mode));
       launched = e == cudaSuccess;
       if (!launched) {
         // a rejected launch (nothing ran): record why, stop specializing
@@ -819,7 +819,21 @@ int tfqg_internal_batch_jit(void* batch, int mode, int32_t* nsig, int32_t* activ
   return 0;
 }
 
-// Generates and compiles the batch's specialized module on the host only.
+// Generated specialized source of `mode` for a batch; returns its length
+// (the copy into buf is truncated to size - 1 bytes).
+int64_t tfqg_internal_jit_source(void* batch, int mode, char* buf, int64_t size) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  if (!b || mode < 0 || mode >= kJitModes) return -1;
+  const std::string src = jit_source(b, mode);
+  if (buf && size > 0) {
+    strncpy(buf, src.c_str(), size_t(size - 1));
+    buf[size - 1] = 0;
+  }
+  return int64_t(src.size());
+}
+
+// Generates and compiles the batch's specialized module on the host only;
+// `err` receives the compiler log (resource usage on success).
 int tfqg_internal_jit_compile_check(void* batch, int mode, char* err, int64_t err_size) {
   tfqg_batch* b = static_cast<tfqg_batch*>(batch);
   std::string log;

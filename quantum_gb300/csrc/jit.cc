@@ -156,38 +156,37 @@ void emit_forward(std::ostringstream& o, int id, const std::vector<uint32_t>& co
        "  constexpr int RB = kFwdRB, NA = 1 << RB;\n"
        "  float2* s = reinterpret_cast<float2*>(smem_raw + s_off);\n"
        "  const Stage* st = reinterpret_cast<const Stage*>(smem_raw + st_off);\n"
-       "  uint32_t soff[NA];\n"
-       "#pragma unroll\n"
-       "  for (int k = 0; k < NA; ++k) {\n"
-       "    uint32_t o = 0;\n"
-       "#pragma unroll\n"
-       "    for (int j = 0; j < RB; ++j) if (k >> j & 1) o |= 1u << ((rbits >> (8 * j)) & 0xFF);\n"
-       "    soff[k] = swz(o);\n"
-       "  }\n"
+       "  // swz is XOR-linear: the offset of amplitude k is the XOR of the\n"
+       "  // offsets of its register bits\n"
+       "  const uint32_t o0 = swz(1u << (rbits & 0xFF)), o1 = swz(1u << ((rbits >> 8) & 0xFF));\n"
+       "  const uint32_t o2 = swz(1u << ((rbits >> 16) & 0xFF)), o3 = swz(1u << (rbits >> 24));\n"
        "  const uint32_t ngroups = 1u << (T - RB);\n"
        "  for (uint32_t g = threadIdx.x; g < ngroups; g += blockDim.x) {\n"
        "    const uint32_t gb = group_base(g, rbits, RB);\n"
        "    const uint32_t sgb = swz(gb);\n"
        "    float2 A[NA], B[NA];\n"
        "#pragma unroll\n"
-       "    for (int k = 0; k < NA; ++k) A[k] = s[sgb ^ soff[k]];\n"
+       "    for (int k = 0; k < NA; ++k)\n"
+       "      A[k] = s[sgb ^ (k & 1 ? o0 : 0u) ^ (k & 2 ? o1 : 0u) ^ (k & 4 ? o2 : 0u) ^ (k & 8 ? o3 : 0u)];\n"
        "    (void)base;\n";
   for (size_t i = 0; i < codes.size(); ++i)
     emit_forward_op(o, int(i), codes[i], i % 2 ? "B" : "A", i % 2 ? "A" : "B");
   const char* fin = codes.size() % 2 ? "B" : "A";
   o << "#pragma unroll\n"
-       "    for (int k = 0; k < NA; ++k) s[sgb ^ soff[k]] = "
+       "    for (int k = 0; k < NA; ++k)\n"
+       "      s[sgb ^ (k & 1 ? o0 : 0u) ^ (k & 2 ? o1 : 0u) ^ (k & 4 ? o2 : 0u) ^ (k & 8 ? o3 : 0u)] = "
     << fin << "[k];\n  }\n}\n\n";
 }
 
 void emit_backward(std::ostringstream& o, int id, const std::vector<uint32_t>& codes) {
   o << "__device__ __noinline__ void jit_sub_" << id
     << "(uint32_t s_off, uint32_t l_off, int T, uint32_t base, uint32_t st_off,"
-       " uint32_t rbits, int rbuf) {\n"
+       " uint32_t rb_off, uint32_t rbits, int rbuf) {\n"
        "  constexpr int RB = kBwdRB, NA = 1 << RB;\n"
        "  float2* s = reinterpret_cast<float2*>(smem_raw + s_off);\n"
        "  float2* l = reinterpret_cast<float2*>(smem_raw + l_off);\n"
-       "  Stage* st = reinterpret_cast<Stage*>(smem_raw + st_off);\n"
+       "  const Stage* st = reinterpret_cast<const Stage*>(smem_raw + st_off);\n"
+       "  RedBuf* rb = reinterpret_cast<RedBuf*>(smem_raw + rb_off);\n"
        "  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n"
        "  uint32_t soff[NA];\n"
        "#pragma unroll\n"
@@ -247,8 +246,8 @@ void emit_backward(std::ostringstream& o, int id, const std::vector<uint32_t>& c
     o << "      if (" << cond << ") { " << call.str() << " } else { copy_regs(" << a << ", " << b
       << "); copy_regs(" << la << ", " << lb << "); }\n";
     for (int q = 0; q < ng; ++q)
-      o << "      { float v = warp_sum(part[" << q << "]); if (lane == 0) { if (it == 0) st->red[rbuf]["
-        << gi + q << "][warp] = v; else st->red[rbuf][" << gi + q << "][warp] += v; } }\n";
+      o << "      { float v = warp_sum(part[" << q << "]); if (lane == 0) { if (it == 0) rb->red[rbuf]["
+        << gi + q << "][warp] = v; else rb->red[rbuf][" << gi + q << "][warp] += v; } }\n";
     o << "    }\n";
     gi += ng;
   }
@@ -305,27 +304,30 @@ void write_file(const std::string& path, const std::vector<char>& data) {
   else remove(tmp.c_str());
 }
 
-// Compiles `src` for sm_103a; returns the CUBIN.
-std::vector<char> nvrtc_compile(const std::string& src) {
+// Compiles `src` for sm_103a; returns the CUBIN.  With `info`, ptxas also
+// reports resource usage (registers, spills, shared memory) into *info.
+std::vector<char> nvrtc_compile(const std::string& src, std::string* info = nullptr) {
   const Nvrtc& nv = nvrtc();
   if (!nv.ok) throw Error(kUnimplemented, "NVRTC is not available");
   nvrtcProgram prog;
   if (nv.create(&prog, src.c_str(), "tfqg_jit.cu", kJitHeaderCount,
                 kJitHeaderSources, kJitHeaderNames) != NVRTC_SUCCESS)
     throw Error(kInternal, "nvrtcCreateProgram failed");
-  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-DTFQG_JIT=1"};
-  nvrtcResult r = nv.compile(prog, 3, opts);
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-DTFQG_JIT=1",
+                        "--ptxas-options=-v"};
+  nvrtcResult r = nv.compile(prog, info ? 4 : 3, opts);
+  size_t n = 0;
+  nv.log_size(prog, &n);
+  std::string log(n, '\0');
+  if (n) nv.log(prog, &log[0]);
   if (r != NVRTC_SUCCESS) {
-    size_t n = 0;
-    nv.log_size(prog, &n);
-    std::string log(n, '\0');
-    nv.log(prog, &log[0]);
     nv.destroy(&prog);
     throw Error(kInternal, "NVRTC compile failed: " + log.substr(0, 2000));
   }
-  size_t n = 0;
-  nv.cubin_size(prog, &n);
-  std::vector<char> cubin(n);
+  if (info) *info = log;
+  size_t bytes = 0;
+  nv.cubin_size(prog, &bytes);
+  std::vector<char> cubin(bytes);
   nv.cubin(prog, cubin.data());
   nv.destroy(&prog);
   return cubin;
@@ -378,12 +380,13 @@ std::string jit_source(const tfqg_batch* b, int mode) {
       o << "      case " << id << ": jit_sub_" << id << "(so, T, base, sto, rbits); break;\n";
   o << "      default: break;\n    }\n    (void)nops;\n  }\n"
        "  static __device__ __forceinline__ void backward(uint32_t so, uint32_t lo, int T,"
-       " uint32_t base, uint32_t sto, int nops, uint32_t rbits, int rbuf, int sig) {\n"
+       " uint32_t base, uint32_t sto, uint32_t rbo, int nops, uint32_t rbits, int rbuf,"
+       " int sig) {\n"
        "    switch (sig) {\n";
   for (size_t id = 0; id < b->jit_signatures.size(); ++id)
     if (adj && b->jit_signatures[id][0] == 3)
       o << "      case " << id << ": jit_sub_" << id
-        << "(so, lo, T, base, sto, rbits, rbuf); break;\n";
+        << "(so, lo, T, base, sto, rbo, rbits, rbuf); break;\n";
   o << "      default: break;\n    }\n    (void)nops;\n  }\n};\n\n}  // namespace\n\n";
   if (mode == kJitWide)
     o << "extern \"C\" __global__ void __launch_bounds__(kWideThreads, 2) " << kModeNames[mode]
@@ -391,7 +394,8 @@ std::string jit_source(const tfqg_batch* b, int mode) {
          " int state_amps) {\n"
          "  wide_pass_body<JitExec>(b, a, row, pass, init, psi, state_amps);\n}\n";
   else
-    o << "extern \"C\" __global__ void __launch_bounds__(kSimThreads, 1) " << kModeNames[mode]
+    o << "extern \"C\" __global__ void __launch_bounds__(" << jit_threads(mode) << ", 1) "
+      << kModeNames[mode]
       << "(BatchDevice b, RunArgs a, int state_amps, int nstates) {\n"
          "  simulate_body<"
       << kModeEnums[mode] << ", JitExec>(b, a, state_amps, nstates);\n}\n";
@@ -482,7 +486,7 @@ cudaKernel_t jit_kernel(tfqg_batch* b, int mode, int dev) {
 int jit_compile_check(tfqg_batch* b, int mode, std::string* log) {
   if (mode < 0 || mode >= kJitModes) return kInvalidArgument;
   try {
-    std::vector<char> cubin = nvrtc_compile(jit_source(b, mode));
+    std::vector<char> cubin = nvrtc_compile(jit_source(b, mode), log);
     return cubin.empty() ? kInternal : 0;
   } catch (const Error& e) {
     *log = e.what();
@@ -504,14 +508,22 @@ int jit_grid(cudaKernel_t k, size_t smem, int dev, int threads) {
   return sms * per_sm;
 }
 
+// Threads per CTA of the specialized persistent kernel of `mode`.  (1024
+// threads for the adjoint, whose backward sub-passes fit the 64 registers a
+// thread then has, measured no faster than 512.)
+int jit_threads(int mode) {
+  (void)mode;
+  return kSimThreads;
+}
+
 cudaError_t jit_launch(cudaKernel_t k, const BatchDevice& bd, const RunArgs& a,
                        int grid, size_t smem, int state_amps, int nstates,
-                       cudaStream_t s) {
+                       cudaStream_t s, int threads) {
   BatchDevice b = bd;
   RunArgs ra = a;
   void* args[] = {&b, &ra, &state_amps, &nstates};
   return cudaLaunchKernel(reinterpret_cast<const void*>(k), dim3(grid),
-                          dim3(kSimThreads), args, smem, s);
+                          dim3(threads), args, smem, s);
 }
 
 cudaError_t jit_launch_wide(cudaKernel_t k, const BatchDevice& bd, const RunArgs& a,

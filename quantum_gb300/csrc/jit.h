@@ -23,9 +23,10 @@ bool jit_enabled_for(const tfqg_batch* b);
 cudaKernel_t jit_kernel(tfqg_batch* b, int mode, int dev);
 int jit_compile_check(tfqg_batch* b, int mode, std::string* log);
 int jit_grid(cudaKernel_t k, size_t smem, int dev, int threads);
+int jit_threads(int mode);
 cudaError_t jit_launch(cudaKernel_t k, const BatchDevice& bd, const RunArgs& a,
                        int grid, size_t smem, int state_amps, int nstates,
-                       cudaStream_t s);
+                       cudaStream_t s, int threads);
 cudaError_t jit_launch_wide(cudaKernel_t k, const BatchDevice& bd, const RunArgs& a,
                             int row, int pass, int init, float2* psi, int grid,
                             size_t smem, int state_amps, cudaStream_t s);

@@ -270,7 +270,7 @@ size_t sim_smem_bytes(int mode, int max_resident_n, bool any_streamed,
   size_t amps = size_t(sim_state_amps(max_resident_n, any_streamed));
   int nstates = mode == kModeAdjoint ? 2 : 1;
   size_t bytes = amps * nstates * sizeof(float2);
-  bytes += sizeof(Stage);
+  bytes += 2 * sizeof(Stage) + sizeof(RedBuf);
   bytes += (1u << kHiBits) * sizeof(uint32_t);
   bytes += 2 * 4 * kWarps * sizeof(double);
   if (mode == kModeSample) bytes += kMaxChunks * sizeof(double);

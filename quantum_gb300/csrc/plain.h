@@ -33,6 +33,7 @@ cudaError_t plain_expect_adjoint(const PlainJob& j, cudaStream_t s,
 extern "C" {
 int64_t tfqg_internal_batch_table_bytes(void* batch);
 int tfqg_internal_jit_compile_check(void* batch, int mode, char* err, int64_t err_size);
+int64_t tfqg_internal_jit_source(void* batch, int mode, char* buf, int64_t size);
 int tfqg_internal_batch_jit(void* batch, int mode, int32_t* nsig, int32_t* active,
                             char* err, int64_t err_size);
 int tfqg_internal_batch_subpasses(void* batch, int32_t* fwd_subs,

@@ -90,17 +90,30 @@ constexpr int kRB = 4;            // register bits of forward sub-passes
 constexpr int kRA = 1 << kRB;     // amplitudes per forward thread group
 constexpr int kMaxOps = 32;       // ops per sub-pass (host kMaxSubOps)
 
-// One sub-pass staged in shared memory: descriptors, matrices, derivative
-// matrices, and the per-warp gradient partials of its adjoint ops.
+// One sub-pass staged in shared memory: descriptors, matrices and
+// derivative matrices.  Two of these alternate, so that sub-pass k + 1 is
+// staged while sub-pass k runs and one barrier separates them.
 struct Stage {
   uint32_t code[kMaxOps];
   uint32_t lcmask[kMaxOps], lcval[kMaxOps], gcmask[kMaxOps], gcval[kMaxOps];
   float2 mat[kMaxOps][16];
   float2 dmat[kMaxOps][2][16];
-  float red[2][2 * kMaxOps][kWarps];  // [buffer][grad slot in sub-pass][warp]
-  int32_t red_slot[2][2 * kMaxOps];   // derivative slot of each entry
-  int32_t nred[2];
 };
+
+// Gradient partials of the adjoint's sub-passes.  Sub-pass k writes its
+// per-warp partials to red[k & 1]; after the barrier that ends it, the
+// partials are summed into the accumulators while sub-pass k + 1 runs and
+// sub-pass k + 2 is staged, so the slot lists rotate through three buffers.
+struct RedBuf {
+  float red[2][2 * kMaxOps][kWarps];  // [k & 1][grad entry of the sub-pass][warp]
+  int32_t red_slot[3][2 * kMaxOps];   // [k % 3]: derivative slot of each entry
+  int32_t nred[3];
+  int32_t pad;
+};
+// carve_smem places sections back to back: every section size must keep the
+// 16-byte alignment of the next (float4 staging, double scratch)
+static_assert(sizeof(Stage) % 16 == 0, "Stage size must be a multiple of 16");
+static_assert(sizeof(RedBuf) % 16 == 0, "RedBuf size must be a multiple of 16");
 
 struct Smem {
   float2* psi;        // resident state / tile
@@ -109,7 +122,8 @@ struct Smem {
   double* red;        // [2][4][kWarps] reduction scratch (terms, channels)
   double* csum;       // sampler chunk prefix sums
   double* grad;       // adjoint accumulators
-  Stage* st;
+  Stage* st;          // [2] staged sub-passes
+  RedBuf* rb;
   double* macc;       // [2 * kMaxMeasTerms] term sums (re, im)
   struct MTerm { float w; uint32_t lflip, zy; uint16_t op; uint8_t ny, identity; }* mterm;
   double* oacc;       // [kMaxOpsSmem] per-op sums (expectation mode)
@@ -602,8 +616,8 @@ __device__ __noinline__ void exec_forward(uint32_t s_off, int T, uint32_t base,
 #endif  // TFQG_JIT
 
 // One adjoint op of the sub-pass: (a, l) -> (ao, lo) plus warp-reduced
-// gradient partials into st->red.
-__device__ __forceinline__ void backward_op(Stage* st, int i, uint32_t gb,
+// gradient partials into rb->red.
+__device__ __forceinline__ void backward_op(const Stage* st, RedBuf* rb, int i, uint32_t gb,
                                             uint32_t base, bool active, int it,
                                             int rbuf, int& gi,
                                             const float2 (&a)[1 << kBwdRB],
@@ -626,8 +640,8 @@ __device__ __forceinline__ void backward_op(Stage* st, int i, uint32_t gb,
     if (q < ng) {
       float v = warp_sum(part[q]);
       if (lane == 0) {
-        if (it == 0) st->red[rbuf][gi + q][warp] = v;
-        else st->red[rbuf][gi + q][warp] += v;
+        if (it == 0) rb->red[rbuf][gi + q][warp] = v;
+        else rb->red[rbuf][gi + q][warp] += v;
       }
     }
   }
@@ -638,11 +652,13 @@ __device__ __forceinline__ void backward_op(Stage* st, int i, uint32_t gb,
 // Adjoint sub-pass on psi (s) and lambda (l) with 3 register bits.
 __device__ __noinline__ void exec_backward(uint32_t s_off, uint32_t l_off, int T,
                                            uint32_t base, uint32_t st_off,
-                                           int nops, uint32_t rbits, int rbuf) {
+                                           uint32_t rb_off, int nops, uint32_t rbits,
+                                           int rbuf) {
   constexpr int RB = kBwdRB, NA = 1 << RB;
   float2* s = reinterpret_cast<float2*>(smem_raw + s_off);
   float2* l = reinterpret_cast<float2*>(smem_raw + l_off);
-  Stage* st = reinterpret_cast<Stage*>(smem_raw + st_off);
+  const Stage* st = reinterpret_cast<const Stage*>(smem_raw + st_off);
+  RedBuf* rb = reinterpret_cast<RedBuf*>(smem_raw + rb_off);
   uint32_t soff[NA];
 #pragma unroll
   for (int k = 0; k < NA; ++k) {
@@ -676,7 +692,7 @@ __device__ __noinline__ void exec_backward(uint32_t s_off, uint32_t l_off, int T
         }
         break;
       }
-      backward_op(st, i, gb, base, active, int(it), rbuf, gi, A, LA, B, LB);
+      backward_op(st, rb, i, gb, base, active, int(it), rbuf, gi, A, LA, B, LB);
       if (++i >= nops) {
         if (active) {
 #pragma unroll
@@ -684,7 +700,7 @@ __device__ __noinline__ void exec_backward(uint32_t s_off, uint32_t l_off, int T
         }
         break;
       }
-      backward_op(st, i, gb, base, active, int(it), rbuf, gi, B, LB, A, LA);
+      backward_op(st, rb, i, gb, base, active, int(it), rbuf, gi, B, LB, A, LA);
       ++i;
     }
   }
@@ -752,11 +768,12 @@ struct RowCtx {
   DevProgram p;
 };
 
-// Copies the sub-pass's descriptors and matrices into shared memory.
+// Copies the sub-pass's descriptors and matrices into shared memory (st),
+// and for the adjoint its list of derivative slots (rb slot list `slots`).
 template <int MODE>
 __device__ void stage_subpass(const BatchDevice& b, const RunArgs& a,
-                              const RowCtx& rc, Stage* st, uint32_t first,
-                              int nops, int buf) {
+                              const RowCtx& rc, Stage* st, RedBuf* rb,
+                              uint32_t first, int nops, int slots) {
   const float2* mats = a.mats + int64_t(rc.r.mat_offset) * 16;
   const float2* dmats = a.dmats + int64_t(rc.r.dmat_offset) * 16;
   const int per_op = MODE == kModeAdjoint ? 24 : 8;  // 16-byte chunks
@@ -802,20 +819,26 @@ __device__ void stage_subpass(const BatchDevice& b, const RunArgs& a,
     for (int i = 0; i < nops; ++i) {
       const DevOp op = b.ops[first + i];
       if ((op.type == OP_B1 || op.type == OP_B2) && op.ngrad)
-        for (int g = 0; g < op.ngrad; ++g) st->red_slot[buf][nr++] = op.grad_slot + g;
+        for (int g = 0; g < op.ngrad; ++g) rb->red_slot[slots][nr++] = op.grad_slot + g;
     }
-    st->nred[buf] = nr;
+    rb->nred[slots] = nr;
   }
 }
 
 // Executes the instruction stream [ob, oe) on a tile: s (psi) and l
 // (lambda) hold 2^T amplitudes; `base` are the tile's fixed global bits.
+// `kc` counts the CTA's sub-passes across calls: sub-pass k uses staging
+// buffer k & 1, partial buffer k & 1 and slot list k % 3.  While sub-pass
+// k runs, sub-pass k + 1 of the same stream is staged into the other
+// buffer, so one barrier separates consecutive sub-passes.
 template <int MODE, class Exec>
 __device__ void run_ops(const BatchDevice& b, const RunArgs& a, const Smem& sm,
                         const RowCtx& rc, uint32_t ob, uint32_t oe, float2* s,
-                        float2* l, int T, uint32_t base, int& rbuf) {
-  Stage* st = sm.st;
+                        float2* l, int T, uint32_t base, int& kc) {
   uint32_t o = ob;
+  bool staged = false;  // ops[o] (a sub-pass) already staged in buffer kc & 1
+  const uint32_t so = uint32_t(reinterpret_cast<unsigned char*>(s) - smem_raw);
+  const uint32_t rbo = uint32_t(reinterpret_cast<unsigned char*>(sm.rb) - smem_raw);
   while (o < oe) {
     const DevOp h = b.ops[o];
     if (h.type == OP_CHAN) {
@@ -826,28 +849,42 @@ __device__ void run_ops(const BatchDevice& b, const RunArgs& a, const Smem& sm,
       }
       __syncthreads();
       ++o;
+      staged = false;
       continue;
     }
     // sub-pass
     const int nops = int(h.gate);
-    stage_subpass<MODE>(b, a, rc, st, o + 1, nops, rbuf);
-    __syncthreads();
-    const uint32_t so = uint32_t(reinterpret_cast<unsigned char*>(s) - smem_raw);
+    Stage* st = sm.st + (kc & 1);
+    if (!staged) {
+      stage_subpass<MODE>(b, a, rc, st, sm.rb, o + 1, nops, kc % 3);
+      __syncthreads();
+    }
+    const uint32_t next = o + 1 + uint32_t(nops);
+    staged = false;
+    if (next < oe) {
+      const DevOp hn = b.ops[next];
+      if (hn.type != OP_CHAN) {
+        stage_subpass<MODE>(b, a, rc, sm.st + ((kc + 1) & 1), sm.rb, next + 1,
+                            int(hn.gate), (kc + 1) % 3);
+        staged = true;
+      }
+    }
     const uint32_t sto = uint32_t(reinterpret_cast<unsigned char*>(st) - smem_raw);
     if (MODE == kModeAdjoint && h.t0 == kBwdRB) {
       const uint32_t lo = uint32_t(reinterpret_cast<unsigned char*>(l) - smem_raw);
-      Exec::backward(so, lo, T, base, sto, nops, h.lcmask, rbuf, h.grad_slot);
+      Exec::backward(so, lo, T, base, sto, rbo, nops, h.lcmask, kc & 1, h.grad_slot);
     } else {
       Exec::forward(so, T, base, sto, nops, h.lcmask, h.grad_slot);
     }
     __syncthreads();
-    if (MODE == kModeAdjoint && int(threadIdx.x) < st->nred[rbuf]) {
+    if (MODE == kModeAdjoint && int(threadIdx.x) < sm.rb->nred[kc % 3]) {
       double acc = 0.0;
-      for (int w = 0; w < int(blockDim.x >> 5); ++w) acc += st->red[rbuf][threadIdx.x][w];
-      sm.grad[st->red_slot[rbuf][threadIdx.x]] += acc;
+      for (int w = 0; w < int(blockDim.x >> 5); ++w)
+        acc += sm.rb->red[kc & 1][threadIdx.x][w];
+      sm.grad[sm.rb->red_slot[kc % 3][threadIdx.x]] += acc;
     }
-    if (MODE == kModeAdjoint) rbuf ^= 1;
-    o += 1 + nops;
+    ++kc;
+    o = next;
   }
 }
 
@@ -916,7 +953,7 @@ template <int MODE, class Exec>
 __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
                            const Smem& sm, const RowCtx& rc, uint32_t pb,
                            uint32_t pe, float2* g_psi, float2* g_lam,
-                           bool init, int& rbuf, uint32_t t0 = 0,
+                           bool init, int& kc, uint32_t t0 = 0,
                            uint32_t tstride = 1) {
   const int n = rc.p.n;
   if (rc.p.resident) {
@@ -924,7 +961,7 @@ __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
     for (uint32_t p = pb; p < pe; ++p) {
       const DevPass ps = b.passes[p];
       run_ops<MODE, Exec>(b, a, sm, rc, ps.op_begin, ps.op_end, sm.psi, sm.lam, T, 0u,
-                    rbuf);
+                    kc);
     }
     return;
   }
@@ -942,7 +979,7 @@ __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
       if (MODE == kModeAdjoint && g_lam) tile_load(sm.lam, g_lam, sm.hi, base);
       __syncthreads();
       run_ops<MODE, Exec>(b, a, sm, rc, ps.op_begin, ps.op_end, sm.psi, sm.lam, kTile,
-                    base, rbuf);
+                    base, kc);
       tile_store(g_psi, sm.psi, sm.hi, base);
       if (MODE == kModeAdjoint && g_lam) tile_store(g_lam, sm.lam, sm.hi, base);
       __syncthreads();
@@ -1212,7 +1249,7 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
   rc.p = b.programs[rc.r.program];
   const int n = rc.p.n;
   const bool empty = n == 0 || rc.p.fwd_pass_begin == rc.p.fwd_pass_end;
-  int rbuf = 0;
+  int kc = 0;  // sub-pass counter
 
   if (MODE == kModeExpect || MODE == kModeNoisy) {
     if (empty) {
@@ -1247,10 +1284,10 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     init_resident(sm.psi, n);
     __syncthreads();
     run_passes<MODE, Exec>(b, a, sm, rc, rc.p.fwd_pass_begin, rc.p.fwd_pass_end,
-                     nullptr, nullptr, true, rbuf);
+                     nullptr, nullptr, true, kc);
   } else {
     run_passes<MODE, Exec>(b, a, sm, rc, rc.p.fwd_pass_begin, rc.p.fwd_pass_end,
-                     g_psi, nullptr, true, rbuf);
+                     g_psi, nullptr, true, kc);
   }
   __syncthreads();
   const float2* psi = rc.p.resident ? sm.psi : g_psi;
@@ -1290,7 +1327,7 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     __syncthreads();
     run_passes<MODE, Exec>(b, a, sm, rc, rc.p.bwd_pass_begin, rc.p.bwd_pass_end,
                      rc.p.resident ? nullptr : g_psi,
-                     rc.p.resident ? nullptr : g_lam, false, rbuf);
+                     rc.p.resident ? nullptr : g_lam, false, kc);
     __syncthreads();
     if (threadIdx.x == 0) {
       float* out = a.out_f + int64_t(row) * b.num_symbols;
@@ -1303,7 +1340,14 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
   __syncthreads();
 }
 
-// Dynamic shared memory layout of a simulation CTA.
+// Dynamic shared memory layout of a simulation CTA.  The state section holds
+// at least kRA amplitudes (128 bytes), and every other section size is a
+// multiple of 16 bytes, so each section starts 16-byte aligned.
+static_assert(((1u << kHiBits) * sizeof(uint32_t)) % 16 == 0, "hi table");
+static_assert((2 * 4 * kWarps * sizeof(double)) % 16 == 0, "reduction scratch");
+static_assert((kMaxChunks * sizeof(double)) % 16 == 0, "sampler chunks");
+static_assert((2 * kMaxMeasTermsDev * sizeof(double)) % 16 == 0, "term sums");
+static_assert((kMaxOpsSmem * sizeof(double)) % 16 == 0, "per-op sums");
 template <int MODE>
 __device__ __forceinline__ Smem carve_smem(int state_amps, int nstates) {
   Smem sm;
@@ -1311,7 +1355,9 @@ __device__ __forceinline__ Smem carve_smem(int state_amps, int nstates) {
   sm.lam = sm.psi + state_amps;
   unsigned char* p = smem_raw + size_t(state_amps) * nstates * sizeof(float2);
   sm.st = reinterpret_cast<Stage*>(p);
-  p += sizeof(Stage);
+  p += 2 * sizeof(Stage);
+  sm.rb = reinterpret_cast<RedBuf*>(p);
+  p += sizeof(RedBuf);
   sm.hi = reinterpret_cast<uint32_t*>(p);
   p += (1u << kHiBits) * sizeof(uint32_t);
   sm.red = reinterpret_cast<double*>(p);
@@ -1376,9 +1422,9 @@ __device__ __forceinline__ void wide_pass_body(const BatchDevice& b, const RunAr
   rc.traj = 0;
   rc.r = b.rows[row];
   rc.p = b.programs[rc.r.program];
-  int rbuf = 0;
+  int kc = 0;  // sub-pass counter
   run_passes<kModeState, Exec>(b, a, sm, rc, uint32_t(pass), uint32_t(pass) + 1, psi,
-                               nullptr, init != 0, rbuf, blockIdx.x, gridDim.x);
+                               nullptr, init != 0, kc, blockIdx.x, gridDim.x);
 }
 
 // Measurement pass `mp` of wide row `row`: this CTA's tiles add their term
@@ -1424,9 +1470,9 @@ struct InterpExec {
   }
   static __device__ __forceinline__ void backward(uint32_t so, uint32_t lo, int T,
                                                   uint32_t base, uint32_t sto,
-                                                  int nops, uint32_t rbits,
-                                                  int rbuf, int sig) {
-    exec_backward(so, lo, T, base, sto, nops, rbits, rbuf);
+                                                  uint32_t rbo, int nops,
+                                                  uint32_t rbits, int rbuf, int sig) {
+    exec_backward(so, lo, T, base, sto, rbo, nops, rbits, rbuf);
   }
 };
 #endif  // TFQG_JIT
