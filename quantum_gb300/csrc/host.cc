@@ -800,8 +800,15 @@ void plan_subpasses(const std::vector<DevOp>& in, int T, int regbits,
     h.lcmask = uint32_t(rb[0]) | uint32_t(rb[1]) << 8 | uint32_t(rb[2]) << 16 |
                uint32_t(rb[3]) << 24;
     h.grad_slot = -1;
+    int entries = 0;
+    for (const DevOp& op : taken)
+      if (op.type == OP_B1 || op.type == OP_B2) entries += op.ngrad;
+    h.t1 = uint8_t(entries);  // <= 2 * kMaxSubOps
     out->push_back(h);
+    int gi = 0;
     for (DevOp op : taken) {
+      op.gi = uint8_t(gi);
+      if (op.type == OP_B1 || op.type == OP_B2) gi += op.ngrad;
       uint32_t lm = op.lcmask, lv = op.lcval;
       op.lcmask = 0;
       op.lcval = 0;

@@ -65,6 +65,7 @@ struct Nvrtc {
   decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
   decltype(&nvrtcGetCUBIN) cubin = nullptr;
   decltype(&nvrtcDestroyProgram) destroy = nullptr;
+  decltype(&nvrtcVersion) version = nullptr;
   bool ok = false;
 };
 
@@ -85,6 +86,7 @@ const Nvrtc& nvrtc() {
     n.cubin_size = reinterpret_cast<decltype(n.cubin_size)>(dlsym(h, "nvrtcGetCUBINSize"));
     n.cubin = reinterpret_cast<decltype(n.cubin)>(dlsym(h, "nvrtcGetCUBIN"));
     n.destroy = reinterpret_cast<decltype(n.destroy)>(dlsym(h, "nvrtcDestroyProgram"));
+    n.version = reinterpret_cast<decltype(n.version)>(dlsym(h, "nvrtcVersion"));
     n.ok = n.create && n.compile && n.log_size && n.log && n.cubin_size && n.cubin && n.destroy;
   });
   return n;
@@ -93,12 +95,37 @@ const Nvrtc& nvrtc() {
 std::mutex g_mu;
 std::map<std::string, std::shared_ptr<Loaded>> g_cache;  // source -> module
 
+// Compile options of every specialized module (sm_103a only).
+const char* const kNvrtcOptions[] = {"--gpu-architecture=sm_103a", "-std=c++17",
+                                     "-DTFQG_JIT=1", "--ptxas-options=-v"};
+
 uint64_t fnv1a(const std::string& s) {
   uint64_t h = 1469598103934665603ull;
   for (unsigned char c : s) {
     h ^= c;
     h *= 1099511628211ull;
   }
+  return h;
+}
+
+// Hash of everything besides the generated source that determines a
+// module: the embedded device headers, the compile options and the NVRTC
+// version.  It keys the disk cache together with the source, so a library
+// built from changed headers never loads a module compiled from old ones.
+uint64_t toolchain_hash() {
+  static uint64_t h = [] {
+    std::string all;
+    for (int i = 0; i < kJitHeaderCount; ++i) {
+      all += kJitHeaderNames[i];
+      all += kJitHeaderSources[i];
+    }
+    for (const char* o : kNvrtcOptions) all += o;
+    int major = 0, minor = 0;
+    const Nvrtc& nv = nvrtc();
+    if (nv.version) nv.version(&major, &minor);
+    all += std::to_string(major) + "." + std::to_string(minor);
+    return fnv1a(all);
+  }();
   return h;
 }
 
@@ -313,9 +340,7 @@ std::vector<char> nvrtc_compile(const std::string& src, std::string* info = null
   if (nv.create(&prog, src.c_str(), "tfqg_jit.cu", kJitHeaderCount,
                 kJitHeaderSources, kJitHeaderNames) != NVRTC_SUCCESS)
     throw Error(kInternal, "nvrtcCreateProgram failed");
-  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-DTFQG_JIT=1",
-                        "--ptxas-options=-v"};
-  nvrtcResult r = nv.compile(prog, info ? 4 : 3, opts);
+  nvrtcResult r = nv.compile(prog, info ? 4 : 3, kNvrtcOptions);
   size_t n = 0;
   nv.log_size(prog, &n);
   std::string log(n, '\0');
@@ -437,8 +462,9 @@ cudaKernel_t jit_kernel(tfqg_batch* b, int mode, int dev) {
         mod->mode = mode;
         std::string dir = cache_dir();
         char name[64];
-        snprintf(name, sizeof(name), "/jit_%016llx_%zu.cubin",
-                 (unsigned long long)fnv1a(src), src.size());
+        snprintf(name, sizeof(name), "/jit_%016llx_%016llx_%zu.cubin",
+                 (unsigned long long)toolchain_hash(), (unsigned long long)fnv1a(src),
+                 src.size());
         std::string path = dir.empty() ? "" : dir + name;
         if (path.empty() || !read_file(path, &mod->cubin)) {
           mod->cubin = nvrtc_compile(src);

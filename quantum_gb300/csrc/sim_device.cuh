@@ -803,6 +803,8 @@ __device__ void stage_subpass(const BatchDevice& b, const RunArgs& a,
       st->code[i] = op_code(op);
       st->lcmask[i] = op.lcmask; st->lcval[i] = op.lcval;
       st->gcmask[i] = op.gcmask; st->gcval[i] = op.gcval;
+      if (MODE == kModeAdjoint && (op.type == OP_B1 || op.type == OP_B2))
+        for (int g = 0; g < op.ngrad; ++g) rb->red_slot[slots][op.gi + g] = op.grad_slot + g;
     }
     if (c < 8) {
       reinterpret_cast<float4*>(st->mat[i])[c] =
@@ -814,15 +816,8 @@ __device__ void stage_subpass(const BatchDevice& b, const RunArgs& a,
             reinterpret_cast<const float4*>(dmats + int64_t(op.grad_slot + g) * 16) + cc);
     }
   }
-  if (MODE == kModeAdjoint && threadIdx.x == 0) {
-    int nr = 0;
-    for (int i = 0; i < nops; ++i) {
-      const DevOp op = b.ops[first + i];
-      if ((op.type == OP_B1 || op.type == OP_B2) && op.ngrad)
-        for (int g = 0; g < op.ngrad; ++g) rb->red_slot[slots][nr++] = op.grad_slot + g;
-    }
-    rb->nred[slots] = nr;
-  }
+  // entries of the sub-pass: counted by the planner into the header
+  if (MODE == kModeAdjoint && threadIdx.x == 0) rb->nred[slots] = b.ops[first - 1].t1;
 }
 
 // Executes the instruction stream [ob, oe) on a tile: s (psi) and l

@@ -79,7 +79,8 @@ struct DevOp {
   int32_t grad_slot;       // first derivative slot (OP_B*)
   uint8_t cls;             // GateClass
   uint8_t kmask, kval;     // controls on register bits
-  uint8_t pad;
+  uint8_t gi;              // first gradient entry of the op in its sub-pass
+                           // (sub-pass header: t1 = entries of the sub-pass)
 };
 static_assert(sizeof(DevOp) == 32, "DevOp layout");
 
