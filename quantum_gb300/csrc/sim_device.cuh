@@ -125,6 +125,7 @@ struct Smem {
   Stage* st;          // [2] staged sub-passes
   RedBuf* rb;
   double* macc;       // [2 * kMaxMeasTerms] term sums (re, im)
+  // ny: bits 0-1 the Y count mod 4, bit 2 parity(flip & zy) (global bits)
   struct MTerm { float w; uint32_t lflip, zy; uint16_t op; uint8_t ny, identity; }* mterm;
   double* oacc;       // [kMaxOpsSmem] per-op sums (expectation mode)
 };
@@ -1000,33 +1001,63 @@ __device__ void stage_terms(const BatchDevice& b, const RunArgs& a, const Smem& 
     sm.mterm[i].lflip = mt.lflip;
     sm.mterm[i].zy = t.zy;
     sm.mterm[i].op = t.op;
-    sm.mterm[i].ny = t.ny;
+    sm.mterm[i].ny = uint8_t((t.ny & 3) | ((__popc(t.flip & t.zy) & 1) << 2));
     sm.mterm[i].identity = t.identity;
   }
 }
 
 // Adds <psi| P_t |psi> over one tile in shared memory (N amplitudes, fixed
 // global bits `base`) to the term sums sm.macc, for the nt staged terms.
+// Each thread takes amplitudes x = x0 + threadIdx.x + k * blockDim.x in
+// blocks of kMeasAmps and keeps them, their swizzled positions and global
+// indices in registers across the terms.  For P = i^ny X^flip Z^zy:
+// <psi|P|psi> = i^ny sum_x conj(psi_x) (-1)^popc((x ^ flip) & zy) psi_{x^flip},
+// and (-1)^popc((x ^ flip) & zy) = (-1)^(popc(x & zy) + popc(flip & zy)).
+// Only the component that Re(i^ny * sum) needs is accumulated: the real
+// part for even ny (into macc[2i]), the imaginary part for odd ny (into
+// macc[2i + 1]).
+constexpr int kMeasAmps = 16;
 __device__ void measure_tile(const Smem& sm, int nt, uint32_t N, uint32_t base,
                              bool resident) {
-  const int lane = threadIdx.x & 31;
-  for (int i = 0; i < nt; ++i) {
-    if (sm.mterm[i].identity) continue;
-    const uint32_t lf = sm.mterm[i].lflip, zy = sm.mterm[i].zy;
-    float re = 0.f, im = 0.f;
-    for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
-      const uint32_t y = x ^ lf;
-      const float2 av = sm.psi[swz(x)], bv = sm.psi[swz(y)];
-      const uint32_t yg = resident ? y : ((y & 31u) | sm.hi[y >> 5] | base);
-      const float sg = (__popc(yg & zy) & 1) ? -1.f : 1.f;
-      re = fmaf(sg, fmaf(av.x, bv.x, av.y * bv.y), re);
-      im = fmaf(sg, fmaf(av.x, bv.y, -av.y * bv.x), im);
+  const uint32_t stride = blockDim.x;
+  for (uint32_t x0 = 0; x0 < N; x0 += kMeasAmps * stride) {
+    float2 av[kMeasAmps];
+    uint32_t sx[kMeasAmps], gx[kMeasAmps];
+#pragma unroll
+    for (int k = 0; k < kMeasAmps; ++k) {
+      const uint32_t x = x0 + threadIdx.x + k * stride;
+      const bool ok = x < N;
+      sx[k] = swz(ok ? x : 0u);
+      gx[k] = resident ? x : ((x & 31u) | sm.hi[(ok ? x : 0u) >> 5] | base);
+      av[k] = ok ? sm.psi[sx[k]] : make_float2(0.f, 0.f);
     }
-    re = warp_sum(re);
-    im = warp_sum(im);
-    if (lane == 0) {
-      atomicAdd(&sm.macc[2 * i], double(re));
-      atomicAdd(&sm.macc[2 * i + 1], double(im));
+    for (int i = 0; i < nt; ++i) {
+      const auto t = sm.mterm[i];
+      if (t.identity) continue;
+      const uint32_t zy = t.zy, c0 = (t.ny >> 2) & 1;
+      float acc = 0.f;
+      if (t.lflip == 0) {
+        if (!(t.ny & 1)) {  // diagonal term: sum |psi_x|^2 (-1)^popc(x & zy)
+#pragma unroll
+          for (int k = 0; k < kMeasAmps; ++k) {
+            const float p = fmaf(av[k].x, av[k].x, av[k].y * av[k].y);
+            acc += ((__popc(gx[k] & zy) ^ c0) & 1) ? -p : p;
+          }
+        }
+      } else {
+        const uint32_t sl = swz(t.lflip);
+        const bool odd = t.ny & 1;
+#pragma unroll
+        for (int k = 0; k < kMeasAmps; ++k) {
+          const float2 bv = sm.psi[sx[k] ^ sl];
+          const float v = odd ? fmaf(av[k].x, bv.y, -av[k].y * bv.x)
+                              : fmaf(av[k].x, bv.x, av[k].y * bv.y);
+          acc += ((__popc(gx[k] & zy) ^ c0) & 1) ? -v : v;
+        }
+      }
+      acc = warp_sum(acc);
+      if ((threadIdx.x & 31) == 0 && acc != 0.f)
+        atomicAdd(&sm.macc[2 * i + (t.ny & 1)], double(acc));
     }
   }
 }
@@ -1089,6 +1120,60 @@ __device__ void measure_passes(const BatchDevice& b, const RunArgs& a,
   }
 }
 
+// lambda[x] += sum_t w_t i^ny_t (-1)^popc((x ^ flip_t) & zy_t) psi[x ^ flip_t]
+// over one tile for the nt staged terms (weights w = g_j c_t, zero for
+// skipped terms).  Each thread keeps a block of kMeasAmps lambda entries,
+// their swizzled positions and global indices in registers across the
+// terms; `fresh` starts lambda at zero instead of loading it.
+template <int NY>
+__device__ __forceinline__ void lambda_term(float2 (&v)[kMeasAmps], const uint32_t (&sx)[kMeasAmps],
+                                            const uint32_t (&gx)[kMeasAmps], const float2* psi,
+                                            uint32_t sl, uint32_t zy, uint32_t c0, float w) {
+#pragma unroll
+  for (int k = 0; k < kMeasAmps; ++k) {
+    float2 p = psi[sx[k] ^ sl];
+    if (NY == 1) p = make_float2(-p.y, p.x);       // multiply by i^ny
+    if (NY == 2) p = make_float2(-p.x, -p.y);
+    if (NY == 3) p = make_float2(p.y, -p.x);
+    const float ws = ((__popc(gx[k] & zy) ^ c0) & 1) ? -w : w;
+    v[k].x = fmaf(ws, p.x, v[k].x);
+    v[k].y = fmaf(ws, p.y, v[k].y);
+  }
+}
+
+__device__ void lambda_tile(const Smem& sm, int nt, uint32_t N, uint32_t base,
+                            bool resident, bool fresh) {
+  const uint32_t stride = blockDim.x;
+  for (uint32_t x0 = 0; x0 < N; x0 += kMeasAmps * stride) {
+    float2 v[kMeasAmps];
+    uint32_t sx[kMeasAmps], gx[kMeasAmps];
+#pragma unroll
+    for (int k = 0; k < kMeasAmps; ++k) {
+      const uint32_t x = x0 + threadIdx.x + k * stride;
+      const bool ok = x < N;
+      sx[k] = swz(ok ? x : 0u);
+      gx[k] = resident ? x : ((x & 31u) | sm.hi[(ok ? x : 0u) >> 5] | base);
+      v[k] = (ok && !fresh) ? sm.lam[sx[k]] : make_float2(0.f, 0.f);
+    }
+    for (int i = 0; i < nt; ++i) {
+      const auto t = sm.mterm[i];
+      const float w = t.w;
+      if (w == 0.f) continue;
+      const uint32_t sl = t.identity ? 0u : swz(t.lflip);
+      const uint32_t zy = t.identity ? 0u : t.zy, c0 = t.identity ? 0u : (t.ny >> 2) & 1;
+      switch (t.identity ? 0 : (t.ny & 3)) {
+        case 1: lambda_term<1>(v, sx, gx, sm.psi, sl, zy, c0, w); break;
+        case 2: lambda_term<2>(v, sx, gx, sm.psi, sl, zy, c0, w); break;
+        case 3: lambda_term<3>(v, sx, gx, sm.psi, sl, zy, c0, w); break;
+        default: lambda_term<0>(v, sx, gx, sm.psi, sl, zy, c0, w); break;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kMeasAmps; ++k)
+      if (x0 + threadIdx.x + k * stride < N) sm.lam[sx[k]] = v[k];
+  }
+}
+
 // lambda = sum_j g_j sum_t c_t P_t psi by measurement passes
 // (AccumulateOperators, util_qsim.h:362-414).  Streamed rows read psi tiles
 // and accumulate lambda tiles in their global slot.
@@ -1128,32 +1213,7 @@ __device__ void lambda_passes(const BatchDevice& b, const RunArgs& a,
         if (!first) tile_load(sm.lam, g_lam, sm.hi, base);
         __syncthreads();
       }
-      for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
-        float2 v = (first && !resident) ? make_float2(0.f, 0.f) : sm.lam[swz(x)];
-        for (int i = 0; i < nt; ++i) {
-          float w = sm.mterm[i].w;
-          if (w == 0.f) continue;
-          if (sm.mterm[i].identity) {
-            const float2 p = sm.psi[swz(x)];
-            v.x = fmaf(w, p.x, v.x);
-            v.y = fmaf(w, p.y, v.y);
-            continue;
-          }
-          const uint32_t y = x ^ sm.mterm[i].lflip;
-          float2 p = sm.psi[swz(y)];
-          const uint32_t yg = resident ? y : ((y & 31u) | sm.hi[y >> 5] | base);
-          if (__popc(yg & sm.mterm[i].zy) & 1) w = -w;
-          switch (sm.mterm[i].ny & 3) {  // multiply by i^ny
-            case 1: p = make_float2(-p.y, p.x); break;
-            case 2: p = make_float2(-p.x, -p.y); break;
-            case 3: p = make_float2(p.y, -p.x); break;
-            default: break;
-          }
-          v.x = fmaf(w, p.x, v.x);
-          v.y = fmaf(w, p.y, v.y);
-        }
-        sm.lam[swz(x)] = v;
-      }
+      lambda_tile(sm, nt, N, base, resident, first && !resident);
       __syncthreads();
       if (!resident) {
         tile_store(g_lam, sm.lam, sm.hi, base);
