@@ -206,6 +206,13 @@ void emit_forward(std::ostringstream& o, int id, const std::vector<uint32_t>& co
 }
 
 void emit_backward(std::ostringstream& o, int id, const std::vector<uint32_t>& codes) {
+  // gradient entries of the sub-pass; up to kRegGradEntries of them are
+  // accumulated in registers over the group iterations and warp-reduced once
+  constexpr int kRegGradEntries = 16;
+  int entries = 0;
+  for (uint32_t code : codes)
+    if ((code & 7) == OP_B1 || (code & 7) == OP_B2) entries += (code >> 18) & 3;
+  const bool in_regs = entries <= kRegGradEntries;
   o << "__device__ __noinline__ void jit_sub_" << id
     << "(uint32_t s_off, uint32_t l_off, int T, uint32_t base, uint32_t st_off,"
        " uint32_t rb_off, uint32_t rbits, int rbuf) {\n"
@@ -224,8 +231,15 @@ void emit_backward(std::ostringstream& o, int id, const std::vector<uint32_t>& c
        "    soff[k] = swz(o);\n"
        "  }\n"
        "  const uint32_t ngroups = 1u << (T - RB);\n"
-       "  const uint32_t iters = (ngroups + blockDim.x - 1) / blockDim.x;\n"
-       "  for (uint32_t it = 0; it < iters; ++it) {\n"
+       "  const uint32_t iters = (ngroups + blockDim.x - 1) / blockDim.x;\n";
+  // accumulator count padded to a power of two for warp_sum_many
+  int padded = 1, lg = 0;
+  while (padded < entries) { padded <<= 1; ++lg; }
+  if (in_regs && entries) {
+    o << "  float gp[" << padded << "];\n#pragma unroll\n  for (int e = 0; e < " << padded
+      << "; ++e) gp[e] = 0.f;\n";
+  }
+  o << "  for (uint32_t it = 0; it < iters; ++it) {\n"
        "    const uint32_t g = it * blockDim.x + threadIdx.x;\n"
        "    const bool active = g < ngroups;\n"
        "    const uint32_t gb = group_base(active ? g : 0u, rbits, RB);\n"
@@ -272,9 +286,13 @@ void emit_backward(std::ostringstream& o, int id, const std::vector<uint32_t>& c
               "u, gb, base)";
     o << "      if (" << cond << ") { " << call.str() << " } else { copy_regs(" << a << ", " << b
       << "); copy_regs(" << la << ", " << lb << "); }\n";
-    for (int q = 0; q < ng; ++q)
-      o << "      { float v = warp_sum(part[" << q << "]); if (lane == 0) { if (it == 0) rb->red[rbuf]["
-        << gi + q << "][warp] = v; else rb->red[rbuf][" << gi + q << "][warp] += v; } }\n";
+    for (int q = 0; q < ng; ++q) {
+      if (in_regs)
+        o << "      gp[" << gi + q << "] += part[" << q << "];\n";
+      else
+        o << "      { float v = warp_sum(part[" << q << "]); if (lane == 0) { if (it == 0) rb->red[rbuf]["
+          << gi + q << "][warp] = v; else rb->red[rbuf][" << gi + q << "][warp] += v; } }\n";
+    }
     o << "    }\n";
     gi += ng;
   }
@@ -282,7 +300,16 @@ void emit_backward(std::ostringstream& o, int id, const std::vector<uint32_t>& c
   const char* lfin = codes.size() % 2 ? "LB" : "LA";
   o << "    if (active) {\n#pragma unroll\n"
        "      for (int k = 0; k < NA; ++k) { s[sgb ^ soff[k]] = "
-    << fin << "[k]; l[sgb ^ soff[k]] = " << lfin << "[k]; }\n    }\n  }\n}\n\n";
+    << fin << "[k]; l[sgb ^ soff[k]] = " << lfin << "[k]; }\n    }\n  }\n";
+  if (in_regs && entries) {
+    // value j of the warp sums ends in lanes whose bits 4 .. 5 - lg spell j
+    const int low = 5 - lg;
+    o << "  {\n    const float v = warp_sum_many<" << padded << ">(gp, lane);\n"
+      << "    const int j = lane >> " << low << ";\n"
+      << "    if (j < " << entries << " && (lane & " << ((1 << low) - 1)
+      << ") == 0) rb->red[rbuf][j][warp] = v;\n  }\n";
+  }
+  o << "}\n\n";
 }
 
 std::string cache_dir() {

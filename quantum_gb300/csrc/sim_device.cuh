@@ -61,6 +61,38 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// Warp sums of P values at once (P a power of two, <= 32) by a transposing
+// butterfly: at each of the first log2(P) steps a lane keeps half of its
+// values, sends the other half to its partner lane and adds what it gets
+// back, so the value count halves while the lanes holding one value double.
+// Then value j of the warp total sits in the lanes whose bits 4, 3, ... spell
+// j; the remaining low lane bits are summed with plain butterflies.  Lane
+// (j << (5 - log2 P)) returns value j; the result in other lanes is partial.
+// Costs (P - 1) + (5 - log2 P) shuffles instead of 5 P.
+template <int P>
+__device__ __forceinline__ float warp_sum_many(float (&v)[P], int lane) {
+  static_assert(P >= 1 && P <= 32 && (P & (P - 1)) == 0, "P: power of two <= 32");
+  int m = P;
+#pragma unroll
+  for (int off = 16; off >= 1 && m > 1; off >>= 1) {
+    const bool up = lane & off;
+    m >>= 1;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (j < m) {
+        const float send = up ? v[j] : v[j + m];
+        const float keep = up ? v[j + m] : v[j];
+        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+      }
+    }
+  }
+  float s = v[0];
+  constexpr int kSteps = (P >= 32) ? 5 : (P >= 16) ? 4 : (P >= 8) ? 3 : (P >= 4) ? 2 : (P >= 2) ? 1 : 0;
+#pragma unroll
+  for (int off = 16 >> kSteps; off >= 1; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  return s;
+}
+
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
 __device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
 #pragma unroll
