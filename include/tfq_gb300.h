@@ -110,6 +110,19 @@ int tfqg_batch_noisy_expectation(tfqg_batch* b, const float* symbol_values,
                                  float* expectations, int device_buffers,
                                  void* stream);
 
+/* Sampled expectations [batch, num_ops]; num_samples int32 [batch, num_ops]
+ * measurement samples per Pauli term of each entry (each >= 1).  Replaces
+ * TfqSimulateSampledExpectationOp::Compute (tfq_simulate_sampled_expectation_
+ * op.cc:50-312; util_qsim.h:199-270): per term, the parities of num_samples
+ * measurements in the term's basis, averaged and weighted by the real
+ * coefficient; identity terms add their coefficient; empty programs give -2.
+ * The parities are drawn from the exact <P> (same distribution as sampling
+ * the rotated state).  FORWARD or ADJOINT batches with pauli sums. */
+int tfqg_batch_sampled_expectation(tfqg_batch* b, const float* symbol_values,
+                                   const int32_t* num_samples, uint64_t seed,
+                                   float* expectations, int device_buffers,
+                                   void* stream);
+
 /* Same result as tfqg_batch_expectation, for callers that must not let the
  * library allocate device memory (for example a host framework whose caching
  * allocator has already reserved nearly all device memory, so a plugin's own
@@ -156,6 +169,17 @@ int tfqg_noisy_expectation(const char* const* programs,
                            const int64_t* pauli_sum_lens, int64_t num_ops,
                            const int32_t* num_samples, uint64_t seed,
                            float* expectations);
+
+/* tfq_simulate_sampled_expectation (tfq_simulate_ops.py:101-135) */
+int tfqg_simulate_sampled_expectation(const char* const* programs,
+                                      const int64_t* program_lens, int64_t batch,
+                                      const char* const* symbol_names,
+                                      const int64_t* symbol_name_lens,
+                                      int64_t num_symbols, const float* symbol_values,
+                                      const char* const* pauli_sums,
+                                      const int64_t* pauli_sum_lens, int64_t num_ops,
+                                      const int32_t* num_samples, uint64_t seed,
+                                      float* expectations);
 
 #ifdef __cplusplus
 }

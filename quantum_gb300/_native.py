@@ -48,6 +48,7 @@ EXPORTED = (
     "tfqg_batch_expectation", "tfqg_batch_state", "tfqg_batch_samples",
     "tfqg_batch_adj_grad", "tfqg_batch_noisy_expectation",
     "tfqg_simulate_expectation", "tfqg_adj_grad", "tfqg_noisy_expectation",
+    "tfqg_batch_sampled_expectation", "tfqg_simulate_sampled_expectation",
 )
 
 
@@ -77,10 +78,14 @@ def _declare(lib):
     lib.tfqg_batch_noisy_expectation.argtypes = [
         c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p, ctypes.c_int,
         c_void_p]
+    lib.tfqg_batch_sampled_expectation.argtypes = [
+        c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p, ctypes.c_int,
+        c_void_p]
     for name in ("tfqg_batch_create", "tfqg_batch_max_num_qubits",
                  "tfqg_batch_expectation", "tfqg_batch_state",
                  "tfqg_batch_samples", "tfqg_batch_adj_grad",
                  "tfqg_batch_noisy_expectation", "tfqg_batch_expectation_noalloc",
+                 "tfqg_batch_sampled_expectation", "tfqg_simulate_sampled_expectation",
                  "tfqg_simulate_expectation",
                  "tfqg_adj_grad", "tfqg_noisy_expectation"):
         getattr(lib, name).restype = ctypes.c_int

@@ -742,6 +742,77 @@ int tfqg_batch_noisy_expectation(tfqg_batch* b, const float* symbol_values,
   });
 }
 
+int tfqg_batch_sampled_expectation(tfqg_batch* b, const float* symbol_values,
+                                   const int32_t* num_samples, uint64_t seed,
+                                   float* expectations, int device_buffers,
+                                   void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    if (b->kind == TFQG_KIND_NOISY)
+      throw Error(kInvalidArgument, "batch was created for noisy simulation");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t cells = b->B * b->n_ops;
+    const size_t obytes = size_t(cells) * sizeof(float);
+    if (cells == 0) return 0;
+    std::vector<int32_t> ns(static_cast<size_t>(cells));
+    if (device_buffers) {
+      TFQG_CUDA(cudaMemcpyAsync(ns.data(), num_samples, cells * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, s));
+      TFQG_CUDA(cudaStreamSynchronize(s));
+    } else {
+      memcpy(ns.data(), num_samples, cells * sizeof(int32_t));
+    }
+    for (int32_t v : ns)  // GetNumSamples (parse_context.cc:349-381)
+      if (v < 1)
+        throw Error(kInvalidArgument, "Each element of num_samples must be greater than 0.");
+    int64_t stride = 1;
+    for (const DevRow& r : b->rows)
+      stride = std::max<int64_t>(stride, int64_t(r.term_end) - int64_t(r.term_begin));
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, false, 0, s, &a);
+    b->aux.reserve(cells * sizeof(int32_t), b->device);
+    TFQG_CUDA(cudaMemcpyAsync(b->aux.p, ns.data(), cells * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, s));
+    b->aux2.reserve(size_t(b->B * stride) * sizeof(double), b->device);
+    a.term_vals = static_cast<double*>(b->aux2.p);
+    a.term_stride = stride;
+    float* dout = expectations;
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<float*>(b->out.p);
+    }
+    a.out_f = dout;
+    a.seed = seed;
+    simulate(b, kModeExpect, &a, s);
+    TFQG_CUDA(launch_sampled_expectation(b->bd, a, static_cast<const int32_t*>(b->aux.p), s));
+    finish(b, expectations, dout, obytes, device_buffers, s);
+    // the host vector above is read by an async copy: keep it alive
+    TFQG_CUDA(cudaStreamSynchronize(s));
+    return 0;
+  });
+}
+
+int tfqg_simulate_sampled_expectation(const char* const* programs,
+                                      const int64_t* program_lens, int64_t batch,
+                                      const char* const* symbol_names,
+                                      const int64_t* symbol_name_lens, int64_t num_symbols,
+                                      const float* symbol_values,
+                                      const char* const* pauli_sums,
+                                      const int64_t* pauli_sum_lens, int64_t num_ops,
+                                      const int32_t* num_samples, uint64_t seed,
+                                      float* expectations) {
+  tfqg_batch* b = nullptr;
+  int rc = tfqg_batch_create(programs, program_lens, batch, symbol_names,
+                             symbol_name_lens, num_symbols, pauli_sums, pauli_sum_lens,
+                             num_ops, TFQG_KIND_FORWARD, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_sampled_expectation(b, symbol_values, num_samples, seed, expectations, 0,
+                                      nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
 int tfqg_simulate_expectation(const char* const* programs,
                               const int64_t* program_lens, int64_t batch,
                               const char* const* symbol_names,

@@ -105,6 +105,57 @@ __global__ void noisy_finalize_kernel(BatchDevice b, RunArgs a) {
   a.out_f[t] = reps > 0 ? float(a.acc[t] / double(reps)) : 0.f;
 }
 
+// ---- sampled expectation ------------------------------------------------------
+
+// One warp per (row, op) (tfq_simulate_sampled_expectation_op.cc:139-312,
+// util_qsim.h:199-270).  The reference rotates a copy of the state into the
+// measurement basis of each Pauli term, draws N bitstrings and adds
+// float(parity_total) * coef / float(N).  The parity of one such sample is
+// +1 with probability (1 + <P>)/2, independently per sample, so this kernel
+// draws the N parities directly as Bernoulli trials from the exact <P>
+// (same distribution of the result) and combines them with the reference's
+// float arithmetic, term by term in pauli-sum order.  Identity terms add
+// their coefficient; empty programs give -2.
+__global__ void sampled_expectation_kernel(BatchDevice b, RunArgs a,
+                                           const int32_t* num_samples) {
+  const int64_t wid = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= int64_t(b.num_rows) * b.num_ops) return;
+  const int row = int(wid / b.num_ops), op = int(wid % b.num_ops);
+  const DevRow r = b.rows[row];
+  const DevProgram p = b.programs[r.program];
+  float* out = a.out_f + wid;
+  if (p.n == 0 || p.fwd_pass_begin == p.fwd_pass_end) {
+    if (lane == 0) *out = -2.f;
+    return;
+  }
+  const int N = num_samples[wid];
+  float ev = 0.f;
+  for (uint32_t t = r.term_begin; t < r.term_end; ++t) {
+    const DevTerm term = b.terms[t];
+    if (term.op != op) continue;
+    if (term.identity) {
+      ev += term.coef;
+      continue;
+    }
+    const double v = a.term_vals[int64_t(row) * a.term_stride + (t - r.term_begin)];
+    const double pp = fmin(fmax(0.5 + 0.5 * v, 0.0), 1.0);  // P(parity = +1)
+    const double thr = pp * 4294967296.0;
+    int k = 0;
+    for (int s0 = 4 * lane; s0 < N; s0 += 128) {
+      const uint4 u = philox(make_uint4(uint32_t(row), t, uint32_t(s0 >> 2), 0x5EA7u),
+                             make_uint2(uint32_t(a.seed), uint32_t(a.seed >> 32)));
+      k += (double(u.x) < thr) + (s0 + 1 < N && double(u.y) < thr) +
+           (s0 + 2 < N && double(u.z) < thr) + (s0 + 3 < N && double(u.w) < thr);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    const int parity_total = 2 * k - N;
+    ev += static_cast<float>(parity_total) * term.coef / static_cast<float>(N);
+  }
+  if (lane == 0) *out = ev;
+}
+
 // ---- wide rows --------------------------------------------------------------
 
 __global__ void __launch_bounds__(kWideThreads, 2)
@@ -139,6 +190,9 @@ __global__ void wide_expect_finalize_kernel(BatchDevice b, RunArgs a, int row,
           }
         }
         acc[t.op] += double(t.coef) * v;
+        if (a.term_vals)
+          a.term_vals[int64_t(row) * a.term_stride +
+                      (b.meas_terms[i].term - r.term_begin)] = v;
       }
     }
   }
@@ -302,6 +356,16 @@ cudaError_t launch_simulate(int mode, const BatchDevice& b, const RunArgs& a,
     case kModeAdjoint: return sim_launch_adjoint(b, a, grid, smem, state_amps, nstates, s);
     default: return sim_launch_noisy(b, a, grid, smem, state_amps, nstates, s);
   }
+}
+
+cudaError_t launch_sampled_expectation(const BatchDevice& b, const RunArgs& a,
+                                       const int32_t* num_samples, cudaStream_t s) {
+  const int64_t warps = int64_t(b.num_rows) * b.num_ops;
+  if (warps == 0) return cudaSuccess;
+  const int threads = 256;
+  const int64_t blocks = (warps * 32 + threads - 1) / threads;
+  sampled_expectation_kernel<<<unsigned(blocks), threads, 0, s>>>(b, a, num_samples);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_noisy_finalize(const BatchDevice& b, const RunArgs& a,

@@ -54,6 +54,8 @@ struct RunArgs {
   uint64_t seed = 0;
   int grad_rule = 0;                 // 0: reference finite difference, 1: exact
   int* error_flag = nullptr;         // device word; nonzero = kernel-side error
+  double* term_vals = nullptr;       // optional [rows, term_stride]: <psi|P_t|psi>
+  int64_t term_stride = 0;           // per term of the row (no coefficient)
 };
 
 // Threads per CTA of the simulation kernel.
@@ -78,6 +80,11 @@ cudaError_t launch_simulate(int mode, const BatchDevice& b, const RunArgs& a,
                             cudaStream_t s);
 cudaError_t launch_noisy_finalize(const BatchDevice& b, const RunArgs& a,
                                   cudaStream_t s);
+// Sampled expectation from the term values a.term_vals: per (row, op), each
+// term's N = num_samples[row, op] measurement parities drawn as Bernoulli
+// trials; writes a.out_f.
+cudaError_t launch_sampled_expectation(const BatchDevice& b, const RunArgs& a,
+                                       const int32_t* num_samples, cudaStream_t s);
 
 // Per-mode interpreter kernels (sim_<mode>.cu): kernel address and launcher.
 #define TFQG_SIM_DECL(name)                                                     \

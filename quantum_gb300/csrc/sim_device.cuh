@@ -1146,6 +1146,9 @@ __device__ void measure_passes(const BatchDevice& b, const RunArgs& a,
           }
         }
         sink(int(sm.mterm[i].op), double(sm.mterm[i].w) * v);
+        if (a.term_vals)
+          a.term_vals[int64_t(rc.row) * a.term_stride +
+                      (b.meas_terms[M.begin + i].term - rc.r.term_begin)] = v;
       }
     }
     __syncthreads();

@@ -216,9 +216,9 @@ class Batch:
             self._device_flag(v), _stream(v)))
         return self._wrap(symbol_values, out)
 
-    def noisy_expectation(self, symbol_values, num_samples, seed=None):
-        v = self._host_or_cuda(_values(symbol_values))
-        self._check_values(v)
+    def _num_samples_2d(self, num_samples):
+        """num_samples [batch, num_ops] int32 with the reference's checks
+        (parse_context.cc:349-381 and the ops' dimension checks)."""
         ns = np.asarray(num_samples.cpu().numpy() if _is_torch(num_samples)
                         else num_samples, dtype=np.int32)
         if ns.ndim != 2:
@@ -234,19 +234,34 @@ class Batch:
                 "Dimension 1 of num_samples and pauli_sums do not match.Got "
                 f"{ns.shape[1]} lists of sample sizes and {self.num_ops} "
                 "lists of pauli sums.")
+        return np.ascontiguousarray(ns)
+
+    def _counts_call(self, fn, symbol_values, num_samples, seed):
+        v = self._host_or_cuda(_values(symbol_values))
+        self._check_values(v)
+        ns = self._num_samples_2d(num_samples)
         if seed is None:
             seed = int.from_bytes(os.urandom(8), "little")
-        ns = np.ascontiguousarray(ns)
         dev = self._device_flag(v)
-        nsp = ns
-        if dev:
-            nsp = torch.as_tensor(ns, device=v.device)
+        nsp = torch.as_tensor(ns, device=v.device) if dev else ns
         out = self._out(v, (self.batch_size, self.num_ops), np.float32,
                         getattr(torch, "float32", None))
-        _native.check(_native.lib().tfqg_batch_noisy_expectation(
-            self._h, _ptr(v), _ptr(nsp), seed & (2 ** 64 - 1), _ptr(out), dev,
-            _stream(v)))
+        _native.check(fn(self._h, _ptr(v), _ptr(nsp), seed & (2 ** 64 - 1),
+                         _ptr(out), dev, _stream(v)))
         return self._wrap(symbol_values, out)
+
+    def noisy_expectation(self, symbol_values, num_samples, seed=None):
+        """Trajectory expectations (noise/noisy_expectation_op.py:23-98);
+        num_samples [batch, num_ops] trajectories per entry."""
+        return self._counts_call(_native.lib().tfqg_batch_noisy_expectation,
+                                 symbol_values, num_samples, seed)
+
+    def sampled_expectation(self, symbol_values, num_samples, seed=None):
+        """Expectations estimated from measurement samples
+        (tfq_simulate_ops.py:101-135); num_samples [batch, num_ops] samples
+        per Pauli term."""
+        return self._counts_call(_native.lib().tfqg_batch_sampled_expectation,
+                                 symbol_values, num_samples, seed)
 
     @staticmethod
     def _wrap(symbol_values, out):
@@ -302,6 +317,16 @@ def tfq_adj_grad(programs, symbol_names, symbol_values, pauli_sums, prev_grad,
     b = Batch(programs, symbol_names, pauli_sums, KIND_ADJOINT)
     try:
         return b.adj_grad(symbol_values, prev_grad, grad_rule)
+    finally:
+        b.close()
+
+
+def tfq_simulate_sampled_expectation(programs, symbol_names, symbol_values,
+                                     pauli_sums, num_samples, seed=None):
+    """tfq_simulate_ops.py:101-135."""
+    b = Batch(programs, symbol_names, pauli_sums, KIND_FORWARD)
+    try:
+        return b.sampled_expectation(symbol_values, num_samples, seed)
     finally:
         b.close()
 

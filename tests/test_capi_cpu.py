@@ -109,3 +109,23 @@ def test_empty_batch():
     b = ops.Batch([], [], np.zeros((0, 0), dtype=object).tolist() or
                   np.empty((0, 0), dtype=object))
     assert b.batch_size == 0
+
+
+def test_sampled_expectation_input_checks():
+    """tfq_simulate_ops_test.py sampled-expectation input checks: rank and
+    dimension messages, and num_samples elements >= 1 (parse_context.cc:
+    349-381), raised before any GPU work."""
+    prog = _prog([S.HPow(Q[0]), S.I(Q[1])])
+    ps = S.serialize_paulisum([(1.0, [(Q[0], "Z")])])
+    b = ops.Batch([prog], [], [[ps]])
+    with pytest.raises(_native.InvalidArgumentError, match="num_samples must be rank 2"):
+        b.sampled_expectation(np.zeros((1, 0), np.float32), [1])
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="Dimension 0 of num_samples and pauli_sums do not match"):
+        b.sampled_expectation(np.zeros((1, 0), np.float32), [[1], [1]])
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="Dimension 1 of num_samples and pauli_sums do not match"):
+        b.sampled_expectation(np.zeros((1, 0), np.float32), [[1, 1]])
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="Each element of num_samples must be greater than 0"):
+        b.sampled_expectation(np.zeros((1, 0), np.float32), [[0]])

@@ -231,3 +231,42 @@ def test_torch_autograd_cuda():
     want_g = O.adj_grad(programs, names, values, psums, w.cpu().numpy())
     np.testing.assert_allclose(e.detach().cpu().numpy(), want_e, atol=1e-4)
     np.testing.assert_allclose(v.grad.cpu().numpy(), want_g, atol=1e-4)
+
+
+@pytest.mark.parametrize("nqs", [[3, 5], [8, 12], [16]])
+def test_sampled_expectation_matches_exact_within_sampling_error(nqs):
+    """tfq_simulate_sampled_expectation: the estimate of each op is a sum over
+    terms of coef * mean parity; its standard deviation is
+    sqrt(sum_t coef_t^2 (1 - <P_t>^2) / N).  Checked at 5 standard deviations
+    against the oracle's exact expectation."""
+    rng = np.random.default_rng(300 + sum(nqs))
+    programs, names, values, psums = _batch(rng, nqs, 5)
+    N = 20000
+    ns = np.full((len(nqs), 2), N, np.int32)
+    got = ops.tfq_simulate_sampled_expectation(programs, names, values, psums, ns, seed=17)
+    want = O.simulate_expectation(programs, names, values, psums)
+    coefs = []
+    for row in psums:
+        coefs.append([sum(c * c for c, _ in _terms(p)) for p in row])
+    bound = 5 * np.sqrt(np.asarray(coefs) / N) + 1e-5
+    assert np.all(np.abs(got - want) <= bound), (got, want, bound)
+    # the same seed reproduces the draws
+    again = ops.tfq_simulate_sampled_expectation(programs, names, values, psums, ns, seed=17)
+    np.testing.assert_array_equal(got, again)
+
+
+def _terms(paulisum_bytes):
+    """(coefficient, paulis) of the non-identity terms of a serialized sum."""
+    return [(float(t["re"]), t["paulis"]) for t in O.decode_paulisum(paulisum_bytes)
+            if t["paulis"]]
+
+
+def test_sampled_expectation_empty_program_and_identity():
+    q = S.GridQubit.rect(1, 2)
+    prog = S.serialize_circuit(S.Circuit([[S.X(q[0]), S.I(q[1])]]))
+    empty = S.serialize_circuit(S.Circuit([]))
+    ps = S.serialize_paulisum([(0.5, []), (2.0, [(q[0], "Z")])])
+    got = ops.tfq_simulate_sampled_expectation([prog, empty], [], np.zeros((2, 0)),
+                                               [[ps], [ps]], np.full((2, 1), 100, np.int32))
+    # X|0> = |1>: Z = -1 exactly, so every parity is -1
+    np.testing.assert_allclose(got, [[0.5 - 2.0], [-2.0]], atol=1e-6)
