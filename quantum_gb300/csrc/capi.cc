@@ -931,6 +931,21 @@ int tfqg_internal_batch_wide_rows(void* batch) {
   return b ? int(b->wide_rows.size()) : -1;
 }
 
+// FNV-1a hash of the batch's packed host tables: equal for batches that
+// compile to the same programs, terms and plans.
+uint64_t tfqg_internal_batch_fingerprint(void* batch) {
+  const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
+  if (!b) return 0;
+  std::vector<unsigned char> blob;
+  pack_tables(b, &blob);
+  uint64_t h = 1469598103934665603ull;
+  for (unsigned char c : blob) {
+    h ^= c;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
 int tfqg_internal_batch_row_costs(void* batch, double* costs) {
   const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
   if (!b || (b->B > 0 && !costs)) return kInvalidArgument;

@@ -213,18 +213,27 @@ const ArgP* OpP::find(const std::string& key) const {
   return nullptr;
 }
 
+// Binary first, then text format (ParseProto, parse_context.cc:155-170).
 void decode_program(const char* data, size_t len, ProgramP* out) {
   *out = ProgramP();
-  if (!parse_program(reinterpret_cast<const uint8_t*>(data), len, out))
-    throw Error(kInvalidArgument,
-                "Unparseable proto: " + std::string(data, len));
+  if (parse_program(reinterpret_cast<const uint8_t*>(data), len, out)) return;
+  std::string wire;
+  *out = ProgramP();
+  if (text_proto_to_wire(data, len, false, &wire) &&
+      parse_program(reinterpret_cast<const uint8_t*>(wire.data()), wire.size(), out))
+    return;
+  throw Error(kInvalidArgument, "Unparseable proto: " + std::string(data, len));
 }
 
 void decode_paulisum(const char* data, size_t len, PauliSumP* out) {
   out->clear();
-  if (!parse_paulisum(reinterpret_cast<const uint8_t*>(data), len, out))
-    throw Error(kInvalidArgument,
-                "Unparseable proto: " + std::string(data, len));
+  if (parse_paulisum(reinterpret_cast<const uint8_t*>(data), len, out)) return;
+  std::string wire;
+  out->clear();
+  if (text_proto_to_wire(data, len, true, &wire) &&
+      parse_paulisum(reinterpret_cast<const uint8_t*>(wire.data()), wire.size(), out))
+    return;
+  throw Error(kInvalidArgument, "Unparseable proto: " + std::string(data, len));
 }
 
 bool simple_atoi(const std::string& s, int64_t* out) {

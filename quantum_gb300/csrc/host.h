@@ -52,6 +52,9 @@ struct TermP {
 using PauliSumP = std::vector<TermP>;
 
 void decode_program(const char* data, size_t len, ProgramP* out);
+// Protobuf text format of a Program (pauli_sum = false) or PauliSum,
+// re-encoded in the binary wire format; false if it does not parse.
+bool text_proto_to_wire(const char* data, size_t len, bool pauli_sum, std::string* wire);
 void decode_paulisum(const char* data, size_t len, PauliSumP* out);
 
 // absl::SimpleAtoi semantics: optional surrounding whitespace and sign.

@@ -45,6 +45,7 @@ int tfqg_internal_batch_passes(void* batch, int32_t* fwd, int32_t* bwd,
 // for empty programs), used to shard a batch across devices.
 int tfqg_internal_batch_row_costs(void* batch, double* costs);
 int tfqg_internal_set_wide_min_qubits(int n);
+uint64_t tfqg_internal_batch_fingerprint(void* batch);
 int tfqg_internal_batch_wide_rows(void* batch);
 // Expectation + adjoint gradient of a uniform batch by the plain path, all
 // buffers on the device.  Used by bench.py as the comparison baseline.

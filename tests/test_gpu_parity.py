@@ -270,3 +270,15 @@ def test_sampled_expectation_empty_program_and_identity():
                                                [[ps], [ps]], np.full((2, 1), 100, np.int32))
     # X|0> = |1>: Z = -1 exactly, so every parity is -1
     np.testing.assert_allclose(got, [[0.5 - 2.0], [-2.0]], atol=1e-6)
+
+
+def test_text_format_inputs_give_identical_results():
+    """Programs and pauli sums given in protobuf text format (the reference's
+    TextFormat fallback, parse_context.cc:155-170) run exactly like binary."""
+    from tests import textfmt
+    rng = np.random.default_rng(77)
+    programs, names, values, psums = _batch(rng, [4, 7, 12], 5)
+    tp = [textfmt.to_text(p).encode() for p in programs]
+    tps = [[textfmt.to_text(x, "PauliSum").encode() for x in row] for row in psums]
+    np.testing.assert_array_equal(ops.tfq_simulate_expectation(tp, names, values, tps),
+                                  ops.tfq_simulate_expectation(programs, names, values, psums))
