@@ -42,6 +42,7 @@ extern "C" {
 #define TFQG_KIND_FORWARD 0 /* expectation / state / samples */
 #define TFQG_KIND_ADJOINT 1 /* adjoint gradient (and forward) */
 #define TFQG_KIND_NOISY 2   /* noisy trajectories (channels allowed) */
+#define TFQG_KIND_INNER 3   /* tfq_inner_product (tfqg_batch_create_inner_product) */
 
 /* Derivative rule of the adjoint gradient. */
 #define TFQG_GRAD_REFERENCE_FD 0 /* (G(x+5e-3)-G(x-5e-3))/1e-2, adj_util.cc:32 */
@@ -123,6 +124,28 @@ int tfqg_batch_sampled_expectation(tfqg_batch* b, const float* symbol_values,
                                    float* expectations, int device_buffers,
                                    void* stream);
 
+/* tfq_inner_product batches (TFQG_KIND_INNER).  other_programs holds
+ * batch x num_others serialized programs, row-major; each resolves its qubits
+ * with the map of its reference program and must use exactly its qubits
+ * (ResolveQubitIds with other_programs, program_resolution.cc:188-310) and
+ * hold no symbols.  Replaces the parse part of TfqInnerProductOp::Compute
+ * (math_ops/tfq_inner_product.cc:48-166). */
+int tfqg_batch_create_inner_product(const char* const* programs,
+                                    const int64_t* program_lens, int64_t batch,
+                                    const char* const* symbol_names,
+                                    const int64_t* symbol_name_lens, int64_t num_symbols,
+                                    const char* const* other_programs,
+                                    const int64_t* other_program_lens, int64_t num_others,
+                                    tfqg_batch** out);
+
+/* <psi_i | phi_ij> as complex64 [batch, num_others] (interleaved re, im),
+ * fp64 sums; 1 for an empty reference program.  Replaces
+ * TfqInnerProductOp::ComputeLarge/Small (math_ops/tfq_inner_product.cc:
+ * 168-279).  symbol_values is [batch, num_symbols] for the reference
+ * programs. */
+int tfqg_batch_inner_product(tfqg_batch* b, const float* symbol_values,
+                             void* inner_products, int device_buffers, void* stream);
+
 /* Same result as tfqg_batch_expectation, for callers that must not let the
  * library allocate device memory (for example a host framework whose caching
  * allocator has already reserved nearly all device memory, so a plugin's own
@@ -180,6 +203,14 @@ int tfqg_simulate_sampled_expectation(const char* const* programs,
                                       const int64_t* pauli_sum_lens, int64_t num_ops,
                                       const int32_t* num_samples, uint64_t seed,
                                       float* expectations);
+
+/* tfq_inner_product (math_ops/inner_product_op.py) */
+int tfqg_inner_product(const char* const* programs, const int64_t* program_lens,
+                       int64_t batch, const char* const* symbol_names,
+                       const int64_t* symbol_name_lens, int64_t num_symbols,
+                       const float* symbol_values, const char* const* other_programs,
+                       const int64_t* other_program_lens, int64_t num_others,
+                       void* inner_products);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,8 @@ complex128 numpy, the algorithm of the reference ops:
 * adjoint gradient ........ tensorflow_quantum/core/ops/tfq_adj_grad_op.cc:199-276,
   AccumulateOperators util_qsim.h:362-414, FD gradient gates
   tensorflow_quantum/core/src/adj_util.cc:32,175-302
+* inner product ........... tensorflow_quantum/core/ops/math_ops/tfq_inner_product.cc,
+  paired resolution program_resolution.cc:188-310
 * noisy expectation ....... tensorflow_quantum/core/ops/noise/tfq_noisy_expectation.cc
   (restated as an exact density-matrix evolution: the trajectory average
   converges to it)
@@ -650,6 +652,64 @@ def simulate_state(programs, symbol_names, symbol_values):
             continue
         psi = simulate([g for _, g in items], n)
         out[i, :2 ** n] = psi.reshape(-1)
+    return out
+
+
+def _check_paired(moments, index):
+    """program_resolution.cc:253-307: a paired circuit uses exactly the
+    reference circuit's qubits."""
+    visited = set()
+    for m in moments:
+        for op in m:
+            qs = list(op["qubits"])
+            cs = _control_str(op, "control_qubits")
+            if cs:
+                qs += cs.split(",")
+            for q in qs:
+                if q not in index:
+                    raise InvalidArgument("A paired circuit contains qubits not "
+                                          "found in reference circuit.")
+                visited.add(q)
+    if len(visited) != len(index):
+        raise InvalidArgument("A reference circuit contains qubits not found in "
+                              "paired circuit.")
+
+
+def inner_product(programs, symbol_names, symbol_values, other_programs):
+    """tfq_inner_product (math_ops/tfq_inner_product.cc): out[i, j] =
+    <psi_i(values_i) | phi_ij>, 1 for an empty reference program."""
+    others = np.asarray(other_programs, dtype=object)
+    if others.ndim != 2:
+        raise InvalidArgument("other_programs must be rank 2. Got rank %d." % others.ndim)
+    moms = [decode_program(p) for p in programs]
+    other_moms = [[decode_program(x) for x in row] for row in others]
+    if len(moms) != len(other_moms):
+        raise InvalidArgument("programs and other_programs batch dimension do not "
+                              "match. Foud: %d and %d" % (len(moms), len(other_moms)))
+    resolved = []
+    for i, m in enumerate(moms):
+        n, index = resolve(m)
+        if n > 0:
+            for om in other_moms[i]:
+                _check_paired(om, index)
+        resolved.append((n, index))
+    maps = _symbol_maps(symbol_names, symbol_values)
+    gates = [[build_gate(op, idx, maps[i]) for mom in moms[i] for op in mom] if n else []
+             for i, (n, idx) in enumerate(resolved)]
+    out = np.zeros((len(moms), others.shape[1]), dtype=np.complex128)
+    for i, (n, index) in enumerate(resolved):
+        if not gates[i]:
+            out[i, :] = 1.0
+            continue
+        psi = simulate(gates[i], n).reshape(-1)
+        for j, om in enumerate(other_moms[i]):
+            try:
+                og = [build_gate(op, index, {}) for mom in om for op in mom]
+            except (InvalidArgument, KeyError):
+                raise InvalidArgument("Found symbols in other_programs.No symbols "
+                                      "are allowed in these circuits.") from None
+            phi = simulate(og, n).reshape(-1) if og else np.eye(1, 2 ** n, dtype=np.complex128)[0]
+            out[i, j] = np.vdot(psi, phi)
     return out
 
 

@@ -57,6 +57,8 @@ int set_last_error(int code, const std::string& msg);
 struct tfqg_batch {
   int kind = 0;
   int64_t B = 0, P = 0, n_ops = 0;
+  int64_t value_rows = 0;          // rows that take symbol values
+  int64_t inner_rows = 0, inner_others = 0;  // TFQG_KIND_INNER shape
   int max_n = 0;
   int max_resident_n = -1;   // largest resident row (-1: none)
   bool any_streamed = false;

@@ -53,15 +53,28 @@ struct Str {
 std::string make_key(const char* p, int64_t n) { return std::string(p, size_t(n)); }
 
 // Parses/compiles every row.  Throws Error on invalid input.
+// TFQG_KIND_INNER: `others` holds batch x num_others paired programs
+// (tfq_inner_product's other_programs); they become rows batch + i *
+// num_others + j, resolved with the qubit map of their reference row i.
 void build_batch(tfqg_batch* b, const char* const* programs,
                  const int64_t* program_lens, int64_t batch,
                  const char* const* symbol_names, const int64_t* name_lens,
                  int64_t num_symbols, const char* const* pauli_sums,
-                 const int64_t* psum_lens, int64_t num_ops, int kind) {
-  if (batch < 0 || num_symbols < 0 || num_ops < 0)
+                 const int64_t* psum_lens, int64_t num_ops, int kind,
+                 const char* const* others = nullptr,
+                 const int64_t* other_lens = nullptr, int64_t num_others = 0) {
+  if (batch < 0 || num_symbols < 0 || num_ops < 0 || num_others < 0)
     throw Error(kInvalidArgument, "negative dimension");
   if (num_ops > 65535)
     throw Error(kInvalidArgument, "at most 65535 pauli_sums columns are supported");
+  const bool inner = kind == TFQG_KIND_INNER;
+  const int64_t main_rows = batch;
+  if (inner) {
+    b->inner_rows = batch;
+    b->inner_others = num_others;
+    batch = batch + batch * num_others;
+  }
+  b->value_rows = main_rows;
   b->kind = kind;
   b->B = batch;
   b->P = num_symbols;
@@ -74,17 +87,25 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   std::unordered_map<std::string, int> prog_ids;
   std::vector<ProgramP> parsed;
   std::vector<int> row_prog(static_cast<size_t>(batch));
+  std::vector<int> pair_of;  // paired program -> its reference program
   for (int64_t i = 0; i < batch; ++i) {
-    std::string key = make_key(programs[i], program_lens[i]);
+    const bool paired = i >= main_rows;
+    const int64_t k = i - main_rows;  // paired row (main row k / num_others)
+    const char* data = paired ? others[k] : programs[i];
+    const int64_t len = paired ? other_lens[k] : program_lens[i];
+    std::string key = make_key(data, len);
+    // a paired program resolves through its reference program's qubits
+    if (paired) key += "\0@" + std::to_string(row_prog[k / num_others]);
     auto it = prog_ids.find(key);
     if (it != prog_ids.end()) {
       row_prog[i] = it->second;
       continue;
     }
     ProgramP p;
-    decode_program(programs[i], size_t(program_lens[i]), &p);
+    decode_program(data, size_t(len), &p);
     int id = int(parsed.size());
     parsed.push_back(std::move(p));
+    pair_of.push_back(paired ? row_prog[k / num_others] : -1);
     prog_ids.emplace(std::move(key), id);
     row_prog[i] = id;
   }
@@ -117,13 +138,32 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   std::vector<std::unordered_map<std::string, int>> index(parsed.size());
   std::vector<char> resolved(parsed.size(), 0);
   // qubit resolution errors surface per row in batch order, before
-  // circuit-construction errors, like GetProgramsAndNumQubits
+  // circuit-construction errors, like GetProgramsAndNumQubits; a paired
+  // program uses its reference's map (checked right after that reference,
+  // as ResolveQubitIds(program, num_qubits, other_programs) does) and is
+  // empty when its reference is
+  auto resolve_paired = [&](int64_t i) {
+    for (int64_t j = 0; j < num_others; ++j) {
+      const int pid = row_prog[main_rows + i * num_others + j];
+      if (resolved[pid]) continue;
+      const int mpid = pair_of[pid];
+      if (parsed[mpid].moments.empty()) {
+        parsed[pid].moments.clear();
+      } else {
+        check_paired_qubits(parsed[pid], index[mpid]);
+        index[pid] = index[mpid];
+      }
+      resolved[pid] = 1;
+    }
+  };
   for (int64_t i = 0; i < batch; ++i) {
     int pid = row_prog[i];
+    if (i >= main_rows) break;  // paired rows: resolved with their reference
     if (!resolved[pid]) {
       resolve_qubits(parsed[pid], &index[pid]);
       resolved[pid] = 1;
     }
+    if (inner) resolve_paired(i);
     if (parsed[pid].moments.empty()) continue;  // (#679) empty program
     for (int64_t j = 0; j < num_ops; ++j) {
       const PauliSumP& ps = psums[row_psum[i * num_ops + j]];
@@ -135,8 +175,23 @@ void build_batch(tfqg_batch* b, const char* const* programs,
                         "circuit.");
     }
   }
+  // reference programs first (their errors come first), then the paired
+  // ones, which may not hold symbols (tfq_inner_product.cc: any construction
+  // error of an other_program reports the symbols message)
+  const SymbolTable no_symbols;
   for (size_t pid = 0; pid < parsed.size(); ++pid) {
+    if (inner && pair_of[pid] >= 0) continue;
     compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
+    plan_program(&compiled[pid], job);
+  }
+  for (size_t pid = 0; pid < parsed.size() && inner; ++pid) {
+    if (pair_of[pid] < 0) continue;
+    try {
+      compile_program(parsed[pid], no_symbols, job, &compiled[pid], &index[pid]);
+    } catch (const Error&) {
+      throw Error(kInvalidArgument,
+                  "Found symbols in other_programs.No symbols are allowed in these circuits.");
+    }
     plan_program(&compiled[pid], job);
   }
 
@@ -354,7 +409,7 @@ const float* prepare(tfqg_batch* b, const float* values, int device_buffers,
                      bool grads, int grad_rule, cudaStream_t s, RunArgs* a) {
   ensure_device(b, s);
   const float* dvals = values;
-  size_t vbytes = size_t(b->B * b->P) * sizeof(float);
+  size_t vbytes = size_t(b->value_rows * b->P) * sizeof(float);
   if (!device_buffers && vbytes) {
     b->values.reserve(vbytes, b->device);
     TFQG_CUDA(cudaMemcpyAsync(b->values.p, values, vbytes,
@@ -809,6 +864,73 @@ int tfqg_simulate_sampled_expectation(const char* const* programs,
   if (rc) return rc;
   rc = tfqg_batch_sampled_expectation(b, symbol_values, num_samples, seed, expectations, 0,
                                       nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
+int tfqg_batch_create_inner_product(const char* const* programs,
+                                    const int64_t* program_lens, int64_t batch,
+                                    const char* const* symbol_names,
+                                    const int64_t* symbol_name_lens, int64_t num_symbols,
+                                    const char* const* other_programs,
+                                    const int64_t* other_program_lens, int64_t num_others,
+                                    tfqg_batch** out) {
+  return guarded([&]() {
+    if (!out) throw Error(kInvalidArgument, "out is NULL");
+    *out = nullptr;
+    std::unique_ptr<tfqg_batch> b(new tfqg_batch());
+    build_batch(b.get(), programs, program_lens, batch, symbol_names, symbol_name_lens,
+                num_symbols, nullptr, nullptr, 0, TFQG_KIND_INNER, other_programs,
+                other_program_lens, num_others);
+    *out = b.release();
+    return 0;
+  });
+}
+
+int tfqg_batch_inner_product(tfqg_batch* b, const float* symbol_values,
+                             void* inner_products, int device_buffers, void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    if (b->kind != TFQG_KIND_INNER)
+      throw Error(kInvalidArgument, "batch was not created for inner products");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t pairs = b->inner_rows * b->inner_others;
+    const size_t obytes = size_t(pairs) * sizeof(float2);
+    if (pairs == 0) return 0;
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, false, 0, s, &a);
+    const int64_t stride = int64_t(1) << b->max_n;
+    b->aux.reserve(size_t(b->B * stride) * sizeof(float2), b->device);
+    a.out_state = static_cast<float2*>(b->aux.p);
+    simulate(b, kModeState, &a, s);
+    b->aux2.reserve(size_t(pairs) * 2 * sizeof(double), b->device);
+    double* acc = static_cast<double*>(b->aux2.p);
+    TFQG_CUDA(cudaMemsetAsync(acc, 0, size_t(pairs) * 2 * sizeof(double), s));
+    float2* dout = static_cast<float2*>(inner_products);
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<float2*>(b->out.p);
+    }
+    TFQG_CUDA(launch_inner_products(b->bd, a.out_state, stride, int(b->inner_rows),
+                                    int(b->inner_others), acc, dout, s));
+    finish(b, inner_products, dout, obytes, device_buffers, s);
+    return 0;
+  });
+}
+
+int tfqg_inner_product(const char* const* programs, const int64_t* program_lens,
+                       int64_t batch, const char* const* symbol_names,
+                       const int64_t* symbol_name_lens, int64_t num_symbols,
+                       const float* symbol_values, const char* const* other_programs,
+                       const int64_t* other_program_lens, int64_t num_others,
+                       void* inner_products) {
+  tfqg_batch* b = nullptr;
+  int rc = tfqg_batch_create_inner_product(programs, program_lens, batch, symbol_names,
+                                           symbol_name_lens, num_symbols, other_programs,
+                                           other_program_lens, num_others, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_inner_product(b, symbol_values, inner_products, 0, nullptr);
   tfqg_batch_destroy(b);
   return rc;
 }

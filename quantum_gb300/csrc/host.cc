@@ -316,6 +316,31 @@ int resolve_qubits(const ProgramP& prog,
   return i;
 }
 
+void check_paired_qubits(const ProgramP& other,
+                         const std::unordered_map<std::string, int>& index) {
+  std::set<std::string> visited;
+  for (const auto& m : other.moments)
+    for (const auto& op : m) {
+      for (const auto& q : op.qubits) {
+        if (!index.count(q))
+          throw Error(kInvalidArgument,
+                      "A paired circuit contains qubits not found in reference circuit.");
+        visited.insert(q);
+      }
+      const std::string& cs = control_string(op, "control_qubits");
+      if (cs.empty()) continue;
+      for (const std::string& q : split(cs, ',')) {
+        if (!index.count(q))
+          throw Error(kInvalidArgument,
+                      "A paired circuit contains qubits not found in reference circuit.");
+        visited.insert(q);
+      }
+    }
+  if (visited.size() != index.size())
+    throw Error(kInvalidArgument,
+                "A reference circuit contains qubits not found in paired circuit.");
+}
+
 // ---------------------------------------------------------------------------
 // gate templates (circuit_parser_qsim.cc:53-596)
 // ---------------------------------------------------------------------------
@@ -860,6 +885,13 @@ void plan_sequence(const CompiledProgram& p, const std::vector<PlanItem>& items,
   }
   std::vector<PlanItem> remaining = items;
   const uint32_t lanes = low_mask(kLaneBits);
+  if (remaining.empty()) {
+    // gates that do nothing (identities) still make a non-empty program, as
+    // in the reference, whose fused circuit keeps them: one pass, no ops
+    passes->push_back(DevPass{low_mask(tile_bits), uint32_t(ops->size()),
+                              uint32_t(ops->size()), 0});
+    return;
+  }
   while (!remaining.empty()) {
     uint32_t S = lanes, blocked = 0;
     std::vector<PlanItem> taken, rest;

@@ -107,6 +107,12 @@ void compile_program(const ProgramP& prog, const SymbolTable& names,
 int resolve_qubits(const ProgramP& prog,
                    std::unordered_map<std::string, int>* index);
 
+// A paired circuit of tfq_inner_product must use exactly the reference
+// circuit's qubits (program_resolution.cc:188-310); `index` is the reference
+// circuit's map.  Throws with the reference's messages.
+void check_paired_qubits(const ProgramP& other,
+                         const std::unordered_map<std::string, int>& index);
+
 // Structure class (GateClass) of a gate template.
 uint8_t classify_gate(const GateTemplate& g);
 

@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "gate_math.cuh"
 #include "sim_device.cuh"
 
@@ -154,6 +156,64 @@ __global__ void sampled_expectation_kernel(BatchDevice b, RunArgs a,
     ev += static_cast<float>(parity_total) * term.coef / static_cast<float>(N);
   }
   if (lane == 0) *out = ev;
+}
+
+// ---- inner products -----------------------------------------------------------
+
+constexpr int kInnerChunkBits = 14;  // amplitudes per CTA of the inner product
+
+// CTA t: pair p = t / nchunks (reference row i = p / others, paired row
+// main_rows + p), chunk c = t % nchunks of 2^kInnerChunkBits amplitudes;
+// adds sum_x conj(psi_i[x]) phi_p[x] over its chunk to acc[2p], acc[2p + 1]
+// (ss.InnerProduct, tfq_inner_product.cc:180-199).
+__global__ void __launch_bounds__(256)
+inner_product_kernel(BatchDevice b, const float2* states, int64_t stride, int main_rows,
+                     int others, int nchunks, double* acc) {
+  __shared__ double part[2][8];
+  const int64_t t = blockIdx.x;
+  const int64_t p = t / nchunks;
+  const int c = int(t % nchunks);
+  const int i = int(p / others);
+  const int n = b.rows[i].n;
+  const int64_t N = int64_t(1) << n;
+  const int64_t x0 = int64_t(c) << kInnerChunkBits;
+  if (x0 >= N) return;  // uniform per CTA
+  const int64_t x1 = min(N, x0 + (int64_t(1) << kInnerChunkBits));
+  const float2* psi = states + int64_t(i) * stride;
+  const float2* phi = states + (int64_t(main_rows) + p) * stride;
+  float re = 0.f, im = 0.f;
+  for (int64_t x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+    const float2 a = psi[x], v = phi[x];
+    re = fmaf(a.x, v.x, fmaf(a.y, v.y, re));
+    im = fmaf(a.x, v.y, fmaf(-a.y, v.x, im));
+  }
+  re = warp_sum(re);
+  im = warp_sum(im);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    part[0][w] = re;
+    part[1][w] = im;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sr = 0.0, si = 0.0;
+    for (int k = 0; k < int(blockDim.x >> 5); ++k) {
+      sr += part[0][k];
+      si += part[1][k];
+    }
+    atomicAdd(acc + 2 * p, sr);
+    atomicAdd(acc + 2 * p + 1, si);
+  }
+}
+
+__global__ void inner_product_finalize_kernel(BatchDevice b, int main_rows, int others,
+                                              const double* acc, float2* out) {
+  const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= int64_t(main_rows) * others) return;
+  const DevProgram pr = b.programs[b.rows[p / others].program];
+  const bool empty = pr.n == 0 || pr.fwd_pass_begin == pr.fwd_pass_end;
+  out[p] = empty ? make_float2(1.f, 0.f)
+                 : make_float2(float(acc[2 * p]), float(acc[2 * p + 1]));
 }
 
 // ---- wide rows --------------------------------------------------------------
@@ -365,6 +425,21 @@ cudaError_t launch_sampled_expectation(const BatchDevice& b, const RunArgs& a,
   const int threads = 256;
   const int64_t blocks = (warps * 32 + threads - 1) / threads;
   sampled_expectation_kernel<<<unsigned(blocks), threads, 0, s>>>(b, a, num_samples);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inner_products(const BatchDevice& b, const float2* states,
+                                  int64_t stride, int main_rows, int others,
+                                  double* acc, float2* out, cudaStream_t s) {
+  const int64_t pairs = int64_t(main_rows) * others;
+  if (pairs == 0) return cudaSuccess;
+  const int nchunks = int(std::max<int64_t>(1, stride >> kInnerChunkBits));
+  inner_product_kernel<<<unsigned(pairs * nchunks), 256, 0, s>>>(b, states, stride, main_rows,
+                                                                  others, nchunks, acc);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  inner_product_finalize_kernel<<<unsigned((pairs + 255) / 256), 256, 0, s>>>(
+      b, main_rows, others, acc, out);
   return cudaGetLastError();
 }
 

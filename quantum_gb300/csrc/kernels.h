@@ -80,6 +80,14 @@ cudaError_t launch_simulate(int mode, const BatchDevice& b, const RunArgs& a,
                             cudaStream_t s);
 cudaError_t launch_noisy_finalize(const BatchDevice& b, const RunArgs& a,
                                   cudaStream_t s);
+// tfq_inner_product over the rows of a TFQG_KIND_INNER batch: states holds
+// every row's final state (row stride `stride` amplitudes); out[i, j] =
+// <psi_i | phi_ij> in complex64 from fp64 sums (`acc`: 2 doubles per pair,
+// zeroed by the caller); 1 for an empty reference program.
+cudaError_t launch_inner_products(const BatchDevice& b, const float2* states,
+                                  int64_t stride, int main_rows, int others,
+                                  double* acc, float2* out, cudaStream_t s);
+
 // Sampled expectation from the term values a.term_vals: per (row, op), each
 // term's N = num_samples[row, op] measurement parities drawn as Bernoulli
 // trials; writes a.out_f.

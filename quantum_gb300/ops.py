@@ -21,7 +21,7 @@ import numpy as np
 from . import _native
 from ._native import InvalidArgumentError  # noqa: F401  (re-export)
 
-KIND_FORWARD, KIND_ADJOINT, KIND_NOISY = 0, 1, 2
+KIND_FORWARD, KIND_ADJOINT, KIND_NOISY, KIND_INNER = 0, 1, 2, 3
 GRAD_REFERENCE_FD, GRAD_EXACT = 0, 1
 
 try:  # torch is optional for the numpy path
@@ -270,6 +270,49 @@ class Batch:
         return out
 
 
+class InnerProductBatch(Batch):
+    """A compiled tfq_inner_product batch: reference programs (with symbols)
+    and their paired other_programs [batch, n_others] (no symbols), parsed and
+    resolved once (math_ops/tfq_inner_product.cc:48-166)."""
+
+    def __init__(self, programs, symbol_names, other_programs):
+        progs, pshape = _strings(programs, "programs", 1)
+        names, _ = _strings(symbol_names, "symbol_names", 1)
+        others, oshape = _strings(other_programs, "other_programs", 2)
+        if oshape[0] != pshape[0]:
+            raise InvalidArgumentError(
+                "programs and other_programs batch dimension do not match. Foud: "
+                f"{pshape[0]} and {oshape[0]}")
+        self.batch_size = pshape[0]
+        self.num_symbols = len(names)
+        self.num_ops = 0
+        self.num_others = oshape[1]
+        self.kind = KIND_INNER
+        lib = _native.lib()
+        pp, pl, k1 = _native.string_array(progs)
+        npp, npl, k2 = _native.string_array(names)
+        opp, opl, k3 = _native.string_array(others)
+        h = ctypes.c_void_p()
+        _native.check(lib.tfqg_batch_create_inner_product(
+            pp, pl, self.batch_size, npp, npl, self.num_symbols, opp, opl,
+            self.num_others, ctypes.byref(h)))
+        self._h = h
+        mq = ctypes.c_int32()
+        _native.check(lib.tfqg_batch_max_num_qubits(h, ctypes.byref(mq)))
+        self.max_num_qubits = mq.value
+        del k1, k2, k3
+
+    def inner_product(self, symbol_values):
+        """complex64 [batch, n_others]: <psi_i(values_i) | phi_ij>."""
+        v = self._host_or_cuda(_values(symbol_values))
+        self._check_values(v)
+        out = self._out(v, (self.batch_size, self.num_others), np.complex64,
+                        getattr(torch, "complex64", None))
+        _native.check(_native.lib().tfqg_batch_inner_product(
+            self._h, _ptr(v), _ptr(out), self._device_flag(v), _stream(v)))
+        return self._wrap(symbol_values, out)
+
+
 # ---------------------------------------------------------------------------
 # the reference's functional API
 # ---------------------------------------------------------------------------
@@ -327,6 +370,15 @@ def tfq_simulate_sampled_expectation(programs, symbol_names, symbol_values,
     b = Batch(programs, symbol_names, pauli_sums, KIND_FORWARD)
     try:
         return b.sampled_expectation(symbol_values, num_samples, seed)
+    finally:
+        b.close()
+
+
+def tfq_inner_product(programs, symbol_names, symbol_values, other_programs):
+    """math_ops/inner_product_op.py:72-130 (tfq.math.inner_product)."""
+    b = InnerProductBatch(programs, symbol_names, other_programs)
+    try:
+        return b.inner_product(symbol_values)
     finally:
         b.close()
 

@@ -131,6 +131,19 @@ GOLDENS = {
         "cases": [[2, 3], [1, 5, 8]],
         "literals": ["'all_n_qubits': [2, 3]", "'all_n_qubits': [1, 5, 8]"],
     },
+    # math_ops/inner_product_op.py:72-130 (docstring example): reference
+    # circuits (H**alpha on each qubit) and (X(q0)**alpha, Y(q1)**beta) with
+    # values [[0, 1], [2, 3]], paired with X on each qubit, Y**0.125 on each
+    # and X**0.5 on each.
+    "inner_product": {
+        "source": "tensorflow_quantum/core/ops/math_ops/inner_product_op.py:72-130",
+        "tolerance": 1e-5,
+        "values": [[0, 1], [2, 3]],
+        "out": [[[0.0, 0.0], [8.8871640e-01, 0.3681184], [0.0, 0.5]],
+                [[0.0, 0.0], [7.3223300e-02, -0.17677669], [0.0, -0.5]]],
+        "literals": ["8.8871640e-01+0.3681184j", "7.3223300e-02-0.17677669j",
+                     "np.arange(4).reshape(2, 2)"],
+    },
 }
 
 FILES = {
@@ -139,6 +152,7 @@ FILES = {
     "adj_grad": "tensorflow_quantum/core/ops/tfq_adj_grad_op_test.py",
     "gradient_gates": "tensorflow_quantum/core/src/adj_util_test.cc",
     "padding": "tensorflow_quantum/core/ops/tfq_simulate_ops_test.py",
+    "inner_product": "tensorflow_quantum/core/ops/math_ops/inner_product_op.py",
 }
 
 

@@ -129,3 +129,32 @@ def test_sampled_expectation_input_checks():
     with pytest.raises(_native.InvalidArgumentError,
                        match="Each element of num_samples must be greater than 0"):
         b.sampled_expectation(np.zeros((1, 0), np.float32), [[0]])
+
+
+def test_inner_product_input_checks():
+    """tfq_inner_product's resolution and parse errors (program_resolution.cc:
+    188-310, math_ops/tfq_inner_product.cc:48-166), raised at batch creation
+    without a GPU."""
+    q = S.GridQubit.rect(1, 3)
+    ref = _prog([S.HPow(q[0]), S.HPow(q[1])])
+    same = _prog([S.X(q[0]), S.X(q[1])])
+    extra = _prog([S.X(q[0]), S.X(q[2])])
+    fewer = _prog([S.X(q[0])])
+    sym = _prog([S.XPow(q[0], S.Symbol("a")), S.X(q[1])])
+    ops.InnerProductBatch([ref], [], [[same]])  # fine
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="A paired circuit contains qubits not found in reference circuit."):
+        ops.InnerProductBatch([ref], [], [[extra]])
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="A reference circuit contains qubits not found in paired circuit."):
+        ops.InnerProductBatch([ref], [], [[fewer]])
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="Found symbols in other_programs.No symbols are allowed"):
+        ops.InnerProductBatch([ref], ["a"], [[sym]])
+    with pytest.raises(_native.InvalidArgumentError, match="other_programs must be rank 2"):
+        ops.InnerProductBatch([ref], [], [same])
+    with pytest.raises(_native.InvalidArgumentError,
+                       match="programs and other_programs batch dimension do not match"):
+        ops.InnerProductBatch([ref, ref], [], [[same]])
+    # an empty reference program skips its paired circuits' checks
+    ops.InnerProductBatch([S.serialize_circuit(S.Circuit())], [], [[extra]])

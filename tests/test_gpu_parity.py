@@ -282,3 +282,52 @@ def test_text_format_inputs_give_identical_results():
     tps = [[textfmt.to_text(x, "PauliSum").encode() for x in row] for row in psums]
     np.testing.assert_array_equal(ops.tfq_simulate_expectation(tp, names, values, tps),
                                   ops.tfq_simulate_expectation(programs, names, values, psums))
+
+
+@pytest.mark.parametrize("n", [2, 15])
+def test_identity_only_program_is_not_empty(n):
+    """A program of identity gates has a non-empty fused circuit in the
+    reference, so its expectation is taken on |0...0> (not the -2 of an
+    empty program), resident (2 qubits) or streamed (15 qubits)."""
+    q = S.GridQubit.rect(1, n)
+    prog = S.serialize_circuit(S.Circuit([[S.I(x) for x in q]]))
+    ps = S.serialize_paulisum([(0.5, [(q[0], "Z")]), (0.25, [])])
+    got = ops.tfq_simulate_expectation([prog], [], np.zeros((1, 0)), [[ps]])
+    np.testing.assert_allclose(got, [[0.75]], atol=1e-6)
+    st = ops.tfq_simulate_state([prog], [], np.zeros((1, 0)))
+    assert st[0, 0] == 1 and np.all(st[0, 1:] == 0)
+
+
+def test_inner_product_docstring_example():
+    """math_ops/inner_product_op.py:72-130 (the reference's documented output)."""
+    import json, os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                    "reference_goldens.json")))["inner_product"]
+    q = S.GridQubit.rect(1, 2)
+    a, b = S.Symbol("alpha"), S.Symbol("beta")
+    ref = [S.serialize_circuit(S.Circuit([[S.HPow(x, a) for x in q]])),
+           S.serialize_circuit(S.Circuit([[S.XPow(q[0], a), S.YPow(q[1], b)]]))]
+    oth = [S.serialize_circuit(S.Circuit([[S.X(x) for x in q]])),
+           S.serialize_circuit(S.Circuit([[S.YPow(x, 0.125) for x in q]])),
+           S.serialize_circuit(S.Circuit([[S.XPow(x, 0.5) for x in q]]))]
+    got = ops.tfq_inner_product(ref, ["alpha", "beta"], np.array(g["values"], np.float32),
+                                [oth, oth])
+    want = np.array([[complex(*z) for z in r] for r in g["out"]])
+    np.testing.assert_allclose(got, want, atol=g["tolerance"])
+
+
+@pytest.mark.parametrize("n,others", [(3, 2), (9, 3), (14, 1), (17, 2)])
+def test_inner_product_matches_oracle(n, others):
+    rng = np.random.default_rng(900 + n)
+    qs = S.GridQubit.rect(1, n)
+    names = ["a", "b"]
+    refs, oth = [], []
+    for _ in range(2):
+        refs.append(S.serialize_circuit(random_circuit(qs, 5, rng, names, p_control=0.3)))
+        oth.append([S.serialize_circuit(random_circuit(qs, 4, rng, (), p_control=0.3))
+                    for _ in range(others)])
+    values = rng.uniform(-2, 2, size=(2, 2)).astype(np.float32)
+    got = ops.tfq_inner_product(refs, names, values, oth)
+    want = O.inner_product(refs, names, values, oth)
+    assert got.dtype == np.complex64 and got.shape == want.shape
+    np.testing.assert_allclose(got, want, atol=1e-5, rtol=0)

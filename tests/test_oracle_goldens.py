@@ -126,3 +126,19 @@ def test_density_matrix_matches_statevector_without_noise():
     a = O.simulate_expectation([prog], ["a"], v, ps)
     b = O.noisy_expectation_exact([prog], ["a"], v, ps)
     np.testing.assert_allclose(a, b, atol=1e-10)
+
+
+def test_oracle_inner_product_docstring_example():
+    """math_ops/inner_product_op.py:72-130: the documented example's output."""
+    from quantum_gb300 import serialize as S
+    g = G["inner_product"]
+    q = S.GridQubit.rect(1, 2)
+    a, b = S.Symbol("alpha"), S.Symbol("beta")
+    ref = [S.serialize_circuit(S.Circuit([[S.HPow(x, a) for x in q]])),
+           S.serialize_circuit(S.Circuit([[S.XPow(q[0], a), S.YPow(q[1], b)]]))]
+    oth = [S.serialize_circuit(S.Circuit([[S.X(x) for x in q]])),
+           S.serialize_circuit(S.Circuit([[S.YPow(x, 0.125) for x in q]])),
+           S.serialize_circuit(S.Circuit([[S.XPow(x, 0.5) for x in q]]))]
+    got = O.inner_product(ref, ["alpha", "beta"], np.array(g["values"], np.float32), [oth, oth])
+    want = np.array([[complex(*z) for z in r] for r in g["out"]])
+    np.testing.assert_allclose(got, want, atol=g["tolerance"])
