@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the one-shot C-ABI leg")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="circuits per GPU (default 256; smaller only for profiling)")
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c2 (default): the headline expectation + adjoint line; "
+                         "c1, c3, c4, c5: the other benchmark configurations, "
+                         "one JSON line each (device time only)")
     return ap.parse_args()
 
 
@@ -184,11 +188,94 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+CONFIGS = {
+    "c1": "expectation: 32 circuits x 12 qubits, 20 layers of Rx Ry Rz (720 symbols) + CZ "
+          "brick-wall; sum Z, sum ZZ, sum X and 10 random Pauli strings",
+    "c3": "expectation (sum Z) + 1000 samples: 4096 circuits, n ~ U{4..20}, depth ~ U{5..40} "
+          "random-axis rotations + CZ / ISWAP^t pairs",
+    "c4": "expectation (sum Z): one 30-qubit circuit on a 5x6 grid, depth 24, sqrt(X)/sqrt(Y)/"
+          "sqrt(W) + fSim on 4 coupler patterns (8 GiB state, wide-row path)",
+    "c5": "noisy expectation (sum Z): 64 circuits x 14 qubits, depth 15 Ry Rz + CZ brick-wall, "
+          "depolarizing(0.01) after every gate, 2000 trajectories per circuit",
+}
+
+
+def run_config(args):
+    """One JSON line for configuration c1 / c3 / c4 / c5: device time per
+    step (CUDA events, inputs resident, L2 flushed between steps)."""
+    import torch
+    from quantum_gb300 import ops, workloads
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    wl = args.workload
+    if wl == "c1":
+        w = workloads.expectation_layers(32, 12, 20, seed=1)
+        units, unit = 32, "circuits/s"
+    elif wl == "c3":
+        w = workloads.uneven_batch(4096, 4, 20, 5, 40, seed=1)
+        units, unit = 4096, "circuits/s"
+    elif wl == "c4":
+        w = workloads.grid_fsim(5, 6, 24, seed=1)
+        units, unit = 1, "circuits/s"
+    else:
+        w = workloads.noisy_brickwall(64, 14, 15, 0.01, seed=1)
+        units, unit = 64 * 2000, "trajectories/s"
+    kind = ops.KIND_NOISY if wl == "c5" else ops.KIND_FORWARD
+    t0 = time.perf_counter()
+    batch = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
+    parse_s = time.perf_counter() - t0
+    vals = torch.tensor(w["symbol_values"], device=dev)
+    reps = np.full((len(w["programs"]), 1), 2000, np.int32)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(k):
+        if wl == "c5":
+            return batch.noisy_expectation(vals, reps, seed=k + 1)
+        e = batch.expectation(vals)
+        if wl == "c3":
+            batch.samples(vals, 1000, seed=k + 1)
+        return e
+
+    for k in range(max(args.warmup, 1)):
+        step(k)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = ClockSampler(0)
+    clocks.start()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        ev[k][0].record()
+        out = step(k)
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    line = {"metric": f"{wl} throughput", "value": units / (ms / 1e3), "unit": unit,
+            "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "c64 (f32 state, f64 reductions)",
+            "data": "synthetic (seeded)", "config": {"workload": wl, "what": CONFIGS[wl]},
+            "host_parse_plan_s": parse_s, "clocks": clk,
+            "specialized": sorted(__import__("quantum_gb300")._native.batch_specialization(
+                batch._h)[1])}
+    if wl == "c1":
+        from oracle import tfq_oracle as O
+        rows = [0, 1]
+        want = O.simulate_expectation([w["programs"][i] for i in rows], w["symbol_names"],
+                                      w["symbol_values"][rows],
+                                      [w["pauli_sums"][i] for i in rows])
+        line["accuracy"] = {"max_abs": float(np.abs(out.cpu().numpy()[rows] - want).max()),
+                            "rows": len(rows)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload != "c2":
+        return run_config(args)
 
     import torch
     torch.cuda.set_device(local)
