@@ -136,7 +136,7 @@ int tfqg_batch_create_inner_product(const char* const* programs,
                                     const int64_t* symbol_name_lens, int64_t num_symbols,
                                     const char* const* other_programs,
                                     const int64_t* other_program_lens, int64_t num_others,
-                                    tfqg_batch** out);
+                                    int with_grads, tfqg_batch** out);
 
 /* <psi_i | phi_ij> as complex64 [batch, num_others] (interleaved re, im),
  * fp64 sums; 1 for an empty reference program.  Replaces
@@ -145,6 +145,16 @@ int tfqg_batch_create_inner_product(const char* const* programs,
  * programs. */
 int tfqg_batch_inner_product(tfqg_batch* b, const float* symbol_values,
                              void* inner_products, int device_buffers, void* stream);
+
+/* Gradient of the inner products weighted by downstream_grads float
+ * [batch, num_others]: complex64 [batch, num_symbols], grads[i, p] = sum over
+ * the gates using symbol p of <dU psi | chi_i>, chi_i = sum_j g_ij |phi_ij>
+ * (reference finite-difference gradient gates).  Replaces
+ * TfqInnerProductGradOp (math_ops/tfq_inner_product_grad.cc:46-452).  The
+ * batch must be created with with_grads = 1. */
+int tfqg_batch_inner_product_grad(tfqg_batch* b, const float* symbol_values,
+                                  const float* downstream_grads, void* grads,
+                                  int device_buffers, void* stream);
 
 /* Same result as tfqg_batch_expectation, for callers that must not let the
  * library allocate device memory (for example a host framework whose caching

@@ -17,7 +17,8 @@ complex128 numpy, the algorithm of the reference ops:
   AccumulateOperators util_qsim.h:362-414, FD gradient gates
   tensorflow_quantum/core/src/adj_util.cc:32,175-302
 * inner product ........... tensorflow_quantum/core/ops/math_ops/tfq_inner_product.cc,
-  paired resolution program_resolution.cc:188-310
+  paired resolution program_resolution.cc:188-310, gradient
+  math_ops/tfq_inner_product_grad.cc:216-318
 * noisy expectation ....... tensorflow_quantum/core/ops/noise/tfq_noisy_expectation.cc
   (restated as an exact density-matrix evolution: the trajectory average
   converges to it)
@@ -710,6 +711,48 @@ def inner_product(programs, symbol_names, symbol_values, other_programs):
                                       "are allowed in these circuits.") from None
             phi = simulate(og, n).reshape(-1) if og else np.eye(1, 2 ** n, dtype=np.complex128)[0]
             out[i, j] = np.vdot(psi, phi)
+    return out
+
+
+def inner_product_grad(programs, symbol_names, symbol_values, other_programs,
+                       downstream_grads):
+    """TfqInnerProductGrad (math_ops/tfq_inner_product_grad.cc:216-318):
+    out[i, p] = sum over the gates using symbol p of <dU psi_before | chi>,
+    chi = sum_j g_ij |phi_ij> uncomputed alongside psi (FD gradient gates,
+    control projector as in the adjoint op); complex, no factor 2."""
+    others = np.asarray(other_programs, dtype=object)
+    ref = inner_product(programs, symbol_names, symbol_values, other_programs)  # checks
+    del ref
+    parsed, _ = _parse_all(programs, symbol_names, symbol_values)
+    cols = _name_cols(symbol_names)
+    dg = np.asarray(downstream_grads, dtype=np.float32)
+    out = np.zeros((len(parsed), len(symbol_names)), dtype=np.complex128)
+    for i, (n, index, items) in enumerate(parsed):
+        gates = [g for _, g in items]
+        if not gates:
+            continue
+        psi = simulate(gates, n)
+        chi = np.zeros_like(psi)
+        for j in range(others.shape[1]):
+            om = decode_program(others[i, j])
+            og = [build_gate(op, index, {}) for mom in om for op in mom]
+            phi = simulate(og, n) if og else np.eye(1, 2 ** n, dtype=np.complex128)[0].reshape(psi.shape)
+            chi = chi + float(dg[i, j]) * phi
+        for g in reversed(gates):
+            mdag = np.conj(g.matrix.T)
+            psi = apply_matrix(psi, n, mdag, g.qubits, g.controls, g.cvals)
+            for sym, dm in g.grads:
+                phi = psi
+                if g.controls:
+                    mask = np.zeros([2] * n, dtype=bool)
+                    sl = [slice(None)] * n
+                    for c, v in zip(g.controls, g.cvals):
+                        sl[c] = int(v)
+                    mask[tuple(sl)] = True
+                    phi = np.where(mask, psi, 0)
+                phi = apply_matrix(phi, n, dm, g.qubits)
+                out[i, cols[sym]] += np.vdot(phi, chi)
+            chi = apply_matrix(chi, n, mdag, g.qubits, g.controls, g.cvals)
     return out
 
 

@@ -50,6 +50,7 @@ EXPORTED = (
     "tfqg_simulate_expectation", "tfqg_adj_grad", "tfqg_noisy_expectation",
     "tfqg_batch_sampled_expectation", "tfqg_simulate_sampled_expectation",
     "tfqg_batch_create_inner_product", "tfqg_batch_inner_product", "tfqg_inner_product",
+    "tfqg_batch_inner_product_grad",
 )
 
 
@@ -81,9 +82,11 @@ def _declare(lib):
         c_void_p]
     lib.tfqg_batch_create_inner_product.argtypes = [
         c_char_pp, c_int64_p, ctypes.c_int64, c_char_pp, c_int64_p, ctypes.c_int64,
-        c_char_pp, c_int64_p, ctypes.c_int64, ctypes.POINTER(c_void_p)]
+        c_char_pp, c_int64_p, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(c_void_p)]
     lib.tfqg_batch_inner_product.argtypes = [c_void_p, c_void_p, c_void_p, ctypes.c_int,
                                              c_void_p]
+    lib.tfqg_batch_inner_product_grad.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p,
+                                                  ctypes.c_int, c_void_p]
     lib.tfqg_batch_sampled_expectation.argtypes = [
         c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p, ctypes.c_int,
         c_void_p]
@@ -93,7 +96,7 @@ def _declare(lib):
                  "tfqg_batch_noisy_expectation", "tfqg_batch_expectation_noalloc",
                  "tfqg_batch_sampled_expectation", "tfqg_simulate_sampled_expectation",
                  "tfqg_batch_create_inner_product", "tfqg_batch_inner_product",
-                 "tfqg_inner_product",
+                 "tfqg_inner_product", "tfqg_batch_inner_product_grad",
                  "tfqg_simulate_expectation",
                  "tfqg_adj_grad", "tfqg_noisy_expectation"):
         getattr(lib, name).restype = ctypes.c_int

@@ -59,6 +59,8 @@ struct tfqg_batch {
   int64_t B = 0, P = 0, n_ops = 0;
   int64_t value_rows = 0;          // rows that take symbol values
   int64_t inner_rows = 0, inner_others = 0;  // TFQG_KIND_INNER shape
+  bool inner_grads = false;        // reference programs planned for the adjoint
+  tfqg::DevBuf inner_tmp;
   int max_n = 0;
   int max_resident_n = -1;   // largest resident row (-1: none)
   bool any_streamed = false;

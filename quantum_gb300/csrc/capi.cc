@@ -62,7 +62,8 @@ void build_batch(tfqg_batch* b, const char* const* programs,
                  int64_t num_symbols, const char* const* pauli_sums,
                  const int64_t* psum_lens, int64_t num_ops, int kind,
                  const char* const* others = nullptr,
-                 const int64_t* other_lens = nullptr, int64_t num_others = 0) {
+                 const int64_t* other_lens = nullptr, int64_t num_others = 0,
+                 bool inner_grads = false) {
   if (batch < 0 || num_symbols < 0 || num_ops < 0 || num_others < 0)
     throw Error(kInvalidArgument, "negative dimension");
   if (num_ops > 65535)
@@ -79,9 +80,12 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   b->B = batch;
   b->P = num_symbols;
   b->n_ops = num_ops;
-  const JobKind job = kind == TFQG_KIND_ADJOINT ? kJobAdjoint
-                      : kind == TFQG_KIND_NOISY ? kJobNoisy
-                                                : kJobForward;
+  // reference programs of an inner-product batch plan the adjoint sweep
+  // when the batch will compute gradients; paired programs only run forward
+  const JobKind job = (kind == TFQG_KIND_ADJOINT || (inner && inner_grads)) ? kJobAdjoint
+                      : kind == TFQG_KIND_NOISY                           ? kJobNoisy
+                                                                          : kJobForward;
+  b->inner_grads = inner && inner_grads;
 
   // 1. parse programs (ParsePrograms, parse_context.cc:174-206), deduplicated
   std::unordered_map<std::string, int> prog_ids;
@@ -187,12 +191,12 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   for (size_t pid = 0; pid < parsed.size() && inner; ++pid) {
     if (pair_of[pid] < 0) continue;
     try {
-      compile_program(parsed[pid], no_symbols, job, &compiled[pid], &index[pid]);
+      compile_program(parsed[pid], no_symbols, kJobForward, &compiled[pid], &index[pid]);
     } catch (const Error&) {
       throw Error(kInvalidArgument,
                   "Found symbols in other_programs.No symbols are allowed in these circuits.");
     }
-    plan_program(&compiled[pid], job);
+    plan_program(&compiled[pid], kJobForward);
   }
 
   // 5. pack programs
@@ -304,6 +308,9 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   };
   std::stable_sort(b->order.begin(), b->order.end(),
                    [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
+  if (inner)  // reference rows first: the gradient's adjoint runs only them
+    std::stable_partition(b->order.begin(), b->order.end(),
+                          [&](int32_t r) { return r < main_rows; });
   // wide rows: in the forward modes the whole grid simulates them one by one
   const int wide_min = std::max(wide_min_qubits(), kStreamTileBits + 2);
   auto is_wide = [&](const DevProgram& p) {
@@ -516,6 +523,8 @@ int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
     bd.order = b->d_order_fwd;
     bd.num_queue = int32_t(b->order_fwd.size());
   }
+  // an inner-product gradient sweeps only the reference rows (first in order)
+  if (b->kind == TFQG_KIND_INNER && mode == kModeAdjoint) bd.num_queue = int32_t(b->inner_rows);
   const bool any_streamed = split ? b->any_streamed_fwd : b->any_streamed;
   const int max_streamed_n = split ? b->max_streamed_n_fwd : b->max_streamed_n;
   int grid = 0;
@@ -874,14 +883,14 @@ int tfqg_batch_create_inner_product(const char* const* programs,
                                     const int64_t* symbol_name_lens, int64_t num_symbols,
                                     const char* const* other_programs,
                                     const int64_t* other_program_lens, int64_t num_others,
-                                    tfqg_batch** out) {
+                                    int with_grads, tfqg_batch** out) {
   return guarded([&]() {
     if (!out) throw Error(kInvalidArgument, "out is NULL");
     *out = nullptr;
     std::unique_ptr<tfqg_batch> b(new tfqg_batch());
     build_batch(b.get(), programs, program_lens, batch, symbol_names, symbol_name_lens,
                 num_symbols, nullptr, nullptr, 0, TFQG_KIND_INNER, other_programs,
-                other_program_lens, num_others);
+                other_program_lens, num_others, with_grads != 0);
     *out = b.release();
     return 0;
   });
@@ -919,6 +928,69 @@ int tfqg_batch_inner_product(tfqg_batch* b, const float* symbol_values,
   });
 }
 
+int tfqg_batch_inner_product_grad(tfqg_batch* b, const float* symbol_values,
+                                  const float* downstream_grads, void* grads,
+                                  int device_buffers, void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    if (b->kind != TFQG_KIND_INNER || !b->inner_grads)
+      throw Error(kInvalidArgument,
+                  "batch was not created for inner-product gradients");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t B = b->inner_rows, M = b->inner_others, P = b->P;
+    const size_t obytes = size_t(B * P) * sizeof(float2);
+    if (B == 0 || P == 0) return 0;
+    float2* dout = static_cast<float2*>(grads);
+    ensure_device(b, s);
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<float2*>(b->out.p);
+    }
+    if (M == 0) {  // no paired circuits: chi = 0
+      TFQG_CUDA(cudaMemsetAsync(dout, 0, obytes, s));
+      finish(b, grads, dout, obytes, device_buffers, s);
+      return 0;
+    }
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, true, TFQG_GRAD_REFERENCE_FD, s, &a);
+    // 1. every row's final state; 2. chi_i = sum_j g_ij phi_ij over the
+    // reference rows' states (the adjoint recomputes psi_i itself)
+    const int64_t stride = int64_t(1) << b->max_n;
+    b->aux.reserve(size_t(b->B * stride) * sizeof(float2), b->device);
+    float2* states = static_cast<float2*>(b->aux.p);
+    a.out_state = states;
+    simulate(b, kModeState, &a, s);
+    const float* dg = downstream_grads;
+    const size_t gbytes = size_t(B * M) * sizeof(float);
+    b->aux2.reserve(gbytes, b->device);
+    if (!device_buffers) {
+      TFQG_CUDA(cudaMemcpyAsync(b->aux2.p, downstream_grads, gbytes,
+                                cudaMemcpyHostToDevice, s));
+      dg = static_cast<const float*>(b->aux2.p);
+    }
+    TFQG_CUDA(launch_paired_sum(b->bd, states, stride, int(B), int(M), dg, s));
+    // 3. Re<chi|dU psi> and Im<chi|dU psi> = Re<i chi|dU psi> by two adjoint
+    // sweeps seeded with chi and i chi; <dU psi|chi> = (Re, -Im)
+    b->inner_tmp.reserve(size_t(2 * B * P) * sizeof(float), b->device);
+    float* re = static_cast<float*>(b->inner_tmp.p);
+    float* im = re + B * P;
+    TFQG_CUDA(cudaMemsetAsync(re, 0, size_t(2 * B * P) * sizeof(float), s));
+    a.lambda_init = states;
+    a.lambda_stride = stride;
+    a.grad_scale = 1.f;
+    a.lambda_rot = 0;
+    a.out_f = re;
+    simulate(b, kModeAdjoint, &a, s);
+    a.lambda_rot = 1;
+    a.out_f = im;
+    simulate(b, kModeAdjoint, &a, s);
+    TFQG_CUDA(launch_conj_combine(re, im, dout, B * P, s));
+    finish(b, grads, dout, obytes, device_buffers, s);
+    return 0;
+  });
+}
+
 int tfqg_inner_product(const char* const* programs, const int64_t* program_lens,
                        int64_t batch, const char* const* symbol_names,
                        const int64_t* symbol_name_lens, int64_t num_symbols,
@@ -928,7 +1000,7 @@ int tfqg_inner_product(const char* const* programs, const int64_t* program_lens,
   tfqg_batch* b = nullptr;
   int rc = tfqg_batch_create_inner_product(programs, program_lens, batch, symbol_names,
                                            symbol_name_lens, num_symbols, other_programs,
-                                           other_program_lens, num_others, &b);
+                                           other_program_lens, num_others, 0, &b);
   if (rc) return rc;
   rc = tfqg_batch_inner_product(b, symbol_values, inner_products, 0, nullptr);
   tfqg_batch_destroy(b);

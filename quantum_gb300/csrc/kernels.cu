@@ -216,6 +216,29 @@ __global__ void inner_product_finalize_kernel(BatchDevice b, int main_rows, int 
                  : make_float2(float(acc[2 * p]), float(acc[2 * p + 1]));
 }
 
+__global__ void paired_sum_kernel(BatchDevice b, float2* states, int64_t stride,
+                                  int main_rows, int others, const float* grads, int row0) {
+  const int i = row0 + int(blockIdx.y);
+  const int64_t N = int64_t(1) << b.rows[i].n;
+  float2* chi = states + int64_t(i) * stride;
+  for (int64_t x = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < N;
+       x += int64_t(gridDim.x) * blockDim.x) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int j = 0; j < others; ++j) {
+      const float g = grads[int64_t(i) * others + j];
+      const float2 v = states[(int64_t(main_rows) + int64_t(i) * others + j) * stride + x];
+      acc.x = fmaf(g, v.x, acc.x);
+      acc.y = fmaf(g, v.y, acc.y);
+    }
+    chi[x] = acc;
+  }
+}
+
+__global__ void conj_combine_kernel(const float* re, const float* im, float2* out, int64_t n) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = make_float2(re[k], -im[k]);
+}
+
 // ---- wide rows --------------------------------------------------------------
 
 __global__ void __launch_bounds__(kWideThreads, 2)
@@ -440,6 +463,28 @@ cudaError_t launch_inner_products(const BatchDevice& b, const float2* states,
   if (e != cudaSuccess) return e;
   inner_product_finalize_kernel<<<unsigned((pairs + 255) / 256), 256, 0, s>>>(
       b, main_rows, others, acc, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_paired_sum(const BatchDevice& b, float2* states, int64_t stride,
+                              int main_rows, int others, const float* grads,
+                              cudaStream_t s) {
+  if (main_rows == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((stride + 255) / 256, 1024);
+  for (int row0 = 0; row0 < main_rows; row0 += 65535) {  // grid.y limit
+    const int rows = std::min(65535, main_rows - row0);
+    paired_sum_kernel<<<dim3(unsigned(blocks), unsigned(rows)), 256, 0, s>>>(
+        b, states, stride, main_rows, others, grads, row0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_conj_combine(const float* re, const float* im, float2* out, int64_t n,
+                                cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  conj_combine_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(re, im, out, n);
   return cudaGetLastError();
 }
 

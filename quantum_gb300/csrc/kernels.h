@@ -54,6 +54,13 @@ struct RunArgs {
   uint64_t seed = 0;
   int grad_rule = 0;                 // 0: reference finite difference, 1: exact
   int* error_flag = nullptr;         // device word; nonzero = kernel-side error
+  // adjoint: lambda seeded from a buffer ([rows, lambda_stride] amplitudes,
+  // times i^lambda_rot) instead of from the observables, and the scale of
+  // the gradient output (2 for the expectation gradient)
+  const float2* lambda_init = nullptr;
+  int64_t lambda_stride = 0;
+  int lambda_rot = 0;
+  float grad_scale = 2.f;
   double* term_vals = nullptr;       // optional [rows, term_stride]: <psi|P_t|psi>
   int64_t term_stride = 0;           // per term of the row (no coefficient)
 };
@@ -87,6 +94,17 @@ cudaError_t launch_noisy_finalize(const BatchDevice& b, const RunArgs& a,
 cudaError_t launch_inner_products(const BatchDevice& b, const float2* states,
                                   int64_t stride, int main_rows, int others,
                                   double* acc, float2* out, cudaStream_t s);
+
+// chi_i = sum_j g_ij phi_ij for the reference rows of a TFQG_KIND_INNER batch
+// (AccumulateFusedCircuits, tfq_inner_product_grad.cc:254-258), written over
+// the reference rows' states (rows 0..main_rows-1 of `states`).
+cudaError_t launch_paired_sum(const BatchDevice& b, float2* states, int64_t stride,
+                              int main_rows, int others, const float* grads,
+                              cudaStream_t s);
+// out[k] = (re[k], -im[k]) as complex64: <dU psi | chi> from the adjoint's
+// Re<lambda|dU psi> runs with lambda = chi and lambda = i chi.
+cudaError_t launch_conj_combine(const float* re, const float* im, float2* out, int64_t n,
+                                cudaStream_t s);
 
 // Sampled expectation from the term values a.term_vals: per (row, op), each
 // term's N = num_samples[row, op] measurement parities drawn as Bernoulli

@@ -1264,6 +1264,32 @@ __device__ void lambda_passes(const BatchDevice& b, const RunArgs& a,
   }
 }
 
+// lambda seeded from a.lambda_init (times i^lambda_rot) for row rc.row: into
+// shared memory (resident, padding zeroed) or the row's global slot.
+__device__ void lambda_from_buffer(const RunArgs& a, const Smem& sm, const RowCtx& rc,
+                                   float2* g_lam) {
+  const int n = rc.p.n;
+  const uint32_t N = 1u << n;
+  const float2* src = a.lambda_init + int64_t(rc.row) * a.lambda_stride;
+  const int rot = a.lambda_rot & 3;
+  auto turn = [rot](float2 v) {
+    switch (rot) {
+      case 1: return make_float2(-v.y, v.x);
+      case 2: return make_float2(-v.x, -v.y);
+      case 3: return make_float2(v.y, -v.x);
+      default: return v;
+    }
+  };
+  if (rc.p.resident) {
+    const uint32_t Np = 1u << (n < kRB ? kRB : n);
+    for (uint32_t x = threadIdx.x; x < Np; x += blockDim.x)
+      sm.lam[swz(x)] = x < N ? turn(src[x]) : make_float2(0.f, 0.f);
+  } else {
+    for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) g_lam[x] = turn(src[x]);
+  }
+  __syncthreads();
+}
+
 // Sampler: chunked |psi|^2 prefix sums in double, then per-sample search
 // (StateSpace::Sample semantics: index x with probability |psi_x|^2).
 __device__ void sample_state(const BatchDevice& b, const RunArgs& a,
@@ -1413,7 +1439,8 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     sample_state(b, a, sm, rc, psi, shared);
   } else if (MODE == kModeAdjoint) {
     for (int k = threadIdx.x; k < rc.p.num_grads; k += blockDim.x) sm.grad[k] = 0.0;
-    lambda_passes(b, a, sm, rc, g_psi, g_lam);
+    if (a.lambda_init) lambda_from_buffer(a, sm, rc, g_lam);
+    else lambda_passes(b, a, sm, rc, g_psi, g_lam);
     __syncthreads();
     run_passes<MODE, Exec>(b, a, sm, rc, rc.p.bwd_pass_begin, rc.p.bwd_pass_end,
                      rc.p.resident ? nullptr : g_psi,
@@ -1423,7 +1450,7 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
       float* out = a.out_f + int64_t(row) * b.num_symbols;
       for (int k = 0; k < rc.p.num_grads; ++k) {
         int col = b.grad_cols[rc.p.grad_col_begin + k];
-        out[col] += float(2.0 * sm.grad[k]);
+        out[col] += float(double(a.grad_scale) * sm.grad[k]);
       }
     }
   }

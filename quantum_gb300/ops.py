@@ -275,7 +275,7 @@ class InnerProductBatch(Batch):
     and their paired other_programs [batch, n_others] (no symbols), parsed and
     resolved once (math_ops/tfq_inner_product.cc:48-166)."""
 
-    def __init__(self, programs, symbol_names, other_programs):
+    def __init__(self, programs, symbol_names, other_programs, with_grads=False):
         progs, pshape = _strings(programs, "programs", 1)
         names, _ = _strings(symbol_names, "symbol_names", 1)
         others, oshape = _strings(other_programs, "other_programs", 2)
@@ -295,7 +295,7 @@ class InnerProductBatch(Batch):
         h = ctypes.c_void_p()
         _native.check(lib.tfqg_batch_create_inner_product(
             pp, pl, self.batch_size, npp, npl, self.num_symbols, opp, opl,
-            self.num_others, ctypes.byref(h)))
+            self.num_others, 1 if with_grads else 0, ctypes.byref(h)))
         self._h = h
         mq = ctypes.c_int32()
         _native.check(lib.tfqg_batch_max_num_qubits(h, ctypes.byref(mq)))
@@ -310,6 +310,40 @@ class InnerProductBatch(Batch):
                         getattr(torch, "complex64", None))
         _native.check(_native.lib().tfqg_batch_inner_product(
             self._h, _ptr(v), _ptr(out), self._device_flag(v), _stream(v)))
+        return self._wrap(symbol_values, out)
+
+    def inner_product_grad(self, symbol_values, prev_grad):
+        """TfqInnerProductGrad's output, complex64 [batch, n_symbols]:
+        sum_j prev_grad[i, j] d<psi_i|phi_ij>/d symbol (the batch must be
+        created with with_grads=True); prev_grad [batch, n_others] real."""
+        v = self._host_or_cuda(_values(symbol_values))
+        self._check_values(v)
+        if _is_torch(v):
+            g = prev_grad if _is_torch(prev_grad) else torch.as_tensor(
+                np.asarray(prev_grad))
+            if g.is_complex():
+                g = g.real
+            g = g.detach().to(device=v.device, dtype=torch.float32).contiguous()
+            gshape = tuple(g.shape)
+        else:
+            g = np.asarray(prev_grad.cpu().numpy() if _is_torch(prev_grad) else prev_grad)
+            g = np.ascontiguousarray(np.real(g).astype(np.float32))
+            gshape = g.shape
+        if len(gshape) != 2:
+            raise InvalidArgumentError(
+                f"downstream_grads must be rank 2. Got rank {len(gshape)}.")
+        if gshape[0] != self.batch_size:
+            raise InvalidArgumentError(
+                "Number of gradients and circuits do not match. Got "
+                f"{gshape[0]} gradients and {self.batch_size} circuits.")
+        if gshape[1] != self.num_others:
+            raise InvalidArgumentError(
+                "Number of gradients and other_programs do not match. Got "
+                f"{gshape[1]} gradient entries and {self.num_others} other programs.")
+        out = self._out(v, (self.batch_size, self.num_symbols), np.complex64,
+                        getattr(torch, "complex64", None))
+        _native.check(_native.lib().tfqg_batch_inner_product_grad(
+            self._h, _ptr(v), _ptr(g), _ptr(out), self._device_flag(v), _stream(v)))
         return self._wrap(symbol_values, out)
 
 
@@ -379,6 +413,18 @@ def tfq_inner_product(programs, symbol_names, symbol_values, other_programs):
     b = InnerProductBatch(programs, symbol_names, other_programs)
     try:
         return b.inner_product(symbol_values)
+    finally:
+        b.close()
+
+
+def inner_product_grad(programs, symbol_names, symbol_values, other_programs,
+                       prev_grad):
+    """math_ops/inner_product_op.py:22-69 (_inner_product_grad): the complex
+    conjugate of TfqInnerProductGrad's output, prev_grad cast to float32."""
+    b = InnerProductBatch(programs, symbol_names, other_programs, with_grads=True)
+    try:
+        out = b.inner_product_grad(symbol_values, prev_grad)
+        return out.conj() if _is_torch(out) else np.conj(out)
     finally:
         b.close()
 

@@ -331,3 +331,31 @@ def test_inner_product_matches_oracle(n, others):
     want = O.inner_product(refs, names, values, oth)
     assert got.dtype == np.complex64 and got.shape == want.shape
     np.testing.assert_allclose(got, want, atol=1e-5, rtol=0)
+
+
+@pytest.mark.parametrize("n,others", [(3, 2), (8, 3), (13, 1), (15, 2)])
+def test_inner_product_grad_matches_oracle(n, others):
+    """TfqInnerProductGrad (math_ops/tfq_inner_product_grad.cc): complex
+    sum_j g_ij <dU psi_i | phi_ij> per symbol with the reference's FD
+    gradient gates; resident (3, 8, 13 qubits) and streamed (15)."""
+    rng = np.random.default_rng(950 + n)
+    qs = S.GridQubit.rect(1, n)
+    names = ["a", "b", "c"]
+    refs, oth = [], []
+    for _ in range(2):
+        refs.append(S.serialize_circuit(random_circuit(qs, 4, rng, names, p_control=0.3)))
+        oth.append([S.serialize_circuit(random_circuit(qs, 3, rng, (), p_control=0.3))
+                    for _ in range(others)])
+    refs.append(S.serialize_circuit(S.Circuit()))  # empty reference: zero row
+    oth.append(list(oth[0]))
+    values = rng.uniform(-2, 2, size=(3, 3)).astype(np.float32)
+    dg = rng.normal(size=(3, others)).astype(np.float32)
+    b = ops.InnerProductBatch(refs, names, oth, with_grads=True)
+    got = b.inner_product_grad(values, dg)
+    want = O.inner_product_grad(refs, names, values, oth, dg)
+    scale = max(1.0, float(np.abs(want).max()))
+    np.testing.assert_allclose(got, want, atol=2e-5 * scale, rtol=0)
+    assert np.all(got[2] == 0)
+    np.testing.assert_allclose(
+        ops.inner_product_grad(refs, names, values, oth, dg), np.conj(want),
+        atol=2e-5 * scale, rtol=0)
