@@ -156,6 +156,25 @@ int tfqg_batch_inner_product_grad(tfqg_batch* b, const float* symbol_values,
                                   const float* downstream_grads, void* grads,
                                   int device_buffers, void* stream);
 
+/* Noisy sampled expectations [batch, num_ops]: num_samples int32
+ * [batch, num_ops] trajectories per entry; in each trajectory every Pauli
+ * term is measured once (a +-1 parity drawn with P(+1) = (1 + <P>)/2 from the
+ * trajectory's state) and the per-entry mean is returned; -2 for empty
+ * programs.  Replaces TfqNoisySampledExpectationOp (noise/
+ * tfq_noisy_sampled_expectation.cc:143-404).  TFQG_KIND_NOISY batches. */
+int tfqg_batch_noisy_sampled_expectation(tfqg_batch* b, const float* symbol_values,
+                                         const int32_t* num_samples, uint64_t seed,
+                                         float* expectations, int device_buffers,
+                                         void* stream);
+
+/* Noisy samples int8 [batch, num_samples, max_num_qubits]: each sample is
+ * the measurement of every qubit at the end of its own trajectory, in the
+ * layout of tfqg_batch_samples (-2 padding).  Replaces TfqNoisySamplesOp
+ * (noise/tfq_noisy_samples.cc:55-280).  TFQG_KIND_NOISY batches. */
+int tfqg_batch_noisy_samples(tfqg_batch* b, const float* symbol_values,
+                             int32_t num_samples, uint64_t seed, int8_t* samples,
+                             int device_buffers, void* stream);
+
 /* Same result as tfqg_batch_expectation, for callers that must not let the
  * library allocate device memory (for example a host framework whose caching
  * allocator has already reserved nearly all device memory, so a plugin's own
@@ -213,6 +232,24 @@ int tfqg_simulate_sampled_expectation(const char* const* programs,
                                       const int64_t* pauli_sum_lens, int64_t num_ops,
                                       const int32_t* num_samples, uint64_t seed,
                                       float* expectations);
+
+/* tfq.noise.sampled_expectation (noise/noisy_sampled_expectation_op.py) */
+int tfqg_noisy_sampled_expectation(const char* const* programs,
+                                   const int64_t* program_lens, int64_t batch,
+                                   const char* const* symbol_names,
+                                   const int64_t* symbol_name_lens, int64_t num_symbols,
+                                   const float* symbol_values,
+                                   const char* const* pauli_sums,
+                                   const int64_t* pauli_sum_lens, int64_t num_ops,
+                                   const int32_t* num_samples, uint64_t seed,
+                                   float* expectations);
+
+/* tfq.noise.samples (noise/noisy_samples_op.py) */
+int tfqg_noisy_samples(const char* const* programs, const int64_t* program_lens,
+                       int64_t batch, const char* const* symbol_names,
+                       const int64_t* symbol_name_lens, int64_t num_symbols,
+                       const float* symbol_values, int32_t num_samples, uint64_t seed,
+                       int8_t* samples);
 
 /* tfq_inner_product (math_ops/inner_product_op.py) */
 int tfqg_inner_product(const char* const* programs, const int64_t* program_lens,

@@ -845,6 +845,31 @@ def _dm_apply(rho, n, m, qubits, controls=(), cvals=()):
     return apply_matrix(rho, 2 * n, np.conj(m), [q + n for q in qubits])
 
 
+def _final_dm(n, items):
+    """Exact density matrix [2^n, 2^n] after the gates and channels."""
+    rho = np.zeros([2] * (2 * n), dtype=np.complex128)
+    rho[(0,) * (2 * n)] = 1.0
+    for it in items:
+        if it[0] == "gate":
+            g = it[1]
+            rho = _dm_apply(rho, n, g.matrix, g.qubits, g.controls, g.cvals)
+        else:
+            kraus, qs = it[1], it[2]
+            acc = 0
+            for K in kraus:
+                acc = acc + _dm_apply(rho, n, np.asarray(K, dtype=np.complex128), qs)
+            rho = acc
+    return rho.reshape(2 ** n, 2 ** n)
+
+
+def noisy_probabilities(programs, symbol_names, symbol_values):
+    """(n, measurement probabilities) per noisy circuit: the diagonal of the
+    exact density matrix (what tfq_noisy_samples' trajectories sample)."""
+    parsed, _ = _parse_all(programs, symbol_names, symbol_values, noisy=True)
+    return [(n, np.real(np.diag(_final_dm(n, items))) if items else np.ones(1))
+            for n, index, items in parsed]
+
+
 def noisy_expectation_exact(programs, symbol_names, symbol_values, pauli_sums):
     parsed, psums = _parse_all(programs, symbol_names, symbol_values,
                                pauli_sums, noisy=True)
@@ -854,19 +879,7 @@ def noisy_expectation_exact(programs, symbol_names, symbol_values, pauli_sums):
         if not items:
             out[i, :] = -2.0
             continue
-        rho = np.zeros([2] * (2 * n), dtype=np.complex128)
-        rho[(0,) * (2 * n)] = 1.0
-        for it in items:
-            if it[0] == "gate":
-                g = it[1]
-                rho = _dm_apply(rho, n, g.matrix, g.qubits, g.controls, g.cvals)
-            else:
-                kraus, qs = it[1], it[2]
-                acc = 0
-                for K in kraus:
-                    acc = acc + _dm_apply(rho, n, np.asarray(K, dtype=np.complex128), qs)
-                rho = acc
-        R = rho.reshape(2 ** n, 2 ** n)
+        R = _final_dm(n, items)
         for j in range(n_ops):
             v = 0.0
             for t in psums[i][j]:

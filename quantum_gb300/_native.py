@@ -50,7 +50,8 @@ EXPORTED = (
     "tfqg_simulate_expectation", "tfqg_adj_grad", "tfqg_noisy_expectation",
     "tfqg_batch_sampled_expectation", "tfqg_simulate_sampled_expectation",
     "tfqg_batch_create_inner_product", "tfqg_batch_inner_product", "tfqg_inner_product",
-    "tfqg_batch_inner_product_grad",
+    "tfqg_batch_inner_product_grad", "tfqg_batch_noisy_sampled_expectation",
+    "tfqg_batch_noisy_samples", "tfqg_noisy_sampled_expectation", "tfqg_noisy_samples",
 )
 
 
@@ -87,6 +88,11 @@ def _declare(lib):
                                              c_void_p]
     lib.tfqg_batch_inner_product_grad.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p,
                                                   ctypes.c_int, c_void_p]
+    lib.tfqg_batch_noisy_sampled_expectation.argtypes = [
+        c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p, ctypes.c_int, c_void_p]
+    lib.tfqg_batch_noisy_samples.argtypes = [c_void_p, c_void_p, ctypes.c_int32,
+                                             ctypes.c_uint64, c_void_p, ctypes.c_int,
+                                             c_void_p]
     lib.tfqg_batch_sampled_expectation.argtypes = [
         c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p, ctypes.c_int,
         c_void_p]
@@ -97,6 +103,8 @@ def _declare(lib):
                  "tfqg_batch_sampled_expectation", "tfqg_simulate_sampled_expectation",
                  "tfqg_batch_create_inner_product", "tfqg_batch_inner_product",
                  "tfqg_inner_product", "tfqg_batch_inner_product_grad",
+                 "tfqg_batch_noisy_sampled_expectation", "tfqg_batch_noisy_samples",
+                 "tfqg_noisy_sampled_expectation", "tfqg_noisy_samples",
                  "tfqg_simulate_expectation",
                  "tfqg_adj_grad", "tfqg_noisy_expectation"):
         getattr(lib, name).restype = ctypes.c_int

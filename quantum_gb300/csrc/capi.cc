@@ -735,10 +735,13 @@ int tfqg_batch_adj_grad(tfqg_batch* b, const float* symbol_values,
   });
 }
 
-int tfqg_batch_noisy_expectation(tfqg_batch* b, const float* symbol_values,
-                                 const int32_t* num_samples, uint64_t seed,
-                                 float* expectations, int device_buffers,
-                                 void* stream) {
+namespace {
+
+// Trajectory expectations; with sample_terms each Pauli term is measured once
+// per trajectory instead of evaluated exactly (noisy sampled expectation).
+int noisy_expectation_impl(tfqg_batch* b, const float* symbol_values,
+                           const int32_t* num_samples, uint64_t seed, float* expectations,
+                           int device_buffers, void* stream, bool sample_terms) {
   return guarded([&]() {
     if (!b) throw Error(kInvalidArgument, "NULL batch");
     if (b->kind != TFQG_KIND_NOISY)
@@ -797,11 +800,73 @@ int tfqg_batch_noisy_expectation(tfqg_batch* b, const float* symbol_values,
     a.acc = acc;
     a.seed = seed;
     a.out_f = dout;
+    a.sample_terms = sample_terms ? 1 : 0;
     if (a.total_traj > 0) simulate(b, kModeNoisy, &a, s);
     TFQG_CUDA(launch_noisy_finalize(b->bd, a, s));
     finish(b, expectations, dout, obytes, device_buffers, s);
     // the host vectors above are read by async copies: keep them alive
     TFQG_CUDA(cudaStreamSynchronize(s));
+    return 0;
+  });
+}
+
+}  // namespace
+
+int tfqg_batch_noisy_expectation(tfqg_batch* b, const float* symbol_values,
+                                 const int32_t* num_samples, uint64_t seed,
+                                 float* expectations, int device_buffers,
+                                 void* stream) {
+  return noisy_expectation_impl(b, symbol_values, num_samples, seed, expectations,
+                                device_buffers, stream, false);
+}
+
+int tfqg_batch_noisy_sampled_expectation(tfqg_batch* b, const float* symbol_values,
+                                         const int32_t* num_samples, uint64_t seed,
+                                         float* expectations, int device_buffers,
+                                         void* stream) {
+  return noisy_expectation_impl(b, symbol_values, num_samples, seed, expectations,
+                                device_buffers, stream, true);
+}
+
+int tfqg_batch_noisy_samples(tfqg_batch* b, const float* symbol_values,
+                             int32_t num_samples, uint64_t seed, int8_t* samples,
+                             int device_buffers, void* stream) {
+  return guarded([&]() {
+    if (!b) throw Error(kInvalidArgument, "NULL batch");
+    if (b->kind != TFQG_KIND_NOISY)
+      throw Error(kInvalidArgument, "batch was not created for noisy simulation");
+    if (num_samples < 0)
+      throw Error(kInvalidArgument, "num_samples must be non-negative.");
+    std::lock_guard<std::mutex> lk(b->mu);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t obytes = size_t(b->B) * size_t(num_samples) * size_t(b->max_n);
+    if (obytes == 0) return 0;  // tfq_noisy_samples.cc:122-124
+    for (const DevChannel& ch : b->channels)
+      if (!ch.mixed_unitary && b->any_streamed)
+        throw Error(kUnimplemented,
+                    "Amplitude-damping, reset and phase-damping channels are "
+                    "supported up to 14 qubits.");
+    // one trajectory per sample, rows in order
+    std::vector<int64_t> prefix(static_cast<size_t>(b->B) + 1, 0);
+    for (int64_t i = 0; i < b->B; ++i) prefix[i + 1] = prefix[i] + num_samples;
+    RunArgs a;
+    prepare(b, symbol_values, device_buffers, false, 0, s, &a);
+    b->aux2.reserve(prefix.size() * sizeof(int64_t), b->device);
+    TFQG_CUDA(cudaMemcpyAsync(b->aux2.p, prefix.data(), prefix.size() * sizeof(int64_t),
+                              cudaMemcpyHostToDevice, s));
+    int8_t* dout = samples;
+    if (!device_buffers) {
+      b->out.reserve(obytes, b->device);
+      dout = static_cast<int8_t*>(b->out.p);
+    }
+    a.traj_prefix = static_cast<const int64_t*>(b->aux2.p);
+    a.total_traj = prefix.back();
+    a.out_samples = dout;
+    a.num_samples = num_samples;
+    a.seed = seed;
+    simulate(b, kModeNoisy, &a, s);
+    finish(b, samples, dout, obytes, device_buffers, s);
+    TFQG_CUDA(cudaStreamSynchronize(s));  // the host prefix is read asynchronously
     return 0;
   });
 }
@@ -1003,6 +1068,40 @@ int tfqg_inner_product(const char* const* programs, const int64_t* program_lens,
                                            other_program_lens, num_others, 0, &b);
   if (rc) return rc;
   rc = tfqg_batch_inner_product(b, symbol_values, inner_products, 0, nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
+int tfqg_noisy_sampled_expectation(const char* const* programs,
+                                   const int64_t* program_lens, int64_t batch,
+                                   const char* const* symbol_names,
+                                   const int64_t* symbol_name_lens, int64_t num_symbols,
+                                   const float* symbol_values,
+                                   const char* const* pauli_sums,
+                                   const int64_t* pauli_sum_lens, int64_t num_ops,
+                                   const int32_t* num_samples, uint64_t seed,
+                                   float* expectations) {
+  tfqg_batch* b = nullptr;
+  int rc = tfqg_batch_create(programs, program_lens, batch, symbol_names, symbol_name_lens,
+                             num_symbols, pauli_sums, pauli_sum_lens, num_ops,
+                             TFQG_KIND_NOISY, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_noisy_sampled_expectation(b, symbol_values, num_samples, seed,
+                                            expectations, 0, nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
+int tfqg_noisy_samples(const char* const* programs, const int64_t* program_lens,
+                       int64_t batch, const char* const* symbol_names,
+                       const int64_t* symbol_name_lens, int64_t num_symbols,
+                       const float* symbol_values, int32_t num_samples, uint64_t seed,
+                       int8_t* samples) {
+  tfqg_batch* b = nullptr;
+  int rc = tfqg_batch_create(programs, program_lens, batch, symbol_names, symbol_name_lens,
+                             num_symbols, nullptr, nullptr, 0, TFQG_KIND_NOISY, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_noisy_samples(b, symbol_values, num_samples, seed, samples, 0, nullptr);
   tfqg_batch_destroy(b);
   return rc;
 }

@@ -410,7 +410,7 @@ size_t sim_smem_bytes(int mode, int max_resident_n, bool any_streamed,
   bytes += 2 * sizeof(Stage) + sizeof(RedBuf);
   bytes += (1u << kHiBits) * sizeof(uint32_t);
   bytes += 2 * 4 * kWarps * sizeof(double);
-  if (mode == kModeSample) bytes += kMaxChunks * sizeof(double);
+  if (mode == kModeSample || mode == kModeNoisy) bytes += kMaxChunks * sizeof(double);
   bytes += 2 * kMaxMeasTermsDev * sizeof(double) + kMaxMeasTermsDev * 16;
   if (mode == kModeExpect) bytes += kMaxOpsSmem * sizeof(double);
   if (mode == kModeAdjoint) bytes += size_t(max_grads) * sizeof(double);

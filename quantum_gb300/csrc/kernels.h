@@ -61,6 +61,7 @@ struct RunArgs {
   int64_t lambda_stride = 0;
   int lambda_rot = 0;
   float grad_scale = 2.f;
+  int sample_terms = 0;              // noisy: each term measured once per trajectory
   double* term_vals = nullptr;       // optional [rows, term_stride]: <psi|P_t|psi>
   int64_t term_stride = 0;           // per term of the row (no coefficient)
 };

@@ -1145,6 +1145,12 @@ __device__ void measure_passes(const BatchDevice& b, const RunArgs& a,
             default: v = sim; break;
           }
         }
+        if (a.sample_terms && !sm.mterm[i].identity) {
+          // one measurement of the term: parity +1 with probability (1 + v)/2
+          const double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(rc.traj),
+                                     0xB0000000u + M.begin + uint32_t(i));
+          v = u < 0.5 + 0.5 * v ? 1.0 : -1.0;
+        }
         sink(int(sm.mterm[i].op), double(sm.mterm[i].w) * v);
         if (a.term_vals)
           a.term_vals[int64_t(rc.row) * a.term_stride +
@@ -1292,10 +1298,13 @@ __device__ void lambda_from_buffer(const RunArgs& a, const Smem& sm, const RowCt
 
 // Sampler: chunked |psi|^2 prefix sums in double, then per-sample search
 // (StateSpace::Sample semantics: index x with probability |psi_x|^2).
+// S samples into out (rows of max_n columns); sample s draws its uniform
+// from the counter (row, s0 + s).
 __device__ void sample_state(const BatchDevice& b, const RunArgs& a,
                              const Smem& sm, const RowCtx& rc,
-                             const float2* psi, bool shared) {
-  const int n = rc.p.n, maxn = b.max_n, S = a.num_samples;
+                             const float2* psi, bool shared, int8_t* out, int S,
+                             int s0) {
+  const int n = rc.p.n, maxn = b.max_n;
   const uint32_t N = 1u << n;
   const uint32_t nch = N < kMaxChunks ? N : kMaxChunks;
   const uint32_t L = N / nch;
@@ -1322,9 +1331,8 @@ __device__ void sample_state(const BatchDevice& b, const RunArgs& a,
     __syncthreads();
   }
   const double total = sm.csum[nch - 1];
-  int8_t* out = a.out_samples + int64_t(rc.row) * S * maxn;
   for (int s = threadIdx.x; s < S; s += blockDim.x) {
-    double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(s), 0x5A3Fu) * total;
+    double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(s0 + s), 0x5A3Fu) * total;
     uint32_t lo = 0, hi = nch - 1;
     while (lo < hi) {
       uint32_t mid = (lo + hi) >> 1;
@@ -1372,6 +1380,11 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
       if (MODE == kModeExpect)
         for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x)
           a.out_f[int64_t(row) * b.num_ops + j] = -2.f;
+      // noisy samples of an empty program: every column is padding
+      if (MODE == kModeNoisy && a.out_samples) {
+        int8_t* o = a.out_samples + (int64_t(row) * a.num_samples + traj) * b.max_n;
+        for (int c = threadIdx.x; c < b.max_n; c += blockDim.x) o[c] = int8_t(-2);
+      }
       return;  // noisy empty rows are finalised on the host side kernel
     }
   }
@@ -1423,6 +1436,11 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     });
     if (small)
       for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x) out[j] = float(sm.oacc[j]);
+  } else if (MODE == kModeNoisy && a.out_samples) {
+    // noisy samples: one measurement of every qubit per trajectory
+    // (tfq_noisy_samples.cc:166-187)
+    sample_state(b, a, sm, rc, psi, shared,
+                 a.out_samples + (int64_t(row) * a.num_samples + traj) * b.max_n, 1, traj);
   } else if (MODE == kModeNoisy) {
     const int64_t base = int64_t(row) * b.num_ops;
     measure_passes(b, a, sm, rc, g_psi, [&](int op, double v) {
@@ -1436,7 +1454,8 @@ __device__ void run_row(const BatchDevice& b, const RunArgs& a, const Smem& sm,
     for (uint32_t x = N + threadIdx.x; x < M; x += blockDim.x)
       o[x] = make_float2(-2.f, 0.f);
   } else if (MODE == kModeSample) {
-    sample_state(b, a, sm, rc, psi, shared);
+    sample_state(b, a, sm, rc, psi, shared,
+                 a.out_samples + int64_t(row) * a.num_samples * b.max_n, a.num_samples, 0);
   } else if (MODE == kModeAdjoint) {
     for (int k = threadIdx.x; k < rc.p.num_grads; k += blockDim.x) sm.grad[k] = 0.0;
     if (a.lambda_init) lambda_from_buffer(a, sm, rc, g_lam);
@@ -1480,7 +1499,7 @@ __device__ __forceinline__ Smem carve_smem(int state_amps, int nstates) {
   sm.red = reinterpret_cast<double*>(p);
   p += 2 * 4 * kWarps * sizeof(double);
   sm.csum = reinterpret_cast<double*>(p);
-  if (MODE == kModeSample) p += kMaxChunks * sizeof(double);
+  if (MODE == kModeSample || MODE == kModeNoisy) p += kMaxChunks * sizeof(double);
   sm.macc = reinterpret_cast<double*>(p);
   p += 2 * kMaxMeasTermsDev * sizeof(double);
   sm.mterm = reinterpret_cast<decltype(sm.mterm)>(p);

@@ -256,6 +256,27 @@ class Batch:
         return self._counts_call(_native.lib().tfqg_batch_noisy_expectation,
                                  symbol_values, num_samples, seed)
 
+    def noisy_sampled_expectation(self, symbol_values, num_samples, seed=None):
+        """Trajectory means of once-per-trajectory term measurements
+        (noise/noisy_sampled_expectation_op.py); num_samples [batch,
+        num_ops] trajectories per entry."""
+        return self._counts_call(_native.lib().tfqg_batch_noisy_sampled_expectation,
+                                 symbol_values, num_samples, seed)
+
+    def noisy_samples(self, symbol_values, num_samples, seed=None):
+        """int8 [batch, num_samples, max_n]: one sample per trajectory
+        (noise/noisy_samples_op.py), the samples op's layout."""
+        v = self._host_or_cuda(_values(symbol_values))
+        self._check_values(v)
+        if seed is None:
+            seed = int.from_bytes(os.urandom(8), "little")
+        out = self._out(v, (self.batch_size, int(num_samples), self.max_num_qubits),
+                        np.int8, getattr(torch, "int8", None))
+        _native.check(_native.lib().tfqg_batch_noisy_samples(
+            self._h, _ptr(v), int(num_samples), seed & (2 ** 64 - 1), _ptr(out),
+            self._device_flag(v), _stream(v)))
+        return self._wrap(symbol_values, out)
+
     def sampled_expectation(self, symbol_values, num_samples, seed=None):
         """Expectations estimated from measurement samples
         (tfq_simulate_ops.py:101-135); num_samples [batch, num_ops] samples
@@ -425,6 +446,37 @@ def inner_product_grad(programs, symbol_names, symbol_values, other_programs,
     try:
         out = b.inner_product_grad(symbol_values, prev_grad)
         return out.conj() if _is_torch(out) else np.conj(out)
+    finally:
+        b.close()
+
+
+def _one_sample_count(num_samples):
+    ns = np.asarray(num_samples.cpu().numpy() if _is_torch(num_samples)
+                    else num_samples)
+    if ns.ndim != 1:
+        raise InvalidArgumentError(f"num_samples must be rank 1. Got rank {ns.ndim}.")
+    if ns.shape[0] != 1:
+        raise InvalidArgumentError(f"num_samples must contain 1 element. Got {ns.shape[0]}.")
+    return int(ns[0])
+
+
+def noisy_samples(programs, symbol_names, symbol_values, num_samples, seed=None):
+    """noise/noisy_samples_op.py (tfq.noise.samples); `num_samples` is a
+    1-element tensor."""
+    n = _one_sample_count(num_samples)
+    b = Batch(programs, symbol_names, None, KIND_NOISY)
+    try:
+        return b.noisy_samples(symbol_values, n, seed)
+    finally:
+        b.close()
+
+
+def noisy_sampled_expectation(programs, symbol_names, symbol_values, pauli_sums,
+                              num_samples, seed=None):
+    """noise/noisy_sampled_expectation_op.py (tfq.noise.sampled_expectation)."""
+    b = Batch(programs, symbol_names, pauli_sums, KIND_NOISY)
+    try:
+        return b.noisy_sampled_expectation(symbol_values, num_samples, seed)
     finally:
         b.close()
 

@@ -359,3 +359,69 @@ def test_inner_product_grad_matches_oracle(n, others):
     np.testing.assert_allclose(
         ops.inner_product_grad(refs, names, values, oth, dg), np.conj(want),
         atol=2e-5 * scale, rtol=0)
+
+
+def test_noisy_samples_distribution_and_layout():
+    """tfq.noise.samples (noise/tfq_noisy_samples.cc): one measurement per
+    trajectory; the sample histogram against the exact density matrix's
+    diagonal (chi-squared, p > 1e-3), the samples op's bit layout and -2
+    padding, and an empty program padded throughout."""
+    rng = np.random.default_rng(41)
+    q3 = S.GridQubit.rect(1, 3)
+    c = random_circuit(q3, 5, rng, ["a"], p_control=0.2, channels=list(CHANNELS),
+                       p_channel=0.4)
+    prog3 = S.serialize_circuit(c)
+    q2 = S.GridQubit.rect(1, 2)
+    prog2 = S.serialize_circuit(S.Circuit([[S.X(q2[0]), S.I(q2[1])],
+                                           [S.bit_flip(q2[1], 0.25)]]))
+    empty = S.serialize_circuit(S.Circuit())
+    vals = np.array([[0.4], [0.0], [0.0]], np.float32)
+    shots = 20000
+    res = ops.noisy_samples([prog3, prog2, empty], ["a"], vals, [shots], seed=3)
+    assert res.shape == (3, shots, 3)
+    assert (res[2] == -2).all()
+    assert (res[1, :, 0] == -2).all() and (res[1, :, 1] == 1).all()
+    flips = res[1, :, 2].mean()
+    assert abs(flips - 0.25) < 5 * np.sqrt(0.25 * 0.75 / shots)
+    from scipy import stats
+    (n, probs), *_ = O.noisy_probabilities([prog3], ["a"], vals[:1])
+    idx = (res[0].astype(np.int64)[:, ::-1] << np.arange(3)).sum(axis=1)
+    counts = np.bincount(idx, minlength=8)
+    exp = probs * shots
+    keep = exp >= 5
+    cc = list(counts[keep]) + [counts[~keep].sum()]
+    ce = list(exp[keep]) + [exp[~keep].sum()]
+    if ce[-1] < 5:
+        cc[-2] += cc.pop()
+        ce[-2] += ce.pop()
+    p = stats.chisquare(cc, np.asarray(ce) * sum(cc) / sum(ce)).pvalue
+    assert p > 1e-3, (counts, probs, p)
+
+
+@pytest.mark.parametrize("n,channels", [(3, CHANNELS), (5, ["DP", "AD", "BF"])])
+def test_noisy_sampled_expectation_vs_density_matrix(n, channels):
+    """tfq.noise.sampled_expectation: each trajectory measures every term once;
+    the mean of R trajectories is within 5 standard errors (sum|c| / sqrt(R))
+    of the exact density-matrix expectation; empty programs give -2."""
+    rng = np.random.default_rng(610 + n)
+    qs = S.GridQubit.rect(1, n)
+    names = ["a", "b"]
+    progs, psums = [], []
+    for _ in range(2):
+        c = random_circuit(qs, 5, rng, names, p_control=0.2, channels=list(channels),
+                           p_channel=0.4)
+        progs.append(S.serialize_circuit(c))
+        psums.append([S.serialize_paulisum([(1.0, [(q, "Z")]) for q in qs]),
+                      random_paulisum(qs, rng)])
+    progs.append(S.serialize_circuit(S.Circuit()))
+    psums.append(psums[0])
+    vals = rng.uniform(-1, 1, size=(3, 2)).astype(np.float32)
+    R = 20000
+    got = ops.noisy_sampled_expectation(progs, names, vals, psums,
+                                        np.full((3, 2), R, np.int32), seed=9)
+    want = O.noisy_expectation_exact(progs[:2], names, vals[:2], psums[:2])
+    absc = [[sum(abs(float(t["re"])) for t in O.decode_paulisum(p) if t["paulis"])
+             for p in row] for row in psums[:2]]
+    bound = 5 * np.asarray(absc) / np.sqrt(R) + 1e-4
+    assert np.all(np.abs(got[:2] - want) <= bound), (got, want, bound)
+    np.testing.assert_array_equal(got[2], [-2.0, -2.0])
