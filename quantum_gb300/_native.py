@@ -195,6 +195,44 @@ def set_wide_min_qubits(n):
     return f(int(n))
 
 
+def set_gate_fusion(on):
+    """Gate fusion of forward plans on or off for batches created from now
+    on; returns the previous setting."""
+    f = lib().tfqg_internal_set_gate_fusion
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return bool(f(1 if on else 0))
+
+
+def forward_plan_gates(handle, row, row_values):
+    """The gates of a row's forward plan in execution order, with matrices
+    bound on the host: a list of (nq, b0, b1, cmask, cval, kind, matrix)."""
+    import numpy as np
+    f = lib().tfqg_internal_forward_plan_gates
+    f.argtypes = [c_void_p, ctypes.c_int64, c_void_p, c_void_p, c_void_p,
+                  ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    f.restype = ctypes.c_int
+    vals = np.ascontiguousarray(row_values, dtype=np.float32)
+    if vals.size == 0:
+        vals = np.zeros(1, np.float32)
+    count = ctypes.c_int64()
+    check(f(handle, int(row), vals.ctypes.data, None, None, 0, ctypes.byref(count)))
+    k = count.value
+    meta = np.zeros((max(k, 1), 6), np.int32)
+    mats = np.zeros((max(k, 1), 32), np.float32)
+    check(f(handle, int(row), vals.ctypes.data, meta.ctypes.data,
+            mats.ctypes.data, k, ctypes.byref(count)))
+    out = []
+    for i in range(k):
+        nq = int(meta[i, 0])
+        m = (mats[i, 0::2] + 1j * mats[i, 1::2]).astype(np.complex128)
+        m = m[:4].reshape(2, 2) if nq == 1 else m.reshape(4, 4)
+        out.append((nq, int(meta[i, 1]), int(meta[i, 2]),
+                    int(meta[i, 3]) & 0xFFFFFFFF, int(meta[i, 4]) & 0xFFFFFFFF,
+                    int(meta[i, 5]), m))
+    return out
+
+
 def batch_wide_rows(handle):
     f = lib().tfqg_internal_batch_wide_rows
     f.argtypes = [c_void_p]

@@ -73,6 +73,7 @@ struct tfqg_batch {
   int max_streamed_n_fwd = 0;
   int max_grads = 0;
   int64_t total_gates = 0, total_grads = 0;
+  bool any_fused = false;  // forward plans hold GK_FUSED gates
 
   // packed host copies of the device tables
   std::vector<tfqg::DevProgram> programs;

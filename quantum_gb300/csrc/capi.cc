@@ -15,6 +15,7 @@
 
 #include "../../include/tfq_gb300.h"
 #include "batch_internal.h"
+#include "gate_math.cuh"
 #include "host.h"
 #include "jit.h"
 #include "kernels.h"
@@ -40,6 +41,9 @@ namespace {
 std::atomic<int> g_wide_min_qubits{kWideMinQubits};
 
 int wide_min_qubits() { return g_wide_min_qubits.load(); }
+
+// Gate fusion of forward plans (on by default).
+std::atomic<int> g_gate_fusion{1};
 
 }  // namespace
 
@@ -186,7 +190,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   for (size_t pid = 0; pid < parsed.size(); ++pid) {
     if (inner && pair_of[pid] >= 0) continue;
     compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
-    plan_program(&compiled[pid], job);
+    plan_program(&compiled[pid], job, g_gate_fusion.load() != 0);
   }
   for (size_t pid = 0; pid < parsed.size() && inner; ++pid) {
     if (pair_of[pid] < 0) continue;
@@ -196,7 +200,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       throw Error(kInvalidArgument,
                   "Found symbols in other_programs.No symbols are allowed in these circuits.");
     }
-    plan_program(&compiled[pid], kJobForward);
+    plan_program(&compiled[pid], kJobForward, g_gate_fusion.load() != 0);
   }
 
   // 5. pack programs
@@ -299,6 +303,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   }
   b->total_gates = mat;
   b->total_grads = dmat;
+  for (const GateTemplate& g : b->gates) b->any_fused |= g.kind == GK_FUSED;
   // most expensive rows first (approximate longest-processing-time order)
   b->order.resize(size_t(batch));
   for (int64_t i = 0; i < batch; ++i) b->order[i] = int32_t(i);
@@ -406,6 +411,7 @@ BatchDevice tfqg::table_view(const tfqg_batch* b, unsigned char* base,
   d.max_n = b->max_n;
   d.total_gates = b->total_gates;
   d.total_grads = b->total_grads;
+  d.any_fused = b->any_fused ? 1 : 0;
   return d;
 }
 
@@ -1218,6 +1224,12 @@ int tfqg_internal_set_wide_min_qubits(int n) {
   return g_wide_min_qubits.exchange(n);
 }
 
+// Gate fusion of forward plans on (1) or off (0) for batches created after
+// the call; returns the previous setting.
+int tfqg_internal_set_gate_fusion(int on) {
+  return g_gate_fusion.exchange(on ? 1 : 0);
+}
+
 // Number of wide rows of a batch (forward modes).
 int tfqg_internal_batch_wide_rows(void* batch) {
   const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
@@ -1247,6 +1259,59 @@ int tfqg_internal_batch_row_costs(void* batch, double* costs) {
     const DevProgram& p = b->programs[r.program];
     costs[i] = r.n > 0 ? double(p.num_gates + 1) * std::ldexp(1.0, r.n) : 0.0;
   }
+  return 0;
+}
+
+// The gates of row `row`'s forward plan in execution order, with their
+// matrices bound to `row_values` on the host (the product the device builds
+// for a fused gate).  Per gate, meta holds (nq, b0, b1, cmask, cval, kind)
+// and mats 16 complex entries (row-major 2x2 or 4x4, b0 the MSB).  Returns
+// the count in *count; at most `max` gates are written.
+int tfqg_internal_forward_plan_gates(void* batch, int64_t row,
+                                     const float* row_values, int32_t* meta,
+                                     float* mats, int64_t max, int64_t* count) {
+  const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
+  if (!b || row < 0 || row >= int64_t(b->rows.size()) || !count)
+    return kInvalidArgument;
+  const DevProgram& p = b->programs[b->rows[size_t(row)].program];
+  const GateTemplate* gates = b->gates.data() + p.gate_begin;
+  int64_t k = 0;
+  for (uint32_t ps = p.fwd_pass_begin; ps < p.fwd_pass_end; ++ps)
+    for (uint32_t o = b->passes[ps].op_begin; o < b->passes[ps].op_end; ++o) {
+      const DevOp& op = b->ops[o];
+      if (op.type != OP_F1 && op.type != OP_F2) continue;
+      if (k < max) {
+        const GateTemplate& g = gates[op.gate];
+        Cx<double> m[16];
+        int nq = g.nq;
+        if (g.kind == GK_FUSED) {
+          Cx<float> f[16];
+          fused_product(gates, g,
+                        [&](int k, Cx<float>* mf) {
+                          Cx<double> md[16];
+                          const int kq = bound_matrix(gates[k], row_values, md);
+                          for (int i = 0; i < 16; ++i)
+                            mf[i] = i < (kq == 1 ? 4 : 16)
+                                        ? Cx<float>(float(md[i].re), float(md[i].im))
+                                        : Cx<float>(0.f, 0.f);
+                        },
+                        f);
+          for (int i = 0; i < 16; ++i) m[i] = Cx<double>(f[i].re, f[i].im);
+        } else {
+          nq = bound_matrix(g, row_values, m);
+        }
+        const int32_t mt[6] = {nq, g.b0, g.b1, int32_t(g.cmask), int32_t(g.cval),
+                               g.kind};
+        for (int i = 0; i < 6; ++i) meta[k * 6 + i] = mt[i];
+        for (int i = 0; i < 16; ++i) {
+          const bool in = i < (nq == 1 ? 4 : 16);
+          mats[k * 32 + 2 * i] = in ? float(m[i].re) : 0.f;
+          mats[k * 32 + 2 * i + 1] = in ? float(m[i].im) : 0.f;
+        }
+      }
+      ++k;
+    }
+  *count = k;
   return 0;
 }
 

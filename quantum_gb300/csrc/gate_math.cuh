@@ -261,4 +261,59 @@ TFQG_HD void effective_params(const GateTemplate& g, float raw0, float raw1,
   }
 }
 
+// Matrix of one template with its parameters bound: a[i] is replaced by
+// row_values[src[i]] where the template names a symbol column.
+TFQG_HD int bound_matrix(const GateTemplate& gt, const float* row_values,
+                         Cx<double>* m) {
+  GateTemplate gv = gt;
+  for (int i = 0; i < 5; ++i)
+    if (gt.src[i] >= 0) gv.a[i] = row_values[gt.src[i]];
+  float e0, e1, e2;
+  effective_params(gv, gv.a[0], gv.a[2], &e0, &e1, &e2);
+  return gate_matrix<double>(gt.kind, e0, e1, e2, m);
+}
+
+// Matrix of a GK_FUSED gate: the product of its members' matrices in time
+// order (the last member leftmost), each member embedded into the fused
+// gate's space (2x2 for nq == 1, 4x4 with b0 as MSB for nq == 2) by its
+// FusePos.  Members come as fp32 matrices from `load(k, m)` (k = template
+// index) and are multiplied in fp32, as qsim multiplies the fp32 matrices of
+// the gates it fuses.  `gates` is the program's template array.
+template <class Load>
+TFQG_HD void fused_product(const GateTemplate* gates, const GateTemplate& f,
+                           Load load, Cx<float>* F) {
+  const int D = f.nq == 1 ? 2 : 4;
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; ++c)
+      F[r * D + c] = Cx<float>(r == c ? 1.f : 0.f, 0.f);
+  int k = f.link;
+  for (int guard = 0; k >= 0 && guard < kMaxFuseMembers; ++guard) {
+    const GateTemplate& g = gates[k];
+    Cx<float> m[16], out[16];
+    load(k, m);
+    if (D == 2 || g.fpos == FP_HIGH || g.fpos == FP_LOW) {
+      // 1-qubit member: row r mixes with the row that differs in its bit
+      const int s = D == 2 ? 1 : (g.fpos == FP_HIGH ? 2 : 1);
+      for (int r = 0; r < D; ++r) {
+        const int rb = (r & s) ? 1 : 0, r0 = r & ~s;
+        for (int c = 0; c < D; ++c)
+          out[r * D + c] = m[rb * 2] * F[r0 * D + c] + m[rb * 2 + 1] * F[(r0 | s) * D + c];
+      }
+    } else {
+      for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+          Cx<float> acc(0.f, 0.f);
+          for (int j = 0; j < 4; ++j) {
+            const int rr = g.fpos == FP_SAME ? r : ((r & 1) << 1 | r >> 1);
+            const int jj = g.fpos == FP_SAME ? j : ((j & 1) << 1 | j >> 1);
+            acc = acc + m[rr * 4 + jj] * F[j * 4 + c];
+          }
+          out[r * 4 + c] = acc;
+        }
+    }
+    for (int i = 0; i < D * D; ++i) F[i] = out[i];
+    k = g.link;
+  }
+}
+
 }  // namespace tfqg

@@ -442,6 +442,7 @@ void build_gate(const OpP& op, const GateInfo& info, int n,
   g->nq = uint8_t(info.nq);
   for (int i = 0; i < 5; ++i) g->src[i] = -1;
   g->grad_slot = -1;
+  g->link = -1;
   g->b0 = uint8_t(qubit_bit(op, 0, n, index));
   if (info.nq == 2) g->b1 = uint8_t(qubit_bit(op, 1, n, index));
   switch (info.kind) {
@@ -922,9 +923,216 @@ void plan_sequence(const CompiledProgram& p, const std::vector<PlanItem>& items,
   }
 }
 
+// ---------------------------------------------------------------------------
+// gate fusion (forward plans)
+// ---------------------------------------------------------------------------
+// The analog of qsim's basic fuser, which the reference runs on every
+// parsed circuit (circuit_parser_qsim.cc:857, qsim::BasicGateFuser into
+// 2-qubit gates; applied by tfq_simulate_expectation_op.cc:164-165): runs of
+// uncontrolled 1-qubit
+// gates ("chains") are folded into a neighbouring uncontrolled 2-qubit gate
+// ("anchor") on their qubit, or merged into one 1-qubit gate.  Unlike qsim,
+// a fold is taken only where a cost model over the device's arithmetic per
+// amplitude says the fused gate is cheaper: a diagonal CZ stays diagonal
+// unless enough dense 1-qubit work is folded into it.
+
+// FP32 operations per amplitude of the device's gate arithmetic, plus one
+// for the op itself.
+int fuse_cost(int nq, uint8_t cls) {
+  switch (cls) {
+    case GC_SKIP: return 0;
+    case GC_X: return 1;
+    case GC_DIAG: return 5;
+    case GC_REAL: return nq == 1 ? 5 : 17;
+    default: return nq == 1 ? 9 : 17;
+  }
+}
+
+// Structure class of a product of gates of the given classes.
+uint8_t fold_class(uint8_t acc, uint8_t cls, int nq) {
+  if (cls == GC_SKIP) return acc;
+  if (acc == GC_SKIP) return (nq == 2 && cls == GC_X) ? uint8_t(GC_GENERAL) : cls;
+  if (acc == GC_DIAG && cls == GC_DIAG) return GC_DIAG;
+  if (nq == 1 && (acc == GC_REAL || acc == GC_X) && (cls == GC_REAL || cls == GC_X))
+    return GC_REAL;
+  return GC_GENERAL;
+}
+
+struct FuseChain {
+  int bit = 0;
+  std::vector<int> pos;  // sequence positions of the chain's gates
+  int owner = -1;        // anchor that absorbs it, -1 none
+  uint8_t cls = GC_SKIP;
+  int separate = 0;      // cost of its gates run one by one
+};
+
+struct FuseAnchor {
+  int pos = 0;
+  int chain[4] = {-1, -1, -1, -1};  // before on b0, b1; after on b0, b1
+  uint8_t cls = GC_GENERAL;
+};
+
+constexpr int kMaxChainGates = 15;  // 4 chains + anchor <= kMaxFuseMembers
+
+// Chain cost where it is not folded into an anchor: merged when that is not
+// more expensive than its gates one by one.
+int chain_cost(const FuseChain& c) {
+  if (c.pos.size() < 2) return c.separate;
+  return std::min(c.separate, fuse_cost(1, c.cls));
+}
+
+// Rewrites p->sequence into `out`, appending GK_FUSED templates to p->gates.
+void fuse_forward(CompiledProgram* p, std::vector<int32_t>* out) {
+  const std::vector<int32_t>& seq = p->sequence;
+  std::vector<FuseChain> chains;
+  std::vector<FuseAnchor> anchors;
+  int cur[32], last[32];
+  for (int q = 0; q < 32; ++q) cur[q] = last[q] = -1;
+  auto barrier = [&](uint32_t bits) {
+    for (int q = 0; q < 32; ++q)
+      if (bits >> q & 1) cur[q] = last[q] = -1;
+  };
+  for (size_t i = 0; i < seq.size(); ++i) {
+    const int32_t s = seq[i];
+    if (s < 0) {
+      barrier(1u << p->channels[~s].bit);
+      continue;
+    }
+    const GateTemplate& g = p->gates[s];
+    if (g.cls == GC_SKIP) continue;  // identities commute with everything
+    if (g.cmask != 0 || g.nq > 2) {
+      barrier(g.cmask | 1u << g.b0 | (g.nq == 2 ? 1u << g.b1 : 0u));
+      continue;
+    }
+    if (g.nq == 1) {
+      const int q = g.b0;
+      if (cur[q] >= 0 && int(chains[cur[q]].pos.size()) >= kMaxChainGates)
+        cur[q] = last[q] = -1;  // full: the next chain starts unattached
+      if (cur[q] < 0) {
+        cur[q] = int(chains.size());
+        chains.emplace_back();
+        chains.back().bit = q;
+        if (last[q] >= 0) {
+          FuseAnchor& a = anchors[last[q]];
+          a.chain[q == p->gates[seq[a.pos]].b0 ? 2 : 3] = cur[q];
+        }
+      }
+      FuseChain& c = chains[cur[q]];
+      c.pos.push_back(int(i));
+      c.cls = fold_class(c.cls, g.cls, 1);
+      c.separate += fuse_cost(1, g.cls);
+      continue;
+    }
+    FuseAnchor a;
+    a.pos = int(i);
+    a.cls = g.cls;
+    const int bits[2] = {g.b0, g.b1};
+    for (int j = 0; j < 2; ++j) {
+      const int q = bits[j];
+      a.chain[j] = cur[q];
+      cur[q] = -1;
+      last[q] = int(anchors.size());
+    }
+    anchors.push_back(a);
+  }
+
+  // dense anchors take every chain beside them for free
+  for (FuseAnchor& a : anchors) {
+    if (a.cls != GC_GENERAL) continue;
+    for (int c : a.chain)
+      if (c >= 0 && chains[c].owner < 0) chains[c].owner = int(&a - anchors.data());
+  }
+  // other anchors: diagonal chains into a diagonal anchor keep it diagonal;
+  // the rest are taken together when the dense product is cheaper
+  for (FuseAnchor& a : anchors) {
+    if (a.cls == GC_GENERAL) continue;
+    const int id = int(&a - anchors.data());
+    uint8_t cls = a.cls;
+    if (cls == GC_DIAG)
+      for (int c : a.chain)
+        if (c >= 0 && chains[c].owner < 0 && chains[c].cls == GC_DIAG)
+          chains[c].owner = id;
+    int separate = fuse_cost(2, cls);
+    std::vector<int> rest;
+    for (int c : a.chain)
+      if (c >= 0 && chains[c].owner < 0) {
+        rest.push_back(c);
+        separate += chain_cost(chains[c]);
+      }
+    if (!rest.empty() && fuse_cost(2, GC_GENERAL) <= separate)
+      for (int c : rest) chains[c].owner = id;
+  }
+
+  // emit
+  std::vector<int32_t> at(seq.begin(), seq.end());  // per position, or drop
+  const int32_t kDrop = INT32_MIN;
+  auto new_fused = [&](int nq, int b0, int b1, uint8_t cls) {
+    GateTemplate f;
+    memset(&f, 0, sizeof(f));
+    f.kind = GK_FUSED;
+    f.nq = uint8_t(nq);
+    f.b0 = uint8_t(b0);
+    f.b1 = uint8_t(b1);
+    for (int i = 0; i < 5; ++i) f.src[i] = -1;
+    f.grad_slot = -1;
+    f.link = -1;
+    f.cls = cls;
+    p->gates.push_back(f);
+    return int32_t(p->gates.size() - 1);
+  };
+  for (size_t ai = 0; ai < anchors.size(); ++ai) {
+    const FuseAnchor& a = anchors[ai];
+    std::vector<int> members;  // sequence positions, time order
+    uint8_t cls = GC_SKIP;
+    const GateTemplate anchor = p->gates[seq[a.pos]];
+    for (int j = 0; j < 4; ++j) {
+      if (j == 2) {
+        members.push_back(a.pos);
+        cls = fold_class(cls, anchor.cls, 2);
+      }
+      const int c = a.chain[j];
+      if (c < 0 || chains[c].owner != int(ai)) continue;
+      for (int ps : chains[c].pos) members.push_back(ps);
+      cls = fold_class(cls, chains[c].cls, 2);
+    }
+    if (members.size() < 2) continue;
+    const int32_t f = new_fused(2, anchor.b0, anchor.b1, cls);
+    int32_t prev = -1;
+    for (int ps : members) {
+      const int32_t gi = seq[ps];
+      GateTemplate& m = p->gates[gi];
+      m.fpos = ps == a.pos ? uint8_t(FP_SAME)
+                           : (m.b0 == anchor.b0 ? uint8_t(FP_HIGH) : uint8_t(FP_LOW));
+      m.link = -1;
+      if (prev < 0) p->gates[f].link = gi; else p->gates[prev].link = gi;
+      prev = gi;
+      at[ps] = kDrop;
+    }
+    at[a.pos] = f;
+  }
+  for (const FuseChain& c : chains) {
+    if (c.owner >= 0 || c.pos.size() < 2 || fuse_cost(1, c.cls) > c.separate)
+      continue;
+    const int32_t f = new_fused(1, c.bit, 0, c.cls);
+    int32_t prev = -1;
+    for (int ps : c.pos) {
+      const int32_t gi = seq[ps];
+      p->gates[gi].fpos = FP_HIGH;
+      p->gates[gi].link = -1;
+      if (prev < 0) p->gates[f].link = gi; else p->gates[prev].link = gi;
+      prev = gi;
+      at[ps] = kDrop;
+    }
+    at[c.pos.back()] = f;
+  }
+  out->clear();
+  for (int32_t s : at)
+    if (s != kDrop) out->push_back(s);
+}
+
 }  // namespace
 
-void plan_program(CompiledProgram* p, JobKind kind) {
+void plan_program(CompiledProgram* p, JobKind kind, bool fuse) {
   p->fwd_passes.clear();
   p->bwd_passes.clear();
   p->fwd_ops.clear();
@@ -934,9 +1142,15 @@ void plan_program(CompiledProgram* p, JobKind kind) {
   p->resident = p->n <= res_max;
   const int tile_bits = p->resident ? p->n : kStreamTileBits;
   std::vector<int> chan_bits(p->channels.size(), 0);
+  // a re-plan starts again from the program's own gates
+  while (!p->gates.empty() && p->gates.back().kind == GK_FUSED) p->gates.pop_back();
+  std::vector<int32_t> fused;
+  const bool fusing = fuse && kind == kJobForward;
+  if (fusing) fuse_forward(p, &fused);
+  const std::vector<int32_t>& sequence = fusing ? fused : p->sequence;
   std::vector<PlanItem> items;
-  items.reserve(p->sequence.size());
-  for (int32_t s : p->sequence) {
+  items.reserve(sequence.size());
+  for (int32_t s : sequence) {
     PlanItem it;
     it.seq = s;
     if (s >= 0) {

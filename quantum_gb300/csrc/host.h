@@ -117,7 +117,7 @@ void check_paired_qubits(const ProgramP& other,
 uint8_t classify_gate(const GateTemplate& g);
 
 // Plans forward (and, for the adjoint, backward) passes.
-void plan_program(CompiledProgram* prog, JobKind kind);
+void plan_program(CompiledProgram* prog, JobKind kind, bool fuse = false);
 
 // Groups terms [tb, te) into measurement passes: each pass's tile holds the
 // flip bits of all its terms (resident rows: one pass over the whole state).

@@ -34,7 +34,10 @@ __device__ __forceinline__ void store_mat(float2* dst, const Cx<double>* m,
                      : make_float2(0.f, 0.f);
 }
 
-__global__ void build_matrices_kernel(BatchDevice b, RunArgs a, int with_grads) {
+// phase 0: every gate's own matrix (and derivatives); phase 1: GK_FUSED
+// gates, as products of their members' matrices written in phase 0.
+__global__ void build_matrices_kernel(BatchDevice b, RunArgs a, int with_grads,
+                                      int phase) {
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= b.total_gates) return;
   // locate the row: rows are laid out with increasing mat_offset
@@ -48,6 +51,22 @@ __global__ void build_matrices_kernel(BatchDevice b, RunArgs a, int with_grads) 
   int g = int(t - int64_t(row.mat_offset));
   if (g >= prog.num_gates) return;
   const GateTemplate gt = b.gates[prog.gate_begin + g];
+  if ((gt.kind == GK_FUSED) != (phase == 1)) return;
+  if (phase == 1) {
+    const float2* mats = a.mats + int64_t(row.mat_offset) * 16;
+    Cx<float> f[16];
+    fused_product(b.gates + prog.gate_begin, gt,
+                  [&](int k, Cx<float>* m) {
+                    const float2* src = mats + int64_t(k) * 16;
+                    for (int i = 0; i < 16; ++i) m[i] = Cx<float>(src[i].x, src[i].y);
+                  },
+                  f);
+    float2* dst = a.mats + int64_t(t) * 16;
+    const int dim = gt.nq == 1 ? 4 : 16;
+    for (int i = 0; i < 16; ++i)
+      dst[i] = i < dim ? make_float2(f[i].re, f[i].im) : make_float2(0.f, 0.f);
+    return;
+  }
   float v[5];
   for (int i = 0; i < 5; ++i)
     v[i] = gt.src[i] >= 0 ? a.values[int64_t(lo) * b.num_symbols + gt.src[i]]
@@ -392,7 +411,9 @@ cudaError_t launch_build_matrices(const BatchDevice& b, const RunArgs& a,
   if (b.total_gates == 0) return cudaSuccess;
   const int threads = 128;
   int64_t blocks = (b.total_gates + threads - 1) / threads;
-  build_matrices_kernel<<<unsigned(blocks), threads, 0, s>>>(b, a, with_grads ? 1 : 0);
+  build_matrices_kernel<<<unsigned(blocks), threads, 0, s>>>(b, a, with_grads ? 1 : 0, 0);
+  if (b.any_fused)
+    build_matrices_kernel<<<unsigned(blocks), threads, 0, s>>>(b, a, 0, 1);
   return cudaGetLastError();
 }
 

@@ -33,6 +33,8 @@ struct BatchDevice {
   int32_t max_n = 0;
   int64_t total_gates = 0;   // matrix slots over all rows
   int64_t total_grads = 0;   // derivative slots over all rows
+  int32_t any_fused = 0;     // some program holds GK_FUSED gates
+  int32_t pad_ = 0;
 };
 
 struct RunArgs {

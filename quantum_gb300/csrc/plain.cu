@@ -205,6 +205,7 @@ cudaError_t plain_expect_adjoint(const PlainJob& j, cudaStream_t s,
   plain_init<<<blocks_for(total, T), T, 0, s>>>(j.psi, total, n); ++L;
   for (int g = 0; g < j.num_gates; ++g) {
     const GateTemplate& gt = j.gates[g];
+    if (gt.kind == GK_FUSED) continue;  // its members run one by one
     plain_gate<<<blocks_for((N >> gt.nq) * j.rows, T), T, 0, s>>>(
         gt, j.mats, j.num_gates, g, j.psi, j.rows, n, 0);
     ++L;
@@ -223,6 +224,7 @@ cudaError_t plain_expect_adjoint(const PlainJob& j, cudaStream_t s,
   }
   for (int g = j.num_gates - 1; g >= 0; --g) {
     const GateTemplate& gt = j.gates[g];
+    if (gt.kind == GK_FUSED) continue;
     const int64_t work = (N >> gt.nq) * j.rows;
     plain_gate<<<blocks_for(work, T), T, 0, s>>>(gt, j.mats, j.num_gates, g,
                                                  j.psi, j.rows, n, 1);

@@ -45,6 +45,10 @@ int tfqg_internal_batch_passes(void* batch, int32_t* fwd, int32_t* bwd,
 // for empty programs), used to shard a batch across devices.
 int tfqg_internal_batch_row_costs(void* batch, double* costs);
 int tfqg_internal_set_wide_min_qubits(int n);
+int tfqg_internal_set_gate_fusion(int on);
+int tfqg_internal_forward_plan_gates(void* batch, int64_t row,
+                                     const float* row_values, int32_t* meta,
+                                     float* mats, int64_t max, int64_t* count);
 uint64_t tfqg_internal_batch_fingerprint(void* batch);
 int tfqg_internal_batch_wide_rows(void* batch);
 // Expectation + adjoint gradient of a uniform batch by the plain path, all

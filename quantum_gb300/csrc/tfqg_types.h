@@ -17,8 +17,23 @@ namespace tfqg {
 // Gate kinds: the 16 gate ids of circuit_parser_qsim.cc:577-584.
 enum GateKind : uint8_t {
   GK_I1 = 0, GK_I2, GK_XP, GK_YP, GK_ZP, GK_HP, GK_XXP, GK_YYP, GK_ZZP,
-  GK_CZP, GK_CNP, GK_SP, GK_ISP, GK_PXP, GK_FSIM, GK_PISP, GK_COUNT
+  GK_CZP, GK_CNP, GK_SP, GK_ISP, GK_PXP, GK_FSIM, GK_PISP, GK_COUNT,
+  // Product of several gates of one program on one or two bits, made by the
+  // host's gate fuser for forward plans; its matrix is built on the device
+  // from the members' matrices (GateTemplate::link).
+  GK_FUSED = 32
 };
+
+// Placement of a fused gate's member inside the fused matrix.
+enum FusePos : uint8_t {
+  FP_HIGH = 0,     // 1-qubit member on the fused gate's b0 (matrix MSB)
+  FP_LOW = 1,      // 1-qubit member on b1
+  FP_SAME = 2,     // 2-qubit member with the fused gate's (b0, b1)
+  FP_SWAPPED = 3   // 2-qubit member on (b1, b0)
+};
+
+// Upper bound on the members of one fused gate.
+constexpr int kMaxFuseMembers = 64;
 
 // Channel kinds: the 8 channel ids of circuit_parser_qsim.cc:757-761.
 enum ChannelKind : uint8_t {
@@ -43,6 +58,10 @@ struct GateTemplate {
   uint8_t gparam[2];   // parameter (0 or 1) differentiated by each slot
   uint8_t cls;         // GateClass
   int32_t grad_slot;   // first derivative slot of this gate, or -1
+  // Fusion links: a GK_FUSED gate names its first member here, and each
+  // member names the next one (-1 ends the list; members are in time order).
+  int32_t link;
+  uint8_t fpos;        // FusePos of a member
 };
 
 // Structure class of a gate matrix, chosen on the host; the kernels use the

@@ -425,3 +425,41 @@ def test_noisy_sampled_expectation_vs_density_matrix(n, channels):
     bound = 5 * np.asarray(absc) / np.sqrt(R) + 1e-4
     assert np.all(np.abs(got[:2] - want) <= bound), (got, want, bound)
     np.testing.assert_array_equal(got[2], [-2.0, -2.0])
+
+
+@pytest.mark.parametrize("case", ["layers", "grid", "uneven", "random"])
+def test_fused_forward_plans_match_unfused_and_oracle(case):
+    """Forward plans run fused gates (one-qubit chains folded into two-qubit
+    gates); states and expectations must match the unfused plan and the
+    oracle, resident (<= 14 qubits) and streamed (15, 16 qubits) alike."""
+    from quantum_gb300 import _native, workloads
+    rng = np.random.default_rng(17)
+    if case == "layers":
+        w = workloads.expectation_layers(batch=4, n=15, layers=3, seed=2)
+        programs, names, values = w["programs"], w["symbol_names"], w["symbol_values"]
+        psums = w["pauli_sums"]
+    elif case == "grid":
+        w = workloads.grid_fsim(rows=4, cols=4, depth=10, seed=3)
+        programs, names, values = w["programs"], [], np.zeros((1, 0), np.float32)
+        psums = w["pauli_sums"]
+    elif case == "uneven":
+        w = workloads.uneven_batch(batch=24, n_min=4, n_max=16, d_min=4, d_max=12, seed=5)
+        programs, names, values = w["programs"], [], w["symbol_values"]
+        psums = w["pauli_sums"]
+    else:
+        programs, names, values, psums = _batch(rng, [3, 7, 12, 15], 10, n_ops=1)
+    want_e = O.simulate_expectation(programs, names, values, psums)
+    want_s = O.simulate_state(programs, names, values)
+    results = {}
+    for fuse in (True, False):
+        prev = _native.set_gate_fusion(fuse)
+        try:
+            b = ops.Batch(programs, names, psums, kind=ops.KIND_FORWARD)
+        finally:
+            _native.set_gate_fusion(prev)
+        results[fuse] = (b.expectation(values), b.state(values))
+        b.close()
+    for fuse, (e, s) in results.items():
+        scale = max(1.0, float(np.abs(want_e).max()))
+        np.testing.assert_allclose(e, want_e, atol=2e-5 * scale, rtol=0)
+        np.testing.assert_allclose(s, want_s, atol=1e-5, rtol=0)
