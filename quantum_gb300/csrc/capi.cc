@@ -778,11 +778,6 @@ int noisy_expectation_impl(tfqg_batch* b, const float* symbol_values,
         for (int64_t j = 0; j < b->n_ops; ++j) m = std::max(m, reps[i * b->n_ops + j]);
       prefix[i + 1] = prefix[i] + m;
     }
-    for (const DevChannel& ch : b->channels)
-      if (!ch.mixed_unitary && b->any_streamed)
-        throw Error(kUnimplemented,
-                    "Amplitude-damping, reset and phase-damping channels are "
-                    "supported up to 14 qubits.");
     RunArgs a;
     prepare(b, symbol_values, device_buffers, false, 0, s, &a);
     // aux: reps (int32) ; aux2: prefix (int64) + accumulators (double)
@@ -847,11 +842,6 @@ int tfqg_batch_noisy_samples(tfqg_batch* b, const float* symbol_values,
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t obytes = size_t(b->B) * size_t(num_samples) * size_t(b->max_n);
     if (obytes == 0) return 0;  // tfq_noisy_samples.cc:122-124
-    for (const DevChannel& ch : b->channels)
-      if (!ch.mixed_unitary && b->any_streamed)
-        throw Error(kUnimplemented,
-                    "Amplitude-damping, reset and phase-damping channels are "
-                    "supported up to 14 qubits.");
     // one trajectory per sample, rows in order
     std::vector<int64_t> prefix(static_cast<size_t>(b->B) + 1, 0);
     for (int64_t i = 0; i < b->B; ++i) prefix[i + 1] = prefix[i] + num_samples;

@@ -893,10 +893,28 @@ void plan_sequence(const CompiledProgram& p, const std::vector<PlanItem>& items,
                               uint32_t(ops->size()), 0});
     return;
   }
+  // a channel whose branch probabilities are state norms (not mixed-unitary)
+  // needs the whole state: it gets a global-channel pass of its own, and
+  // blocks only its own bit for the passes around it
+  auto global_channel = [&](const PlanItem& it) {
+    return it.seq < 0 && !p.channels[~it.seq].dev.mixed_unitary;
+  };
   while (!remaining.empty()) {
+    if (global_channel(remaining.front())) {
+      const DevOp op = make_op(p, remaining.front(), low_mask(n), backward, chan_bits);
+      passes->push_back(DevPass{0u, uint32_t(ops->size()), uint32_t(ops->size() + 1), 1u});
+      ops->push_back(op);
+      remaining.erase(remaining.begin());
+      continue;
+    }
     uint32_t S = lanes, blocked = 0;
     std::vector<PlanItem> taken, rest;
     for (const auto& it : remaining) {
+      if (global_channel(it)) {
+        rest.push_back(it);
+        blocked |= it.deps;
+        continue;
+      }
       if (it.deps & blocked) {
         rest.push_back(it);
         blocked |= it.deps;

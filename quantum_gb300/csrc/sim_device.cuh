@@ -741,11 +741,25 @@ __device__ __noinline__ void exec_backward(uint32_t s_off, uint32_t l_off, int T
 
 #endif  // TFQG_JIT
 
-// Any channel on local bit t0 of a shared-memory state (qsim
+// Amplitude accessors of a channel: a swizzled shared-memory tile, or a
+// whole state in global memory (read through L2, as tiles are).
+struct SharedAmps {
+  float2* s;
+  __device__ float2 ld(uint32_t i) const { return s[swz(i)]; }
+  __device__ void st(uint32_t i, float2 v) const { s[swz(i)] = v; }
+};
+struct GlobalAmps {
+  float2* g;
+  __device__ float2 ld(uint32_t i) const { return __ldcg(g + i); }
+  __device__ void st(uint32_t i, float2 v) const { __stcg(g + i, v); }
+};
+
+// Any channel on bit t0 of a 2^T-amplitude state (qsim
 // QuantumTrajectorySimulator semantics: mixed-unitary channels draw the
 // branch from fixed probabilities, others from |K_k psi|^2, then renormalize).
-__device__ void op_channel(float2* s, int T, int t0, const DevChannel& ch,
-                           const float2* kraus, double u, double* red) {
+template <class Amps>
+__device__ void apply_channel(Amps A, int T, int t0, const DevChannel& ch,
+                              const float2* kraus, double u, double* red) {
   const uint32_t np = 1u << (T - 1), bit = 1u << t0;
   int k = ch.nk - 1;
   float scale = 1.f;
@@ -758,7 +772,7 @@ __device__ void op_channel(float2* s, int T, int t0, const DevChannel& ch,
     float part[4] = {0.f, 0.f, 0.f, 0.f};
     for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
       uint32_t i0 = ins0(i, t0);
-      float2 a0 = s[swz(i0)], a1 = s[swz(i0 | bit)];
+      float2 a0 = A.ld(i0), a1 = A.ld(i0 | bit);
       for (int j = 0; j < ch.nk; ++j) {
         const float2* K = kraus + (ch.kraus + j) * 4;
         float2 z = make_float2(0.f, 0.f);
@@ -787,11 +801,16 @@ __device__ void op_channel(float2* s, int T, int t0, const DevChannel& ch,
   for (int j = 0; j < 4; ++j) g[j] = make_float2(K[j].x * scale, K[j].y * scale);
   for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) {
     uint32_t i0 = ins0(i, t0);
-    float2 a0 = s[swz(i0)], a1 = s[swz(i0 | bit)];
+    float2 a0 = A.ld(i0), a1 = A.ld(i0 | bit);
     float2 z = make_float2(0.f, 0.f);
-    s[swz(i0)] = cfma(g[1], a1, cfma(g[0], a0, z));
-    s[swz(i0 | bit)] = cfma(g[3], a1, cfma(g[2], a0, z));
+    A.st(i0, cfma(g[1], a1, cfma(g[0], a0, z)));
+    A.st(i0 | bit, cfma(g[3], a1, cfma(g[2], a0, z)));
   }
+}
+
+__device__ void op_channel(float2* s, int T, int t0, const DevChannel& ch,
+                           const float2* kraus, double u, double* red) {
+  apply_channel(SharedAmps{s}, T, t0, ch, kraus, u, red);
 }
 
 struct RowCtx {
@@ -996,6 +1015,21 @@ __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
   const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
   for (uint32_t p = pb; p < pe; ++p) {
     const DevPass ps = b.passes[p];
+    if (ps.global_channel) {
+      if (init && p == pb) {
+        for (uint32_t i = threadIdx.x; i <= all; i += blockDim.x)
+          __stcg(g_psi + i, make_float2(i == 0 ? 1.f : 0.f, 0.f));
+        __syncthreads();
+      }
+      if (MODE == kModeNoisy) {
+        const DevOp h = b.ops[ps.op_begin];
+        const DevChannel ch = b.channels[rc.p.channel_begin + h.gate];
+        const double u = uniform01(a.seed, uint32_t(rc.row), uint32_t(rc.traj), h.gate);
+        apply_channel(GlobalAmps{g_psi}, n, h.t0, ch, b.kraus, u, sm.red);
+      }
+      __syncthreads();
+      continue;
+    }
     build_hi_table(sm.hi, ps.tile_mask);
     __syncthreads();
     const uint32_t outside = all & ~ps.tile_mask;

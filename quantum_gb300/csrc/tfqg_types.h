@@ -104,11 +104,14 @@ struct DevOp {
 static_assert(sizeof(DevOp) == 32, "DevOp layout");
 
 // A pass streams every tile of the state once: the tile holds the 2^T
-// amplitudes whose index bits outside `tile_mask` are fixed.
+// amplitudes whose index bits outside `tile_mask` are fixed.  A
+// global-channel pass (streamed noisy rows) instead applies its one OP_CHAN,
+// whose t0 is a global bit, to the whole state in global memory: its Kraus
+// branch probabilities are norms over the whole state, not over a tile.
 struct DevPass {
   uint32_t tile_mask;
   uint32_t op_begin, op_end;
-  uint32_t pad;
+  uint32_t global_channel;  // 1 for a global-channel pass
 };
 
 // A Pauli term: P|y> = i^ny (-1)^popc(y & zy) |y ^ flip>  (bits).

@@ -463,3 +463,31 @@ def test_fused_forward_plans_match_unfused_and_oracle(case):
         scale = max(1.0, float(np.abs(want_e).max()))
         np.testing.assert_allclose(e, want_e, atol=2e-5 * scale, rtol=0)
         np.testing.assert_allclose(s, want_s, atol=1e-5, rtol=0)
+
+
+@pytest.mark.parametrize("n,channels", [(16, ["AD", "GAD", "RST", "PD", "DP"]),
+                                        (15, ["AD", "PD", "BF", "GAD"])])
+def test_streamed_non_unitary_channels_vs_density_matrix(n, channels):
+    """Channels whose branch probabilities are state norms (amplitude and
+    phase damping, reset, GAD) on streamed states (> 14 qubits): a 6-qubit
+    noisy circuit on qubits spread over high, middle and low index bits,
+    embedded in n qubits whose other qubits only get rotations. Observables
+    on the active qubits must match the 6-qubit exact density matrix."""
+    rng = np.random.default_rng(900 + n)
+    qs = S.GridQubit.rect(1, n)
+    active = [qs[i] for i in (0, 1, n // 2 - 1, n // 2 + 2, n - 2, n - 1)]
+    idle = [q for q in qs if q not in active]
+    names = ["a", "b"]
+    c = random_circuit(active, 6, rng, names, p_control=0.2,
+                       channels=list(channels), p_channel=0.45)
+    full = S.Circuit([[S.rx(q, float(rng.uniform(0, 3))) for q in idle]] + c.moments
+                     + [[S.ry(q, float(rng.uniform(0, 3))) for q in idle]])
+    psums = [[S.serialize_paulisum([(1.0, [(q, "Z")]) for q in active]),
+              random_paulisum(active, rng)]]
+    vals = rng.uniform(-1, 1, size=(1, 2)).astype(np.float32)
+    R = 12000
+    got = ops.noisy_expectation([S.serialize_circuit(full)], names, vals, psums,
+                                np.full((1, 2), R, np.int32), seed=11)
+    want = O.noisy_expectation_exact([S.serialize_circuit(c)], names, vals, psums)
+    bound = 5 * len(active) / np.sqrt(R) + 1e-4
+    np.testing.assert_allclose(got, want, atol=bound, rtol=0)
