@@ -964,14 +964,29 @@ __device__ __forceinline__ uint32_t deposit(uint32_t t, uint32_t mask) {
   return r;
 }
 
-__device__ void tile_load(float2* dst, const float2* src, const uint32_t* hi,
-                          uint32_t base) {
+// Tile loads are asynchronous copies (cp.async) from global to shared
+// memory: every load of a tile is in flight at once and none holds a
+// register.  A pair of amplitudes (2k, 2k+1) lands in one aligned 16-byte
+// slot, possibly swapped (swz(2k+1) == swz(2k) ^ 1), so each amplitude is an
+// 8-byte copy.  tile_load_async issues; tile_load_wait (then a barrier)
+// completes every copy this thread issued.
+__device__ __forceinline__ void cp_async8(float2* smem_dst, const float2* gsrc) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc)
+               : "memory");
+}
+
+__device__ __forceinline__ void tile_load_wait() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+__device__ void tile_load_async(float2* dst, const float2* src, const uint32_t* hi,
+                                uint32_t base) {
   const uint32_t n2 = 1u << (kTile - 1);
   for (uint32_t k = threadIdx.x; k < n2; k += blockDim.x) {
-    uint32_t g = tile_global(hi, 2 * k) | base;
-    float4 v = __ldcg(reinterpret_cast<const float4*>(src + g));
-    dst[swz(2 * k)] = make_float2(v.x, v.y);
-    dst[swz(2 * k + 1)] = make_float2(v.z, v.w);
+    const float2* g = src + (tile_global(hi, 2 * k) | base);
+    cp_async8(dst + swz(2 * k), g);
+    cp_async8(dst + swz(2 * k + 1), g + 1);
   }
 }
 
@@ -1037,8 +1052,9 @@ __device__ void run_passes(const BatchDevice& b, const RunArgs& a,
     for (uint32_t t = t0; t < ntiles; t += tstride) {
       const uint32_t base = deposit(t, outside);
       if (init && p == pb) tile_zero(sm.psi, base == 0);
-      else tile_load(sm.psi, g_psi, sm.hi, base);
-      if (MODE == kModeAdjoint && g_lam) tile_load(sm.lam, g_lam, sm.hi, base);
+      else tile_load_async(sm.psi, g_psi, sm.hi, base);
+      if (MODE == kModeAdjoint && g_lam) tile_load_async(sm.lam, g_lam, sm.hi, base);
+      tile_load_wait();
       __syncthreads();
       run_ops<MODE, Exec>(b, a, sm, rc, ps.op_begin, ps.op_end, sm.psi, sm.lam, kTile,
                     base, kc);
@@ -1159,7 +1175,8 @@ __device__ void measure_passes(const BatchDevice& b, const RunArgs& a,
       uint32_t base = 0;
       if (!resident) {
         base = deposit(tile, outside);
-        tile_load(sm.psi, g_psi, sm.hi, base);
+        tile_load_async(sm.psi, g_psi, sm.hi, base);
+        tile_load_wait();
         __syncthreads();
       }
       measure_tile(sm, nt, N, base, resident);
@@ -1284,8 +1301,9 @@ __device__ void lambda_passes(const BatchDevice& b, const RunArgs& a,
       uint32_t base = 0;
       if (!resident) {
         base = deposit(tile, outside);
-        tile_load(sm.psi, g_psi, sm.hi, base);
-        if (!first) tile_load(sm.lam, g_lam, sm.hi, base);
+        tile_load_async(sm.psi, g_psi, sm.hi, base);
+        if (!first) tile_load_async(sm.lam, g_lam, sm.hi, base);
+        tile_load_wait();
         __syncthreads();
       }
       lambda_tile(sm, nt, N, base, resident, first && !resident);
@@ -1620,7 +1638,8 @@ __device__ __forceinline__ void wide_measure_body(const BatchDevice& b, const Ru
   const uint32_t ntiles = 1u << (n - kTile);
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const uint32_t base = deposit(t, outside);
-    tile_load(sm.psi, psi, sm.hi, base);
+    tile_load_async(sm.psi, psi, sm.hi, base);
+    tile_load_wait();
     __syncthreads();
     measure_tile(sm, nt, 1u << kTile, base, false);
     __syncthreads();
