@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the one-shot C-ABI leg")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="circuits per GPU (default 256; smaller only for profiling)")
+    ap.add_argument("--c4-grid", default="5x6",
+                    help="rows x cols of the C4 grid circuit (5x6 = 30 qubits; a smaller "
+                         "grid gives a profiling case of the same kernels)")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default): the headline expectation + adjoint line; "
                          "c1, c3, c4, c5: the other benchmark configurations, "
@@ -200,6 +203,55 @@ CONFIGS = {
 }
 
 
+def config_roofline(wl, w, batch, ms, clk, units):
+    """Roofline of one configuration step (the whole call, all its launches).
+
+    C4 is bound by HBM: every forward pass reads and writes the 2^n-amplitude
+    complex64 state once and the measurement pass reads it once. C1 and C5
+    are bound by the FP32 pipe: gates counted as dense 2^k x 2^k matvecs,
+    8 * 2^k * 2^n flop each, plus 8 * 2^n per Pauli term; a trajectory counts
+    the Kraus branches it applies (p x channels expected; the identity
+    branch of a depolarizing channel is no work). C3 mixes both bounds and
+    reports none."""
+    import torch
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    n = w.get("n")
+    c = w.get("counts")
+    if wl == "c4":
+        from quantum_gb300 import _native
+        fwd, meas = _native.row_sweeps(batch._h, 0)
+        nbytes = (fwd * 16 + meas * 8) * 2 ** n
+        peak = peaks.get("hbm_gbs") or 6800.0
+        achieved = nbytes * units / (ms / 1e3) / 1e9
+        return {"bound": "hbm", "kernel": "wide passes + measurement (whole call)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None,
+                "algorithmic": f"{fwd} forward passes x 16 B + {meas} measurement "
+                               f"pass(es) x 8 B, times 2^{n} amplitudes",
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"
+                               if peaks.get("hbm_gbs") else "fallback 6800 GB/s"}
+    if wl in ("c1", "c5") and c:
+        per = c["one"] * 16 + c["two"] * 32 + c["terms"] * 8
+        if wl == "c5":
+            per += w["p"] * c["channels"] * 16
+        flop = per * 2 ** n * units
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        mhz = clk.get("sm_mhz") or 2070.0
+        peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+        achieved = flop / (ms / 1e3) / 1e12
+        return {"bound": "fp32", "kernel": "build matrices + simulation (whole call)",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "algorithmic": f"{per * 2 ** n / 1e6:.2f} MFLOP per "
+                               f"{'trajectory' if wl == 'c5' else 'circuit'} x {units}",
+                "peak_source": f"derived: {sms} SMs x 128 FP32 lanes x 2 flop x {mhz:.0f} MHz"}
+    return None
+
+
 def run_config(args):
     """One JSON line for configuration c1 / c3 / c4 / c5: device time per
     step (CUDA events, inputs resident, L2 flushed between steps)."""
@@ -215,7 +267,8 @@ def run_config(args):
         w = workloads.uneven_batch(4096, 4, 20, 5, 40, seed=1)
         units, unit = 4096, "circuits/s"
     elif wl == "c4":
-        w = workloads.grid_fsim(5, 6, 24, seed=1)
+        gr, gc = (int(x) for x in args.c4_grid.split("x"))
+        w = workloads.grid_fsim(gr, gc, 24, seed=1)
         units, unit = 1, "circuits/s"
     else:
         w = workloads.noisy_brickwall(64, 14, 15, 0.01, seed=1)
@@ -254,10 +307,12 @@ def run_config(args):
     line = {"metric": f"{wl} throughput", "value": units / (ms / 1e3), "unit": unit,
             "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "dtype": "c64 (f32 state, f64 reductions)",
-            "data": "synthetic (seeded)", "config": {"workload": wl, "what": CONFIGS[wl]},
+            "data": "synthetic (seeded)", "config": {"workload": wl, "what": CONFIGS[wl],
+                       **({"grid": args.c4_grid} if wl == "c4" else {})},
             "host_parse_plan_s": parse_s, "clocks": clk,
             "specialized": sorted(__import__("quantum_gb300")._native.batch_specialization(
                 batch._h)[1])}
+    line["roofline"] = config_roofline(wl, w, batch, ms, clk, units)
     if wl == "c1":
         from oracle import tfq_oracle as O
         rows = [0, 1]

@@ -233,6 +233,18 @@ def forward_plan_gates(handle, row, row_values):
     return out
 
 
+def row_sweeps(handle, row):
+    """(forward passes, measurement passes) of a row's plan: each forward
+    pass reads and writes the state once, each measurement pass reads it."""
+    f = lib().tfqg_internal_row_sweeps
+    f.argtypes = [c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
+                  ctypes.POINTER(ctypes.c_int32)]
+    f.restype = ctypes.c_int
+    a, m = ctypes.c_int32(), ctypes.c_int32()
+    check(f(handle, int(row), ctypes.byref(a), ctypes.byref(m)))
+    return a.value, m.value
+
+
 def batch_wide_rows(handle):
     f = lib().tfqg_internal_batch_wide_rows
     f.argtypes = [c_void_p]

@@ -1329,6 +1329,19 @@ int tfqg_internal_batch_passes(void* batch, int32_t* fwd, int32_t* bwd,
   return 0;
 }
 
+// State sweeps of row `row`: forward passes (each reads and writes the
+// state once) and measurement passes (each reads it once).
+int tfqg_internal_row_sweeps(void* batch, int64_t row, int32_t* fwd, int32_t* meas) {
+  const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
+  if (!b || row < 0 || row >= int64_t(b->rows.size()) || !fwd || !meas)
+    return kInvalidArgument;
+  const DevRow& r = b->rows[size_t(row)];
+  const DevProgram& p = b->programs[r.program];
+  *fwd = int32_t(p.fwd_pass_end - p.fwd_pass_begin);
+  *meas = int32_t(r.meas_end - r.meas_begin);
+  return 0;
+}
+
 // Sub-pass statistics of program 0: number of sub-pass headers and ops in
 // the forward and backward instruction streams (planner diagnostics).
 int tfqg_internal_batch_subpasses(void* batch, int32_t* fwd_subs,

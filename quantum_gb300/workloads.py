@@ -75,8 +75,11 @@ def expectation_layers(batch=32, n=12, layers=20, seed=1):
                                  for i in range(n - 1)]),
            S.serialize_paulisum([(1.0, [(q, "X")]) for q in qs]),
            S.serialize_paulisum(rand_terms)]
+    n_cz = sum(len(range(layer % 2, n - 1, 2)) for layer in range(layers))
+    n_terms = n + (n - 1) + n + len(rand_terms)
     return dict(programs=[prog] * batch, symbol_names=names, symbol_values=values,
-                pauli_sums=[list(ops) for _ in range(batch)], n=n)
+                pauli_sums=[list(ops) for _ in range(batch)], n=n,
+                counts=dict(one=3 * n * layers, two=n_cz, channels=0, terms=n_terms))
 
 
 def uneven_batch(batch=4096, n_min=4, n_max=20, d_min=5, d_max=40, seed=1):
@@ -132,9 +135,12 @@ def noisy_brickwall(batch=64, n=14, depth=15, p=0.01, seed=1):
             moments.append([S.depolarize(q, p) for a, b in cz for q in (a, b)])
         programs.append(S.serialize_circuit(S.Circuit(moments)))
     ps = S.serialize_paulisum([(1.0, [(q, "Z")]) for q in qs])
+    n_cz = sum(len(range(layer % 2, n - 1, 2)) for layer in range(depth))
     return dict(programs=programs, symbol_names=[],
                 symbol_values=np.zeros((batch, 0), np.float32),
-                pauli_sums=[[ps] for _ in range(batch)])
+                pauli_sums=[[ps] for _ in range(batch)], n=n, p=p,
+                counts=dict(one=2 * n * depth, two=n_cz,
+                            channels=2 * n * depth + 2 * n_cz, terms=n))
 
 
 def grid_fsim(rows=5, cols=6, depth=24, seed=1):
@@ -172,6 +178,8 @@ def grid_fsim(rows=5, cols=6, depth=24, seed=1):
                                float(rng.uniform(0.4, 0.6))) for a, b in pairs])
     prog = S.serialize_circuit(S.Circuit(moments))
     ps = S.serialize_paulisum([(1.0, [(q, "Z")]) for q in qs])
+    n_two = sum(len(m) for m in moments[1::2])
     return dict(programs=[prog], symbol_names=[],
                 symbol_values=np.zeros((1, 0), np.float32), pauli_sums=[[ps]],
-                n=len(qs), depth=depth)
+                n=len(qs), depth=depth,
+                counts=dict(one=len(qs) * depth, two=n_two, channels=0, terms=len(qs)))
