@@ -520,10 +520,65 @@ void run_wide(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a,
   }
 }
 
+// Adjoint of the wide rows, one row after another on stream s: forward
+// passes over the whole grid, lambda by measurement passes, backward passes
+// whose CTAs add gradient-slot sums into a per-row double buffer, finalize.
+void run_wide_adjoint(tfqg_batch* b, const BatchDevice& bd, RunArgs* a, cudaStream_t s) {
+  const int dev = b->device;
+  const int state_amps = 1 << kStreamTileBits;
+  const size_t fsmem = sim_smem_bytes(kModeState, -1, true, 0);
+  const size_t asmem = sim_smem_bytes(kModeAdjoint, -1, true, b->max_grads);
+  if (asmem > 227 * 1024)
+    throw Error(kResourceExhausted, "shared memory request too large");
+  cudaKernel_t jk = jit_kernel(b, kJitWide, dev);
+  int fgrid = jk ? jit_grid(jk, fsmem, dev, kWideThreads)
+                 : occupancy_grid(sim_kernel_wide(), kWideThreads, fsmem, dev);
+  const int lgrid = occupancy_grid(sim_kernel_wide_lambda(), kSimThreads, asmem, dev);
+  const int bgrid = occupancy_grid(sim_kernel_wide_backward(), kSimThreads, asmem, dev);
+  const size_t N = size_t(1) << b->max_wide_n;
+  b->wide_state.reserve(2 * N * sizeof(float2), dev);
+  float2* psi = static_cast<float2*>(b->wide_state.p);
+  float2* lam = psi + N;
+  b->wide_acc.reserve(size_t(std::max(b->max_grads, 1)) * sizeof(double), dev);
+  double* gacc = static_cast<double*>(b->wide_acc.p);
+  for (const int32_t row : b->wide_rows) {
+    const DevRow& r = b->rows[size_t(row)];
+    const DevProgram& p = b->programs[r.program];
+    for (uint32_t q = p.fwd_pass_begin; q < p.fwd_pass_end; ++q) {
+      const int init = q == p.fwd_pass_begin ? 1 : 0;
+      if (jk) {
+        cudaError_t e = jit_launch_wide(jk, bd, *a, row, int(q), init, psi, fgrid, fsmem,
+                                        state_amps, s);
+        if (e == cudaSuccess) continue;
+        cudaGetLastError();
+        b->jit_error = std::string("specialized launch rejected: ") + cudaGetErrorString(e);
+        b->jit_mode = -1;
+        jk = nullptr;
+        fgrid = occupancy_grid(sim_kernel_wide(), kWideThreads, fsmem, dev);
+      }
+      TFQG_CUDA(sim_launch_wide(bd, *a, row, int(q), init, psi, fgrid, fsmem, state_amps, s));
+    }
+    if (r.meas_begin == r.meas_end)
+      TFQG_CUDA(cudaMemsetAsync(lam, 0, (size_t(1) << p.n) * sizeof(float2), s));
+    for (uint32_t mp = r.meas_begin; mp < r.meas_end; ++mp)
+      TFQG_CUDA(sim_launch_wide_lambda(bd, *a, row, int(mp), mp == r.meas_begin ? 1 : 0,
+                                       psi, lam, lgrid, asmem, state_amps, s));
+    if (p.num_grads == 0) continue;
+    TFQG_CUDA(cudaMemsetAsync(gacc, 0, size_t(p.num_grads) * sizeof(double), s));
+    for (uint32_t q = p.bwd_pass_begin; q < p.bwd_pass_end; ++q)
+      TFQG_CUDA(sim_launch_wide_backward(bd, *a, row, int(q), psi, lam, gacc, bgrid, asmem,
+                                         state_amps, s));
+    TFQG_CUDA(launch_wide_grad_finalize(bd, *a, row, gacc, s));
+  }
+}
+
 int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
-  // forward modes: wide rows run on the whole grid, the rest in the queue
+  // forward modes: wide rows run on the whole grid, the rest in the queue;
+  // so does the adjoint of tfq_adj_grad (not the inner-product gradient,
+  // whose lambda comes from a buffer)
   const bool fwd = mode == kModeExpect || mode == kModeState || mode == kModeSample;
-  const bool split = fwd && !b->wide_rows.empty();
+  const bool wide_adj = mode == kModeAdjoint && b->kind != TFQG_KIND_INNER && !a->lambda_init;
+  const bool split = (fwd || wide_adj) && !b->wide_rows.empty();
   BatchDevice bd = b->bd;
   if (split) {
     bd.order = b->d_order_fwd;
@@ -567,7 +622,8 @@ int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
     }
     if (!launched) TFQG_CUDA(launch_simulate(mode, bd, *a, grid, smem, state_amps, s));
   }
-  if (split) run_wide(b, mode, bd, a, s);
+  if (split && wide_adj) run_wide_adjoint(b, bd, a, s);
+  else if (split) run_wide(b, mode, bd, a, s);
   return grid;
 }
 

@@ -134,6 +134,19 @@ const void* sim_kernel_wide();
 cudaError_t sim_launch_wide(const BatchDevice& b, const RunArgs& a, int row, int pass,
                             int init, float2* psi, int grid, size_t smem,
                             int state_amps, cudaStream_t s);
+// Adjoint of a wide row: lambda accumulation per measurement pass, backward
+// passes adding gradient-slot sums into gacc (doubles), then the finalize
+// into out_f.  psi and lam are the row's two 2^n states.
+const void* sim_kernel_wide_lambda();
+const void* sim_kernel_wide_backward();
+cudaError_t sim_launch_wide_lambda(const BatchDevice& b, const RunArgs& a, int row, int mp,
+                                   int first, const float2* psi, float2* lam, int grid,
+                                   size_t smem, int state_amps, cudaStream_t s);
+cudaError_t sim_launch_wide_backward(const BatchDevice& b, const RunArgs& a, int row,
+                                     int pass, float2* psi, float2* lam, double* gacc,
+                                     int grid, size_t smem, int state_amps, cudaStream_t s);
+cudaError_t launch_wide_grad_finalize(const BatchDevice& b, const RunArgs& a, int row,
+                                      const double* gacc, cudaStream_t s);
 const void* wide_measure_kernel_ptr();
 cudaError_t launch_wide_measure(const BatchDevice& b, const RunArgs& a, int row, int mp,
                                 const float2* psi, double* wacc, int term0, int grid,

@@ -1649,6 +1649,70 @@ __device__ __forceinline__ void wide_measure_body(const BatchDevice& b, const Ru
     if (sm.macc[i] != 0.0) atomicAdd(dst + i, sm.macc[i]);
 }
 
+// Wide rows in the adjoint: psi and lambda (2^n amplitudes each) live in
+// global memory and each pass is one launch over the whole grid, as in the
+// forward wide path.
+
+// lambda += sum_t w_t P_t psi over the terms of measurement pass `mp` of
+// wide row `row` (lambda starts from zero when `first`); this CTA's tiles.
+__device__ __forceinline__ void wide_lambda_body(const BatchDevice& b, const RunArgs& a,
+                                                 int row, int mp, int first,
+                                                 const float2* psi, float2* lam,
+                                                 int state_amps) {
+  const Smem sm = carve_smem<kModeAdjoint>(state_amps, 2);
+  RowCtx rc;
+  rc.row = row;
+  rc.traj = 0;
+  rc.r = b.rows[row];
+  rc.p = b.programs[rc.r.program];
+  const int n = rc.p.n;
+  const DevMeas M = b.meas[mp];
+  const int nt = int(M.end - M.begin);
+  stage_terms(b, a, sm, rc, M, true);
+  build_hi_table(sm.hi, M.tile_mask);
+  __syncthreads();
+  const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+  const uint32_t outside = all & ~M.tile_mask;
+  const uint32_t ntiles = 1u << (n - kTile);
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t base = deposit(t, outside);
+    tile_load_async(sm.psi, psi, sm.hi, base);
+    if (!first) tile_load_async(sm.lam, lam, sm.hi, base);
+    tile_load_wait();
+    __syncthreads();
+    lambda_tile(sm, nt, 1u << kTile, base, false, first != 0);
+    __syncthreads();
+    tile_store(lam, sm.lam, sm.hi, base);
+    __syncthreads();
+  }
+}
+
+// Backward pass `pass` of wide row `row` over psi and lambda: this CTA's
+// tiles.  Its gradient-slot sums (shared memory) are added to gacc[slot]
+// with double atomics once, at the end.
+template <class Exec>
+__device__ __forceinline__ void wide_backward_body(const BatchDevice& b, const RunArgs& a,
+                                                   int row, int pass, float2* psi,
+                                                   float2* lam, double* gacc,
+                                                   int state_amps) {
+  const Smem sm = carve_smem<kModeAdjoint>(state_amps, 2);
+  RowCtx rc;
+  rc.row = row;
+  rc.traj = 0;
+  rc.r = b.rows[row];
+  rc.p = b.programs[rc.r.program];
+  for (int k = threadIdx.x; k < rc.p.num_grads; k += blockDim.x) sm.grad[k] = 0.0;
+  __syncthreads();
+  int kc = 0;
+  run_passes<kModeAdjoint, Exec>(b, a, sm, rc, uint32_t(pass), uint32_t(pass) + 1, psi,
+                                 lam, false, kc, blockIdx.x, gridDim.x);
+  __syncthreads();
+  for (int k = threadIdx.x; k < rc.p.num_grads; k += blockDim.x) {
+    const double v = sm.grad[k];
+    if (v != 0.0) atomicAdd(gacc + k, v);
+  }
+}
+
 #ifndef TFQG_JIT
 // Sub-passes run by the precompiled interpreter.
 struct InterpExec {

@@ -1,5 +1,7 @@
 """Wide rows: states too large for one CTA, simulated by the whole grid one
-launch per pass (forward modes). The wide threshold is lowered here so that
+launch per pass (forward modes and the adjoint gradient: forward, lambda and
+backward passes, gradient slots summed across CTAs). The wide threshold is
+lowered here so that
 15..18-qubit rows take the path at oracle-checkable sizes. Narrow rows of
 the same batch still go through the persistent kernel. One 22-qubit row
 checks the default threshold. Tolerances as in test_gpu_parity.py."""
@@ -51,7 +53,7 @@ def test_expectation_mixed_wide_and_narrow(wide_from_15, jit):
     np.testing.assert_allclose(got, want, atol=8e-5, rtol=0)
 
 
-def test_adjoint_batch_runs_wide_forward_and_queued_gradient(wide_from_15):
+def test_adjoint_batch_wide_row_beside_a_queued_row(wide_from_15):
     rng = np.random.default_rng(3)
     programs, names, values, psums = _inputs(rng, [16, 4], n_moments=4)
     b = ops.Batch(programs, names, psums, kind=ops.KIND_ADJOINT)
@@ -108,3 +110,43 @@ def test_default_threshold_22_qubits():
     np.testing.assert_allclose(b.expectation(values),
                                O.simulate_expectation(programs, names, values, psums),
                                atol=8e-5, rtol=0)
+
+
+@pytest.mark.parametrize("rule", [ops.GRAD_REFERENCE_FD, ops.GRAD_EXACT])
+def test_wide_adjoint_gradient_mixed_batch(wide_from_15, rule):
+    """Gradients of wide rows (15..17 qubits, symbols shared by several
+    gates, controlled gates) beside narrow rows, against the oracle."""
+    rng = np.random.default_rng(40 + rule)
+    nqs = [16, 5, 15, 17, 9]
+    programs, names, values, psums = _inputs(rng, nqs, n_moments=5, n_ops=2)
+    b = ops.Batch(programs, names, psums, kind=ops.KIND_ADJOINT)
+    assert _native.batch_wide_rows(b._h) == 3
+    dg = rng.normal(size=(len(nqs), 2)).astype(np.float32)
+    got = b.adj_grad(values, dg, rule)
+    want = O.adj_grad(programs, names, values, psums, dg,
+                      grad_rule="fd" if rule == ops.GRAD_REFERENCE_FD else "exact")
+    np.testing.assert_allclose(got, want, atol=2e-5 * max(1.0, np.abs(want).max()), rtol=0)
+
+
+def test_wide_adjoint_without_terms_is_zero(wide_from_15):
+    """A wide row whose Pauli sums are empty has lambda = 0: zero gradient."""
+    rng = np.random.default_rng(5)
+    qs = S.GridQubit.rect(1, 16)
+    names = ["a", "b"]
+    prog = S.serialize_circuit(random_circuit(qs, 4, rng, names, p_control=0.0))
+    empty = S.serialize_paulisum([])
+    b = ops.Batch([prog], names, [[empty]], kind=ops.KIND_ADJOINT)
+    assert _native.batch_wide_rows(b._h) == 1
+    got = b.adj_grad(np.array([[0.3, -0.7]], np.float32), np.ones((1, 1), np.float32))
+    np.testing.assert_array_equal(got, np.zeros((1, 2), np.float32))
+
+
+def test_wide_adjoint_default_threshold_22_qubits():
+    rng = np.random.default_rng(23)
+    programs, names, values, psums = _inputs(rng, [22, 4], n_moments=2, n_ops=1)
+    b = ops.Batch(programs, names, psums, kind=ops.KIND_ADJOINT)
+    assert _native.batch_wide_rows(b._h) == 1
+    dg = np.ones((2, 1), np.float32)
+    want = O.adj_grad(programs, names, values, psums, dg)
+    np.testing.assert_allclose(b.adj_grad(values, dg), want,
+                               atol=2e-5 * max(1.0, np.abs(want).max()), rtol=0)
