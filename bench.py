@@ -321,7 +321,56 @@ def run_config(args):
                                       [w["pauli_sums"][i] for i in rows])
         line["accuracy"] = {"max_abs": float(np.abs(out.cpu().numpy()[rows] - want).max()),
                             "rows": len(rows)}
+    if wl == "c4":
+        # a 30-qubit complex128 oracle run is out of reach: the fused plan is
+        # checked against the unfused one here (the 4x4 grid is pinned to the
+        # oracle by the GPU parity tests)
+        from quantum_gb300 import _native
+        fused = float(out.cpu().numpy()[0, 0])
+        batch.close()
+        prev = _native.set_gate_fusion(False)
+        try:
+            ub = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
+        finally:
+            _native.set_gate_fusion(prev)
+        unfused = float(ub.expectation(vals).cpu().numpy()[0, 0])
+        ub.close()
+        line["accuracy"] = {"sum_z_fused": fused, "sum_z_unfused": unfused,
+                            "abs_diff_fused_vs_unfused": abs(fused - unfused)}
+    if wl == "c3":
+        line["per_n_bucket"] = c3_buckets(w, dev)
     print(json.dumps(line), flush=True)
+
+
+def c3_buckets(w, dev):
+    """Circuits/s of the C3 step (expectation + 1000 samples) per qubit-count
+    bucket: each bucket's rows as a batch of their own, device time of one
+    step after one warm-up step."""
+    import torch
+    from quantum_gb300 import ops
+    out = []
+    rows_n = w["n_per_row"]
+    for lo, hi in ((4, 8), (9, 12), (13, 16), (17, 20)):
+        rows = [i for i, n in enumerate(rows_n) if lo <= n <= hi]
+        if not rows:
+            continue
+        b = ops.Batch([w["programs"][i] for i in rows], [], [w["pauli_sums"][i] for i in rows],
+                      ops.KIND_FORWARD)
+        vals = torch.zeros((len(rows), 0), device=dev)
+        b.expectation(vals)
+        b.samples(vals, 1000, seed=1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.expectation(vals)
+        b.samples(vals, 1000, seed=2)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out.append({"n": f"{lo}-{hi}", "circuits": len(rows), "ms": ms,
+                    "circuits_per_s": len(rows) / (ms / 1e3)})
+        b.close()
+    return out
 
 
 def main():

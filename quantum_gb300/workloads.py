@@ -88,9 +88,10 @@ def uneven_batch(batch=4096, n_min=4, n_max=20, d_min=5, d_max=40, seed=1):
     qubit, then random disjoint pairs with CZ or ISWAP^t (t ~ U[0, 1]).
     Observable sum_i Z_i."""
     rng = np.random.default_rng(seed)
-    programs, psums = [], []
+    programs, psums, ns = [], [], []
     for _ in range(batch):
         n = int(rng.integers(n_min, n_max + 1))
+        ns.append(n)
         depth = int(rng.integers(d_min, d_max + 1))
         qs = S.GridQubit.rect(1, n)
         moments = []
@@ -113,7 +114,8 @@ def uneven_batch(batch=4096, n_min=4, n_max=20, d_min=5, d_max=40, seed=1):
         programs.append(S.serialize_circuit(S.Circuit(moments)))
         psums.append([S.serialize_paulisum([(1.0, [(q, "Z")]) for q in qs])])
     return dict(programs=programs, symbol_names=[],
-                symbol_values=np.zeros((batch, 0), np.float32), pauli_sums=psums)
+                symbol_values=np.zeros((batch, 0), np.float32), pauli_sums=psums,
+                n_per_row=ns)
 
 
 def noisy_brickwall(batch=64, n=14, depth=15, p=0.01, seed=1):
