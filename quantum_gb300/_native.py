@@ -233,6 +233,25 @@ def forward_plan_gates(handle, row, row_values):
     return out
 
 
+def program_cache(on=None):
+    """Compiled-program cache: on=True/False switches it (False also empties
+    it), None leaves it. Returns (enabled before the call, hits, misses)."""
+    f = lib().tfqg_internal_program_cache
+    f.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    f.restype = ctypes.c_int
+    h, m = ctypes.c_int64(), ctypes.c_int64()
+    prev = f(-1 if on is None else int(bool(on)), ctypes.byref(h), ctypes.byref(m))
+    return bool(prev), h.value, m.value
+
+
+def batch_fingerprint(handle):
+    """FNV-1a hash of a batch's packed host tables."""
+    f = lib().tfqg_internal_batch_fingerprint
+    f.argtypes = [c_void_p]
+    f.restype = ctypes.c_uint64
+    return int(f(handle))
+
+
 def row_sweeps(handle, row):
     """(forward passes, measurement passes) of a row's plan: each forward
     pass reads and writes the state once, each measurement pass reads it."""

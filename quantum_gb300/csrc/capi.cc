@@ -56,6 +56,129 @@ struct Str {
 
 std::string make_key(const char* p, int64_t n) { return std::string(p, size_t(n)); }
 
+// Key of a serialized proto in the batch's dedup maps: a view of the
+// caller's bytes (valid while the batch is built) and a tag (-1, or the
+// reference program of a paired program).  Equality is exact (same
+// pointer, or memcmp); the hash reads the length, the first and last 256
+// bytes and 64 evenly spaced words, so that a batch of one circuit repeated
+// thousands of times is not hashed in full per row.
+struct ProtoKey {
+  const char* p;
+  size_t n;
+  int tag;
+  bool operator==(const ProtoKey& o) const {
+    return n == o.n && tag == o.tag && (p == o.p || memcmp(p, o.p, n) == 0);
+  }
+};
+
+struct ProtoKeyHash {
+  size_t operator()(const ProtoKey& k) const {
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ (uint64_t(k.n) * 0xBF58476D1CE4E5B9ull) ^
+                 uint64_t(int64_t(k.tag));
+    auto mix = [&h](const char* q, size_t m) {
+      uint64_t w = 0;
+      memcpy(&w, q, m < 8 ? m : 8);
+      h ^= w;
+      h *= 0xFF51AFD7ED558CCDull;
+      h ^= h >> 33;
+    };
+    if (k.n <= 1024) {
+      for (size_t i = 0; i < k.n; i += 8) mix(k.p + i, k.n - i);
+    } else {
+      for (size_t i = 0; i < 256; i += 8) mix(k.p + i, 8);
+      for (size_t i = k.n - 256; i < k.n; i += 8) mix(k.p + i, k.n - i);
+      const size_t step = (k.n - 8) / 64;
+      for (size_t j = 0; j < 64; ++j) mix(k.p + j * step, 8);
+    }
+    return size_t(h);
+  }
+};
+
+// Process-wide cache of compiled and planned programs (a training loop sends
+// the same serialized circuits every step).  An entry is keyed exactly by
+// the program bytes, the symbol names in column order, the job kind and the
+// fusion setting: everything compile_program and plan_program read.  Only
+// programs that compiled without error are stored, so a cached program
+// raises no error and the order of the batch's errors is unchanged.
+struct ProgramCacheEntry {
+  std::string bytes;
+  std::string names;  // length-prefixed symbol names, column order
+  int job = 0;
+  bool fuse = false;
+  bool empty = false;  // no moments: expectation -2 (#679)
+  CompiledProgram cp;
+  std::unordered_map<std::string, int> index;
+  size_t cost = 0;
+  uint64_t stamp = 0;
+};
+
+constexpr size_t kProgramCacheBytes = size_t(256) << 20;
+constexpr size_t kProgramCacheEntries = 2048;
+std::mutex g_pc_mu;
+std::unordered_multimap<uint64_t, std::shared_ptr<const ProgramCacheEntry>> g_pc;
+uint64_t g_pc_clock = 0;
+size_t g_pc_bytes = 0;
+std::atomic<int> g_pc_on{1};
+std::atomic<int64_t> g_pc_hits{0}, g_pc_misses{0};
+
+uint64_t program_cache_hash(const char* p, size_t n, const std::string& names, int job,
+                            bool fuse) {
+  uint64_t h = ProtoKeyHash()(ProtoKey{p, n, -1});
+  h ^= ProtoKeyHash()(ProtoKey{names.data(), names.size(), job * 2 + (fuse ? 1 : 0)}) +
+       0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+  return h;
+}
+
+std::shared_ptr<const ProgramCacheEntry> program_cache_find(const char* p, size_t n,
+                                                            const std::string& names,
+                                                            int job, bool fuse) {
+  if (!g_pc_on.load()) return nullptr;
+  const uint64_t h = program_cache_hash(p, n, names, job, fuse);
+  std::lock_guard<std::mutex> lk(g_pc_mu);
+  auto range = g_pc.equal_range(h);
+  for (auto it = range.first; it != range.second; ++it) {
+    const ProgramCacheEntry& e = *it->second;
+    if (e.job == job && e.fuse == fuse && e.bytes.size() == n && e.names == names &&
+        memcmp(e.bytes.data(), p, n) == 0) {
+      const_cast<ProgramCacheEntry&>(e).stamp = ++g_pc_clock;
+      g_pc_hits.fetch_add(1);
+      return it->second;
+    }
+  }
+  g_pc_misses.fetch_add(1);
+  return nullptr;
+}
+
+void program_cache_insert(std::shared_ptr<ProgramCacheEntry> e) {
+  if (!g_pc_on.load()) return;
+  const CompiledProgram& cp = e->cp;
+  e->cost = e->bytes.size() + e->names.size() + cp.gates.size() * sizeof(GateTemplate) +
+            (cp.fwd_ops.size() + cp.bwd_ops.size()) * sizeof(DevOp) +
+            (cp.fwd_passes.size() + cp.bwd_passes.size()) * sizeof(DevPass) +
+            e->index.size() * 48 + 256;
+  if (e->cost > kProgramCacheBytes / 4) return;
+  const uint64_t h = program_cache_hash(e->bytes.data(), e->bytes.size(), e->names, e->job,
+                                        e->fuse);
+  std::lock_guard<std::mutex> lk(g_pc_mu);
+  while (!g_pc.empty() &&
+         (g_pc_bytes + e->cost > kProgramCacheBytes || g_pc.size() >= kProgramCacheEntries)) {
+    auto oldest = g_pc.begin();
+    for (auto it = g_pc.begin(); it != g_pc.end(); ++it)
+      if (it->second->stamp < oldest->second->stamp) oldest = it;
+    g_pc_bytes -= oldest->second->cost;
+    g_pc.erase(oldest);
+  }
+  e->stamp = ++g_pc_clock;
+  g_pc_bytes += e->cost;
+  g_pc.emplace(h, std::move(e));
+}
+
+void program_cache_clear() {
+  std::lock_guard<std::mutex> lk(g_pc_mu);
+  g_pc.clear();
+  g_pc_bytes = 0;
+}
+
 // Parses/compiles every row.  Throws Error on invalid input.
 // TFQG_KIND_INNER: `others` holds batch x num_others paired programs
 // (tfq_inner_product's other_programs); they become rows batch + i *
@@ -91,9 +214,21 @@ void build_batch(tfqg_batch* b, const char* const* programs,
                                                                           : kJobForward;
   b->inner_grads = inner && inner_grads;
 
-  // 1. parse programs (ParsePrograms, parse_context.cc:174-206), deduplicated
-  std::unordered_map<std::string, int> prog_ids;
+  // symbol names in column order: part of the compiled-program cache key
+  std::string names_key;
+  for (int64_t j = 0; j < num_symbols; ++j) {
+    const uint64_t ln = uint64_t(name_lens[j]);
+    names_key.append(reinterpret_cast<const char*>(&ln), sizeof(ln));
+    names_key.append(symbol_names[j], size_t(name_lens[j]));
+  }
+  const bool fuse = g_gate_fusion.load() != 0;
+
+  // 1. parse programs (ParsePrograms, parse_context.cc:174-206), deduplicated;
+  // programs found in the compiled-program cache are not decoded
+  std::unordered_map<ProtoKey, int, ProtoKeyHash> prog_ids;
   std::vector<ProgramP> parsed;
+  std::vector<std::shared_ptr<const ProgramCacheEntry>> cached;
+  std::vector<ProtoKey> src;
   std::vector<int> row_prog(static_cast<size_t>(batch));
   std::vector<int> pair_of;  // paired program -> its reference program
   for (int64_t i = 0; i < batch; ++i) {
@@ -101,28 +236,31 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     const int64_t k = i - main_rows;  // paired row (main row k / num_others)
     const char* data = paired ? others[k] : programs[i];
     const int64_t len = paired ? other_lens[k] : program_lens[i];
-    std::string key = make_key(data, len);
     // a paired program resolves through its reference program's qubits
-    if (paired) key += "\0@" + std::to_string(row_prog[k / num_others]);
+    const ProtoKey key{data, size_t(len), paired ? row_prog[k / num_others] : -1};
     auto it = prog_ids.find(key);
     if (it != prog_ids.end()) {
       row_prog[i] = it->second;
       continue;
     }
     ProgramP p;
-    decode_program(data, size_t(len), &p);
+    std::shared_ptr<const ProgramCacheEntry> hit;
+    if (!inner) hit = program_cache_find(data, size_t(len), names_key, int(job), fuse);
+    if (!hit) decode_program(data, size_t(len), &p);
     int id = int(parsed.size());
     parsed.push_back(std::move(p));
+    cached.push_back(std::move(hit));
+    src.push_back(key);
     pair_of.push_back(paired ? row_prog[k / num_others] : -1);
-    prog_ids.emplace(std::move(key), id);
+    prog_ids.emplace(key, id);
     row_prog[i] = id;
   }
   // 2. parse pauli sums (GetPauliSums, parse_context.cc:367-403)
-  std::unordered_map<std::string, int> psum_ids;
+  std::unordered_map<ProtoKey, int, ProtoKeyHash> psum_ids;
   std::vector<PauliSumP> psums;
   std::vector<int> row_psum(static_cast<size_t>(batch * num_ops));
   for (int64_t k = 0; k < batch * num_ops; ++k) {
-    std::string key = make_key(pauli_sums[k], psum_lens[k]);
+    const ProtoKey key{pauli_sums[k], size_t(psum_lens[k]), -1};
     auto it = psum_ids.find(key);
     if (it != psum_ids.end()) {
       row_psum[k] = it->second;
@@ -132,7 +270,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     decode_paulisum(pauli_sums[k], size_t(psum_lens[k]), &ps);
     int id = int(psums.size());
     psums.push_back(std::move(ps));
-    psum_ids.emplace(std::move(key), id);
+    psum_ids.emplace(key, id);
     row_psum[k] = id;
   }
   // 3. symbol map (GetSymbolMaps): name -> column, last column wins
@@ -168,11 +306,13 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     int pid = row_prog[i];
     if (i >= main_rows) break;  // paired rows: resolved with their reference
     if (!resolved[pid]) {
-      resolve_qubits(parsed[pid], &index[pid]);
+      if (cached[pid]) index[pid] = cached[pid]->index;
+      else resolve_qubits(parsed[pid], &index[pid]);
       resolved[pid] = 1;
     }
     if (inner) resolve_paired(i);
-    if (parsed[pid].moments.empty()) continue;  // (#679) empty program
+    const bool empty = cached[pid] ? cached[pid]->empty : parsed[pid].moments.empty();
+    if (empty) continue;  // (#679) empty program
     for (int64_t j = 0; j < num_ops; ++j) {
       const PauliSumP& ps = psums[row_psum[i * num_ops + j]];
       for (const TermP& t : ps)
@@ -189,8 +329,23 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   const SymbolTable no_symbols;
   for (size_t pid = 0; pid < parsed.size(); ++pid) {
     if (inner && pair_of[pid] >= 0) continue;
+    if (cached[pid]) {
+      compiled[pid] = cached[pid]->cp;
+      continue;
+    }
     compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
-    plan_program(&compiled[pid], job, g_gate_fusion.load() != 0);
+    plan_program(&compiled[pid], job, fuse);
+    if (!inner) {
+      auto e = std::make_shared<ProgramCacheEntry>();
+      e->bytes.assign(src[pid].p, src[pid].n);
+      e->names = names_key;
+      e->job = int(job);
+      e->fuse = fuse;
+      e->empty = parsed[pid].moments.empty();
+      e->cp = compiled[pid];
+      e->index = index[pid];
+      program_cache_insert(std::move(e));
+    }
   }
   for (size_t pid = 0; pid < parsed.size() && inner; ++pid) {
     if (pair_of[pid] < 0) continue;
@@ -200,7 +355,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       throw Error(kInvalidArgument,
                   "Found symbols in other_programs.No symbols are allowed in these circuits.");
     }
-    plan_program(&compiled[pid], kJobForward, g_gate_fusion.load() != 0);
+    plan_program(&compiled[pid], kJobForward, fuse);
   }
 
   // 5. pack programs
@@ -1268,6 +1423,18 @@ int tfqg_internal_jit_compile_check(void* batch, int mode, char* err, int64_t er
 // returns the previous value.
 int tfqg_internal_set_wide_min_qubits(int n) {
   return g_wide_min_qubits.exchange(n);
+}
+
+// Compiled-program cache on (1) or off (0); off also empties it.  Returns
+// the previous setting; hits and misses since the process started go to
+// *hits and *misses when not NULL.
+int tfqg_internal_program_cache(int on, int64_t* hits, int64_t* misses) {
+  if (hits) *hits = g_pc_hits.load();
+  if (misses) *misses = g_pc_misses.load();
+  if (on < 0) return g_pc_on.load();
+  const int prev = g_pc_on.exchange(on ? 1 : 0);
+  if (!on) program_cache_clear();
+  return prev;
 }
 
 // Gate fusion of forward plans on (1) or off (0) for batches created after
