@@ -73,7 +73,16 @@ int tfqg_batch_create(const char* const* programs, const int64_t* program_lens,
 
 /* Largest qubit count in the batch (output width of state / samples). */
 int tfqg_batch_max_num_qubits(const tfqg_batch* b, int32_t* out);
+/* Synchronizes the batch's device and frees the batch.  Its device buffers
+ * return to a process-wide pool that later batches draw from (capped by
+ * TFQG_POOL_MAX_BYTES, default 4 GiB; 0 disables the pool). */
 void tfqg_batch_destroy(tfqg_batch* b);
+
+/* Frees every pooled device block and empties the process-wide cache of
+ * compiled programs (keyed by program bytes, symbol names, batch kind).  No
+ * reference counterpart: the reference re-parses and re-allocates per op
+ * call, which is what these caches save. */
+void tfqg_release_cached_memory(void);
 
 /* Expectations [batch, num_ops]; -2 for empty programs.
  * Replaces TfqSimulateExpectationOp::ComputeSmall/Large

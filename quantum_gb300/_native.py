@@ -52,6 +52,7 @@ EXPORTED = (
     "tfqg_batch_create_inner_product", "tfqg_batch_inner_product", "tfqg_inner_product",
     "tfqg_batch_inner_product_grad", "tfqg_batch_noisy_sampled_expectation",
     "tfqg_batch_noisy_samples", "tfqg_noisy_sampled_expectation", "tfqg_noisy_samples",
+    "tfqg_release_cached_memory",
 )
 
 

@@ -23,6 +23,16 @@ namespace tfqg {
                               cudaGetErrorString(e_) + " at " #call);      \
   } while (0)
 
+// Process-wide pool of device blocks (capi.cc).  pool_take returns a cached
+// block of at least `bytes` (and not much larger) or a new one; pool_give
+// keeps a block for reuse.  A block is given back only when no work can
+// still use it: `synced` says the caller has synchronized the device,
+// otherwise pool_give does (as cudaFree would).  Cached bytes are capped
+// (TFQG_POOL_MAX_BYTES, default 4 GiB; 0 disables the pool).
+void* pool_take(size_t bytes, int dev, size_t* got);
+void pool_give(void* p, size_t bytes, int dev, bool synced) noexcept;
+void pool_trim(int dev) noexcept;  // dev < 0: every device
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -30,13 +40,13 @@ struct DevBuf {
   void reserve(size_t need, int dev) {
     if (need <= bytes && dev == device) return;
     release();
-    size_t sz = std::max<size_t>(need, 256);
-    TFQG_CUDA(cudaMalloc(&p, sz));
-    bytes = sz;
+    size_t got = 0;
+    p = pool_take(std::max<size_t>(need, 256), dev, &got);
+    bytes = got;
     device = dev;
   }
-  void release() {
-    if (p) cudaFree(p);
+  void release(bool synced = false) noexcept {
+    if (p) pool_give(p, bytes, device, synced);
     p = nullptr;
     bytes = 0;
   }
@@ -102,6 +112,12 @@ struct tfqg_batch {
   int device = -1;
   tfqg::DevBuf tables, mats, dmats, work, counter, values, out, aux, aux2;
   tfqg::DevBuf wide_state, wide_acc;
+  // gives every device buffer back to the pool (the device is synchronized)
+  void release_buffers() noexcept {
+    tfqg::DevBuf* all[] = {&tables, &mats,  &dmats,      &work,     &counter,  &values,
+                           &out,    &aux,   &aux2,       &wide_state, &wide_acc, &inner_tmp};
+    for (tfqg::DevBuf* d : all) d->release(true);
+  }
   tfqg::BatchDevice bd;
   const int32_t* d_order_fwd = nullptr;
 };

@@ -2,11 +2,13 @@
 // kernel launches.  See the header for the reference functions each entry
 // point replaces.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -35,6 +37,96 @@ int fail(int code, const std::string& msg) {
 }  // namespace
 
 int tfqg::set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+
+// ---- device block pool -----------------------------------------------------
+namespace {
+
+struct DevicePool {
+  std::multimap<size_t, void*> free;  // size -> block
+  size_t bytes = 0;
+};
+std::mutex g_pool_mu;
+DevicePool g_pool[64];
+
+size_t pool_cap() {
+  static const size_t cap = [] {
+    const char* e = getenv("TFQG_POOL_MAX_BYTES");
+    return e ? size_t(strtoull(e, nullptr, 10)) : size_t(4) << 30;
+  }();
+  return cap;
+}
+
+bool device_sync(int dev) noexcept {
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess) return false;
+  if (cur != dev && cudaSetDevice(dev) != cudaSuccess) return false;
+  const bool ok = cudaDeviceSynchronize() == cudaSuccess;
+  if (cur != dev) cudaSetDevice(cur);
+  if (!ok) cudaGetLastError();
+  return ok;
+}
+
+}  // namespace
+
+void* tfqg::pool_take(size_t bytes, int dev, size_t* got) {
+  if (dev >= 0 && dev < 64) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    DevicePool& pl = g_pool[dev];
+    auto it = pl.free.lower_bound(bytes);
+    // a cached block at most 1.5x (plus 1 MiB) the request
+    if (it != pl.free.end() && it->first <= bytes + bytes / 2 + (size_t(1) << 20)) {
+      void* p = it->second;
+      *got = it->first;
+      pl.bytes -= it->first;
+      pl.free.erase(it);
+      return p;
+    }
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    pool_trim(dev);
+    e = cudaMalloc(&p, bytes);
+  }
+  if (e != cudaSuccess)
+    throw Error(kInternal, std::string("CUDA error: ") + cudaGetErrorString(e) +
+                               " at cudaMalloc");
+  *got = bytes;
+  return p;
+}
+
+void tfqg::pool_give(void* p, size_t bytes, int dev, bool synced) noexcept {
+  if (!p) return;
+  if (dev < 0 || dev >= 64 || (!synced && !device_sync(dev))) {
+    cudaFree(p);
+    return;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    DevicePool& pl = g_pool[dev];
+    if (pl.bytes + bytes <= pool_cap()) {
+      pl.free.emplace(bytes, p);
+      pl.bytes += bytes;
+      return;
+    }
+  }
+  cudaFree(p);
+}
+
+void tfqg::pool_trim(int dev) noexcept {
+  std::vector<void*> blocks;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (int d = 0; d < 64; ++d) {
+      if (dev >= 0 && d != dev) continue;
+      for (auto& kv : g_pool[d].free) blocks.push_back(kv.second);
+      g_pool[d].free.clear();
+      g_pool[d].bytes = 0;
+    }
+  }
+  for (void* p : blocks) cudaFree(p);
+}
 
 namespace {
 
@@ -838,7 +930,18 @@ int tfqg_batch_max_num_qubits(const tfqg_batch* b, int32_t* out) {
   return 0;
 }
 
-void tfqg_batch_destroy(tfqg_batch* b) { delete b; }
+void tfqg_batch_destroy(tfqg_batch* b) {
+  if (!b) return;
+  // one synchronize for all of the batch's buffers, which then return to
+  // the device pool for the next batch
+  if (b->device >= 0 && device_sync(b->device)) b->release_buffers();
+  delete b;
+}
+
+void tfqg_release_cached_memory(void) {
+  pool_trim(-1);
+  program_cache_clear();
+}
 
 int tfqg_batch_expectation(tfqg_batch* b, const float* symbol_values,
                            float* expectations, int device_buffers,
