@@ -265,6 +265,16 @@ def row_sweeps(handle, row):
     return a.value, m.value
 
 
+def set_wide_few_rows(rows):
+    """Batches that stream fewer than `rows` rows run their rows of 17+
+    qubits as wide rows (0: never); for batches created from now on.
+    Returns the previous value."""
+    f = lib().tfqg_internal_set_wide_few_rows
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return f(int(rows))
+
+
 def batch_wide_rows(handle):
     f = lib().tfqg_internal_batch_wide_rows
     f.argtypes = [c_void_p]

@@ -131,6 +131,7 @@ void tfqg::pool_trim(int dev) noexcept {
 namespace {
 
 std::atomic<int> g_wide_min_qubits{kWideMinQubits};
+std::atomic<int> g_wide_few_rows{kWideFewRows};
 
 int wide_min_qubits() { return g_wide_min_qubits.load(); }
 
@@ -563,10 +564,21 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   if (inner)  // reference rows first: the gradient's adjoint runs only them
     std::stable_partition(b->order.begin(), b->order.end(),
                           [&](int32_t r) { return r < main_rows; });
-  // wide rows: in the forward modes the whole grid simulates them one by one
+  // wide rows: the whole grid simulates them one by one.  Rows of at least
+  // wide_min qubits always; rows of kWideFewQubits.. qubits (16+ tiles per
+  // pass) too when the batch streams fewer than kWideFewRows rows, since one
+  // row per CTA would then leave most SMs idle
   const int wide_min = std::max(wide_min_qubits(), kStreamTileBits + 2);
+  int64_t streamed_rows = 0;
+  for (int64_t i = 0; i < batch; ++i) {
+    const DevProgram& p = b->programs[b->rows[i].program];
+    if (p.n > 0 && !p.resident && p.fwd_pass_begin != p.fwd_pass_end) ++streamed_rows;
+  }
+  const int few_min = streamed_rows < g_wide_few_rows.load() && !inner
+                          ? std::min(wide_min, kWideFewQubits)
+                          : wide_min;
   auto is_wide = [&](const DevProgram& p) {
-    return p.n >= wide_min && !p.resident && p.fwd_pass_begin != p.fwd_pass_end;
+    return p.n >= few_min && !p.resident && p.fwd_pass_begin != p.fwd_pass_end;
   };
   for (const int32_t i : b->order) {
     const DevProgram& p = b->programs[b->rows[i].program];
@@ -1545,6 +1557,10 @@ int tfqg_internal_program_cache(int on, int64_t* hits, int64_t* misses) {
 int tfqg_internal_set_gate_fusion(int on) {
   return g_gate_fusion.exchange(on ? 1 : 0);
 }
+
+// Streamed-row count below which rows of 17+ qubits run as wide rows, for
+// batches created after the call (0: never); returns the previous value.
+int tfqg_internal_set_wide_few_rows(int rows) { return g_wide_few_rows.exchange(rows); }
 
 // Number of wide rows of a batch (forward modes).
 int tfqg_internal_batch_wide_rows(void* batch) {

@@ -76,6 +76,10 @@ constexpr int kWideThreads = 256;
 // Rows of at least this many qubits run as wide rows in the forward modes:
 // the whole grid works on one state, one launch per pass.
 constexpr int kWideMinQubits = 22;
+// A batch that streams fewer than kWideFewRows rows runs its rows of
+// kWideFewQubits or more qubits (16+ tiles per pass) as wide rows too.
+constexpr int kWideFewRows = 64;
+constexpr int kWideFewQubits = 17;
 
 #ifndef __CUDACC_RTC__
 cudaError_t launch_build_matrices(const BatchDevice& b, const RunArgs& a,

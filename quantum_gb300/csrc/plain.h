@@ -45,6 +45,7 @@ int tfqg_internal_batch_passes(void* batch, int32_t* fwd, int32_t* bwd,
 // for empty programs), used to shard a batch across devices.
 int tfqg_internal_batch_row_costs(void* batch, double* costs);
 int tfqg_internal_set_wide_min_qubits(int n);
+int tfqg_internal_set_wide_few_rows(int rows);
 int tfqg_internal_set_gate_fusion(int on);
 int tfqg_internal_program_cache(int on, int64_t* hits, int64_t* misses);
 int tfqg_internal_row_sweeps(void* batch, int64_t row, int32_t* fwd, int32_t* meas);

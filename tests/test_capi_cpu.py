@@ -158,3 +158,25 @@ def test_inner_product_input_checks():
         ops.InnerProductBatch([ref, ref], [], [[same]])
     # an empty reference program skips its paired circuits' checks
     ops.InnerProductBatch([S.serialize_circuit(S.Circuit())], [], [[extra]])
+
+
+def test_wide_row_rule_follows_the_batch():
+    """Rows of 22+ qubits always run on the whole grid; rows of 17..21 qubits
+    too when the batch streams fewer than 64 rows (otherwise one row per CTA
+    already fills the GPU); 16-qubit rows (8 tiles per pass) never."""
+    import numpy as np
+    from quantum_gb300 import _native, ops
+    from quantum_gb300 import serialize as S
+    from tests.circuits import random_circuit
+    rng = np.random.default_rng(1)
+
+    def prog(n):
+        return S.serialize_circuit(random_circuit(S.GridQubit.rect(1, n), 2, rng, []))
+
+    p16, p18, p5 = prog(16), prog(18), prog(5)
+    cases = [([p18], 1), ([p16], 0), ([p18] * 70, 0), ([p18] + [p5] * 100, 1),
+             ([p18] * 10 + [p16] * 60, 0)]
+    for progs, want in cases:
+        b = ops.Batch(progs, [], None)
+        assert _native.batch_wide_rows(b._h) == want, (len(progs), want)
+        b.close()
