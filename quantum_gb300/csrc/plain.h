@@ -47,6 +47,9 @@ int tfqg_internal_batch_row_costs(void* batch, double* costs);
 int tfqg_internal_set_wide_min_qubits(int n);
 int tfqg_internal_set_wide_few_rows(int rows);
 int tfqg_internal_set_gate_fusion(int on);
+// tcgen05 self-check (tc_mma.cu): D[128x64] = A[128x32] * B[64x32]^T, tf32.
+int tfqg_internal_tc_gemm_tf32(const float* A, const float* B, float* D, int* status,
+                               void* stream);
 int tfqg_internal_program_cache(int on, int64_t* hits, int64_t* misses);
 int tfqg_internal_row_sweeps(void* batch, int64_t row, int32_t* fwd, int32_t* meas);
 int tfqg_internal_forward_plan_gates(void* batch, int64_t row,
