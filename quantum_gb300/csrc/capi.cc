@@ -565,20 +565,24 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     std::stable_partition(b->order.begin(), b->order.end(),
                           [&](int32_t r) { return r < main_rows; });
   // wide rows: the whole grid simulates them one by one.  Rows of at least
-  // wide_min qubits always; rows of kWideFewQubits.. qubits (16+ tiles per
-  // pass) too when the batch streams fewer than kWideFewRows rows, since one
-  // row per CTA would then leave most SMs idle
+  // wide_min qubits always.  A row of kWideFewQubits..wide_min-1 qubits
+  // too when the batch streams few rows: in the queue R streamed rows run
+  // side by side, one CTA each, while a wide pass keeps 2^(n-13) tiles
+  // busy, and its adjoint passes run the interpreter (about 2x slower than
+  // the queue's specialized module): the whole grid wins when
+  // R <= 2^(n-14) (and R < kWideFewRows)
   const int wide_min = std::max(wide_min_qubits(), kStreamTileBits + 2);
   int64_t streamed_rows = 0;
   for (int64_t i = 0; i < batch; ++i) {
     const DevProgram& p = b->programs[b->rows[i].program];
     if (p.n > 0 && !p.resident && p.fwd_pass_begin != p.fwd_pass_end) ++streamed_rows;
   }
-  const int few_min = streamed_rows < g_wide_few_rows.load() && !inner
-                          ? std::min(wide_min, kWideFewQubits)
-                          : wide_min;
+  const bool few = streamed_rows < g_wide_few_rows.load() && !inner;
   auto is_wide = [&](const DevProgram& p) {
-    return p.n >= few_min && !p.resident && p.fwd_pass_begin != p.fwd_pass_end;
+    if (p.resident || p.fwd_pass_begin == p.fwd_pass_end) return false;
+    if (p.n >= wide_min) return true;
+    return few && p.n >= kWideFewQubits &&
+           streamed_rows <= (int64_t(1) << std::min(p.n - kStreamTileBits - 1, 40));
   };
   for (const int32_t i : b->order) {
     const DevProgram& p = b->programs[b->rows[i].program];

@@ -76,8 +76,9 @@ constexpr int kWideThreads = 256;
 // Rows of at least this many qubits run as wide rows in the forward modes:
 // the whole grid works on one state, one launch per pass.
 constexpr int kWideMinQubits = 22;
-// A batch that streams fewer than kWideFewRows rows runs its rows of
-// kWideFewQubits or more qubits (16+ tiles per pass) as wide rows too.
+// A batch that streams R < kWideFewRows rows runs a row of n >=
+// kWideFewQubits qubits as a wide row too when R <= 2^(n-14) (half its
+// tiles per pass).
 constexpr int kWideFewRows = 64;
 constexpr int kWideFewQubits = 17;
 

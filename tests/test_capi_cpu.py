@@ -161,9 +161,10 @@ def test_inner_product_input_checks():
 
 
 def test_wide_row_rule_follows_the_batch():
-    """Rows of 22+ qubits always run on the whole grid; rows of 17..21 qubits
-    too when the batch streams fewer than 64 rows (otherwise one row per CTA
-    already fills the GPU); 16-qubit rows (8 tiles per pass) never."""
+    """Rows of 22+ qubits always run on the whole grid; a row of n = 17..21
+    qubits too when the batch streams R <= 2^(n-14) rows (a wide pass keeps
+    2^(n-13) tiles busy; in the queue R rows run side by side); 16-qubit
+    rows never."""
     import numpy as np
     from quantum_gb300 import _native, ops
     from quantum_gb300 import serialize as S
@@ -174,8 +175,10 @@ def test_wide_row_rule_follows_the_batch():
         return S.serialize_circuit(random_circuit(S.GridQubit.rect(1, n), 2, rng, []))
 
     p16, p18, p5 = prog(16), prog(18), prog(5)
+    p20 = prog(20)
     cases = [([p18], 1), ([p16], 0), ([p18] * 70, 0), ([p18] + [p5] * 100, 1),
-             ([p18] * 10 + [p16] * 60, 0)]
+             ([p18] * 10 + [p16] * 60, 0), ([p18] * 16, 16), ([p18] * 17, 0),
+             ([p20] * 40, 40), ([p20] + [p18] * 20, 1)]
     for progs, want in cases:
         b = ops.Batch(progs, [], None)
         assert _native.batch_wide_rows(b._h) == want, (len(progs), want)
