@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--c4-grid", default="5x6",
                     help="rows x cols of the C4 grid circuit (5x6 = 30 qubits; a smaller "
                          "grid gives a profiling case of the same kernels)")
+    ap.add_argument("--tensor-cores", action="store_true",
+                    help="c4: forward passes as 5-qubit fused blocks on the tensor cores "
+                         "(split 3xTF32), one HBM sweep per block")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default): the headline expectation + adjoint line; "
                          "c1, c3, c4, c5: the other benchmark configurations, "
@@ -224,14 +227,22 @@ def config_roofline(wl, w, batch, ms, clk, units):
     if wl == "c4":
         from quantum_gb300 import _native
         fwd, meas = _native.row_sweeps(batch._h, 0)
-        nbytes = (fwd * 16 + meas * 8) * 2 ** n
+        blocks = _native.tc_blocks(batch._h, 0)
+        if blocks > 0:
+            # tensor-core blocks: one read+write sweep each, plus the |0> fill
+            nbytes = (blocks * 16 + 8 + meas * 8) * 2 ** n
+            how = (f"{blocks} tensor-core block sweeps x 16 B + |0> fill 8 B + {meas} "
+                   f"measurement pass(es) x 8 B, times 2^{n} amplitudes")
+        else:
+            nbytes = (fwd * 16 + meas * 8) * 2 ** n
+            how = (f"{fwd} forward passes x 16 B + {meas} measurement "
+                   f"pass(es) x 8 B, times 2^{n} amplitudes")
         peak = peaks.get("hbm_gbs") or 6800.0
         achieved = nbytes * units / (ms / 1e3) / 1e9
         return {"bound": "hbm", "kernel": "wide passes + measurement (whole call)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None,
-                "algorithmic": f"{fwd} forward passes x 16 B + {meas} measurement "
-                               f"pass(es) x 8 B, times 2^{n} amplitudes",
+                "algorithmic": how,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"
                                if peaks.get("hbm_gbs") else "fallback 6800 GB/s"}
     if wl in ("c1", "c5") and c:
@@ -250,6 +261,50 @@ def config_roofline(wl, w, batch, ms, clk, units):
                                f"{'trajectory' if wl == 'c5' else 'circuit'} x {units}",
                 "peak_source": f"derived: {sms} SMs x 128 FP32 lanes x 2 flop x {mhz:.0f} MHz"}
     return None
+
+
+def tc_kernel_roofline(n, batch, dev, launches=10):
+    """The tensor-core block kernel alone on a 2^n complex64 state: a random
+    5-qubit unitary on the targets of the row's first block, `launches`
+    launches timed with CUDA events on the launching stream.  Algorithmic
+    bytes per launch: 16 B per amplitude (read + write the state)."""
+    import torch
+    from quantum_gb300 import _native
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    plan = _native.tc_plan(batch._h, 0, np.zeros(0, np.float32))
+    tgt = plan[0][0] if plan else (0, 1, 2, 3, 4)
+    rng = np.random.default_rng(0)
+    z = rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))
+    q, _ = np.linalg.qr(z)
+    U = torch.tensor(q.astype(np.complex64), device=dev)
+    psi = torch.zeros(2 ** n, dtype=torch.complex64, device=dev)
+    psi[0] = 1
+    st = torch.zeros(1, dtype=torch.int32, device=dev)
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        _native.tc_apply(psi.data_ptr(), n, U.data_ptr(), tgt, st.data_ptr(), s.cuda_stream)
+    s.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(launches):
+        _native.tc_apply(psi.data_ptr(), n, U.data_ptr(), tgt, st.data_ptr(), s.cuda_stream)
+    b.record(s)
+    s.synchronize()
+    ms = a.elapsed_time(b) / launches
+    peak = peaks.get("hbm_gbs") or 6800.0
+    achieved = 16 * 2 ** n / (ms / 1e3) / 1e9
+    ok = int(st.item()) == 0
+    del psi
+    return {"bound": "hbm", "kernel": "tc_apply5_kernel", "targets": list(tgt),
+            "ms_per_launch": ms, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "status_ok": ok,
+            "algorithmic": f"16 B x 2^{n} amplitudes per launch (state > L2)",
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"
+                           if peaks.get("hbm_gbs") else "fallback 6800 GB/s"}
 
 
 def run_config(args):
@@ -274,6 +329,9 @@ def run_config(args):
         w = workloads.noisy_brickwall(64, 14, 15, 0.01, seed=1)
         units, unit = 64 * 2000, "trajectories/s"
     kind = ops.KIND_NOISY if wl == "c5" else ops.KIND_FORWARD
+    tc = wl == "c4" and args.tensor_cores
+    if tc:
+        __import__("quantum_gb300")._native.set_tensor_core_gates(True)
     t0 = time.perf_counter()
     batch = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
     parse_s = time.perf_counter() - t0
@@ -321,6 +379,10 @@ def run_config(args):
                                       [w["pauli_sums"][i] for i in rows])
         line["accuracy"] = {"max_abs": float(np.abs(out.cpu().numpy()[rows] - want).max()),
                             "rows": len(rows)}
+    if tc:
+        line["tensor_core_blocks"] = __import__("quantum_gb300")._native.tc_blocks(batch._h, 0)
+        line["tc_block_kernel"] = tc_kernel_roofline(w["n"], batch, dev)
+        line["config"]["tensor_cores"] = "5-qubit blocks, split 3xTF32 (tcgen05 kind::tf32)"
     if wl == "c4":
         # a 30-qubit complex128 oracle run is out of reach: the fused plan is
         # checked against the unfused one here (the 4x4 grid is pinned to the

@@ -205,6 +205,74 @@ def set_gate_fusion(on):
     return bool(f(1 if on else 0))
 
 
+def set_tensor_core_gates(on):
+    """Forward passes of wide rows as 5-qubit fused blocks on the tensor
+    cores (on) or as tile passes on the FP32 pipe (off, the default), for
+    calls made from now on; returns the previous setting."""
+    f = lib().tfqg_internal_set_tensor_core_gates
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return bool(f(1 if on else 0))
+
+
+def tc_apply(psi_ptr, n, u_ptr, targets, status_ptr, stream=0, grid=0):
+    """One launch of the tensor-core 5-qubit block kernel on device buffers:
+    psi (2^n complex64) <- U (32 x 32 complex64, row-major) on the ascending
+    bits `targets`; status (device int32) is set to 1 on an MMA wait
+    timeout.  Raises on a launch error."""
+    f = lib().tfqg_internal_tc_apply
+    f.argtypes = [c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p, ctypes.c_int,
+                  c_void_p]
+    f.restype = ctypes.c_int
+    tgt = (ctypes.c_int32 * 5)(*[int(t) for t in targets])
+    rc = f(psi_ptr, int(n), u_ptr, tgt, status_ptr, int(grid), stream)
+    if rc != 0:
+        raise RuntimeError(f"tc_apply launch failed: cudaError {rc}")
+
+
+def tc_blocks(handle, k):
+    """Tensor-core blocks of the k-th wide row of a batch (-1: no plan, or
+    the batch has not run on the tensor-core path yet)."""
+    f = lib().tfqg_internal_tc_blocks
+    f.argtypes = [c_void_p, ctypes.c_int64]
+    f.restype = ctypes.c_int
+    return int(f(handle, int(k)))
+
+
+def tc_status(handle):
+    """Status word of the batch's tensor-core kernels: 0, or 1 when an MMA
+    completion wait timed out (synchronizes the device)."""
+    f = lib().tfqg_internal_tc_status
+    f.argtypes = [c_void_p]
+    f.restype = ctypes.c_int
+    return int(f(handle))
+
+
+def tc_plan(handle, row, row_values, max_blocks=4096):
+    """Host copy of a row's tensor-core block plan: a list of (targets,
+    matrix) with the 5 target bits ascending and the 32 x 32 complex128
+    product of the member gates (index bit i = targets[i]), or None when the
+    row has no plan."""
+    import numpy as np
+    f = lib().tfqg_internal_tc_plan
+    f.argtypes = [c_void_p, ctypes.c_int64, c_void_p, c_void_p, c_void_p,
+                  ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    f.restype = ctypes.c_int
+    vals = np.ascontiguousarray(row_values, dtype=np.float32)
+    tgt = np.zeros((max_blocks, 5), dtype=np.int32)
+    mats = np.zeros((max_blocks, 32, 32, 2), dtype=np.float64)
+    count = ctypes.c_int64(0)
+    rc = f(handle, int(row), vals.ctypes.data if vals.size else None,
+           tgt.ctypes.data, mats.ctypes.data, max_blocks, ctypes.byref(count))
+    if rc != 0:
+        raise _ERRORS.get(rc, InternalError)("tc_plan failed")
+    if count.value < 0:
+        return None
+    assert count.value <= max_blocks
+    m = mats[:count.value, ..., 0] + 1j * mats[:count.value, ..., 1]
+    return [(tuple(int(x) for x in tgt[i]), m[i]) for i in range(count.value)]
+
+
 def forward_plan_gates(handle, row, row_values):
     """The gates of a row's forward plan in execution order, with matrices
     bound on the host: a list of (nq, b0, b1, cmask, cval, kind, matrix)."""

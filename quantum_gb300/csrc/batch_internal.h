@@ -112,10 +112,18 @@ struct tfqg_batch {
   int device = -1;
   tfqg::DevBuf tables, mats, dmats, work, counter, values, out, aux, aux2;
   tfqg::DevBuf wide_state, wide_acc;
+  // tensor-core forward path of wide rows (tc_gates.cu): per wide row its
+  // first block and block count (count -1: the row has no 5-bit plan)
+  bool tc_planned = false;
+  std::vector<tfqg::TcBlock> tc_blocks;
+  std::vector<int32_t> tc_members;
+  std::vector<std::pair<int32_t, int32_t>> tc_rows;  // parallel to wide_rows
+  tfqg::DevBuf tc_tab, tc_mats, tc_status;
   // gives every device buffer back to the pool (the device is synchronized)
   void release_buffers() noexcept {
-    tfqg::DevBuf* all[] = {&tables, &mats,  &dmats,      &work,     &counter,  &values,
-                           &out,    &aux,   &aux2,       &wide_state, &wide_acc, &inner_tmp};
+    tfqg::DevBuf* all[] = {&tables,     &mats,     &dmats,     &work,   &counter,
+                           &values,     &out,      &aux,       &aux2,   &wide_state,
+                           &wide_acc,   &inner_tmp, &tc_tab,   &tc_mats, &tc_status};
     for (tfqg::DevBuf* d : all) d->release(true);
   }
   tfqg::BatchDevice bd;

@@ -138,6 +138,10 @@ int wide_min_qubits() { return g_wide_min_qubits.load(); }
 // Gate fusion of forward plans (on by default).
 std::atomic<int> g_gate_fusion{1};
 
+// Forward passes of wide rows as 5-bit fused blocks on the tensor cores
+// (tc_gates.cu) instead of tile passes on the FP32 pipe.
+std::atomic<int> g_tc_gates{0};
+
 }  // namespace
 
 namespace {
@@ -715,6 +719,60 @@ int occupancy_grid(const void* k, int threads, size_t smem, int dev) {
   return sms * std::max(per_sm, 1);
 }
 
+// Plans the tensor-core blocks of every wide row once per batch and uploads
+// them (blocks, then members) into b->tc_tab.
+void tc_prepare(tfqg_batch* b, cudaStream_t s) {
+  if (b->tc_planned && b->tc_tab.device == b->device) return;
+  b->tc_blocks.clear();
+  b->tc_members.clear();
+  b->tc_rows.clear();
+  for (const int32_t row : b->wide_rows) {
+    const DevProgram& p = b->programs[b->rows[size_t(row)].program];
+    const int32_t first = int32_t(b->tc_blocks.size());
+    const bool ok = plan_tc_blocks(b->gates.data() + p.gate_begin, p.num_gates, p.n,
+                                   &b->tc_blocks, &b->tc_members);
+    b->tc_rows.emplace_back(first, ok ? int32_t(b->tc_blocks.size()) - first : -1);
+  }
+  const size_t bb = b->tc_blocks.size() * sizeof(TcBlock);
+  const size_t mb = b->tc_members.size() * sizeof(int32_t);
+  b->tc_tab.reserve(align256(bb) + mb + 256, b->device);
+  unsigned char* base = static_cast<unsigned char*>(b->tc_tab.p);
+  if (bb) TFQG_CUDA(cudaMemcpyAsync(base, b->tc_blocks.data(), bb, cudaMemcpyHostToDevice, s));
+  if (mb)
+    TFQG_CUDA(cudaMemcpyAsync(base + align256(bb), b->tc_members.data(), mb,
+                              cudaMemcpyHostToDevice, s));
+  b->tc_mats.reserve(std::max<size_t>(b->tc_blocks.size(), 1) * 1024 * sizeof(float2),
+                     b->device);
+  b->tc_status.reserve(sizeof(int), b->device);
+  TFQG_CUDA(cudaMemsetAsync(b->tc_status.p, 0, sizeof(int), s));
+  b->tc_planned = true;
+}
+
+// The forward passes of wide row `row` (the k-th wide row) as tensor-core
+// blocks: fused matrices, |0...0>, one launch per block.  False when the row
+// has no block plan (a gate on more than 5 bits).
+bool run_wide_tc(tfqg_batch* b, const BatchDevice& bd, const RunArgs* a, size_t k, int row,
+                 float2* psi, int sms, cudaStream_t s) {
+  const std::pair<int32_t, int32_t> rp = b->tc_rows[k];
+  if (rp.second < 0) return false;
+  const int n = b->programs[b->rows[size_t(row)].program].n;
+  unsigned char* base = static_cast<unsigned char*>(b->tc_tab.p);
+  const TcBlock* dblocks = reinterpret_cast<const TcBlock*>(base) + rp.first;
+  const int32_t* dmembers = reinterpret_cast<const int32_t*>(
+      base + align256(b->tc_blocks.size() * sizeof(TcBlock)));
+  float2* U = static_cast<float2*>(b->tc_mats.p) + int64_t(rp.first) * 1024;
+  TFQG_CUDA(launch_tc_fuse(bd, a->mats, row, dblocks, dmembers, rp.second, U, s));
+  TFQG_CUDA(launch_fill(psi, int64_t(1) << n, make_float2(1.f, 0.f), make_float2(0.f, 0.f),
+                        sms * 4, s));
+  const int grid = occupancy_grid(tc_apply5_kernel_ptr(), 128, tc_apply5_smem_bytes(),
+                                  b->device);
+  for (int i = 0; i < rp.second; ++i)
+    TFQG_CUDA(launch_tc_apply5(psi, n, U + int64_t(i) * 1024,
+                               b->tc_blocks[size_t(rp.first + i)],
+                               static_cast<int*>(b->tc_status.p), grid, s));
+  return true;
+}
+
 // Forward-mode work of the wide rows, one row after another on stream s:
 // every pass of a row is one launch over all SMs, then the row's
 // measurement, state padding or sampling.
@@ -729,7 +787,10 @@ void run_wide(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a,
   const int mgrid = occupancy_grid(wide_measure_kernel_ptr(), kWideThreads, smem, dev);
   int sms = 0;
   TFQG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  for (const int32_t row : b->wide_rows) {
+  const bool tc = g_tc_gates.load() != 0;
+  if (tc) tc_prepare(b, s);
+  for (size_t wk = 0; wk < b->wide_rows.size(); ++wk) {
+    const int32_t row = b->wide_rows[wk];
     const DevRow& r = b->rows[size_t(row)];
     const DevProgram& p = b->programs[r.program];
     const int n = p.n;
@@ -740,7 +801,8 @@ void run_wide(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a,
       b->wide_state.reserve((size_t(1) << b->max_wide_n) * sizeof(float2), dev);
       psi = static_cast<float2*>(b->wide_state.p);
     }
-    for (uint32_t q = p.fwd_pass_begin; q < p.fwd_pass_end; ++q) {
+    const bool tc_done = tc && run_wide_tc(b, bd, a, wk, row, psi, sms, s);
+    for (uint32_t q = p.fwd_pass_begin; q < p.fwd_pass_end && !tc_done; ++q) {
       const int init = q == p.fwd_pass_begin ? 1 : 0;
       if (jk) {
         cudaError_t e = jit_launch_wide(jk, bd, *a, row, int(q), init, psi, grid, smem,
@@ -1560,6 +1622,98 @@ int tfqg_internal_program_cache(int on, int64_t* hits, int64_t* misses) {
 // the call; returns the previous setting.
 int tfqg_internal_set_gate_fusion(int on) {
   return g_gate_fusion.exchange(on ? 1 : 0);
+}
+
+// Forward passes of wide rows on the tensor cores (1: 5-bit fused blocks,
+// tc_gates.cu) or as tile passes (0, the default), for calls made after this
+// one; returns the previous setting.
+int tfqg_internal_set_tensor_core_gates(int on) { return g_tc_gates.exchange(on ? 1 : 0); }
+
+// One launch of the tensor-core block kernel on a caller's state: psi (2^n
+// complex64, device), U (32 x 32 complex64 row-major, device), tgt (5
+// ascending bits, host), status (device int).  grid <= 0 picks the
+// occupancy grid.  Returns a cudaError_t.
+int tfqg_internal_tc_apply(void* psi, int n, const void* U, const int32_t* tgt, int* status,
+                           int grid, void* stream) {
+  TcBlock blk{};
+  for (int i = 0; i < kTcBits; ++i) {
+    if (tgt[i] < 0 || tgt[i] > 31) return int(cudaErrorInvalidValue);
+    blk.tgt[i] = uint8_t(tgt[i]);
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return int(e);
+  if (grid <= 0) {
+    try {
+      grid = occupancy_grid(tc_apply5_kernel_ptr(), 128, tc_apply5_smem_bytes(), dev);
+    } catch (const Error&) {
+      return int(cudaErrorInvalidValue);
+    }
+  }
+  return int(launch_tc_apply5(static_cast<float2*>(psi), n, static_cast<const float2*>(U), blk,
+                              status, grid, static_cast<cudaStream_t>(stream)));
+}
+
+// Tensor-core blocks of the k-th wide row of a batch (-1: no block plan or
+// not planned yet), and the kernels' status word (nonzero: an MMA
+// completion wait timed out); synchronizes the device when reading it.
+int tfqg_internal_tc_blocks(void* batch, int64_t k) {
+  const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
+  if (!b || !b->tc_planned || k < 0 || k >= int64_t(b->tc_rows.size())) return -1;
+  return b->tc_rows[size_t(k)].second;
+}
+int tfqg_internal_tc_status(void* batch) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  if (!b || !b->tc_status.p) return 0;
+  int v = 0;
+  if (cudaMemcpy(&v, b->tc_status.p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -1;
+  return v;
+}
+
+// Host copy of the tensor-core block plan of row `row` with its matrices
+// bound to `row_values` (complex128 products of the complex64 gate
+// matrices, as tc_fuse_kernel computes them): per block 5 target bits in
+// tgt[5 * i ...] and the 32 x 32 matrix, row-major, as (re, im) pairs in
+// mats[2048 * i ...].  At most `max` blocks are written; *count gets the
+// total, -1 when the row has no plan.
+int tfqg_internal_tc_plan(void* batch, int64_t row, const float* row_values, int32_t* tgt,
+                          double* mats, int64_t max, int64_t* count) {
+  const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
+  if (!b || row < 0 || row >= int64_t(b->rows.size()) || !count) return kInvalidArgument;
+  const DevProgram& p = b->programs[b->rows[size_t(row)].program];
+  const GateTemplate* gates = b->gates.data() + p.gate_begin;
+  std::vector<TcBlock> blocks;
+  std::vector<int32_t> members;
+  if (!plan_tc_blocks(gates, p.num_gates, p.n, &blocks, &members)) {
+    *count = -1;
+    return 0;
+  }
+  *count = int64_t(blocks.size());
+  for (size_t i = 0; i < blocks.size() && int64_t(i) < max; ++i) {
+    for (int q = 0; q < kTcBits; ++q) tgt[i * kTcBits + q] = blocks[i].tgt[q];
+    for (int j = 0; j < 32; ++j) {
+      Cx<double> col[32];
+      tc_block_column(gates, members.data(), blocks[i], j,
+                      [&](int k, Cx<double>* m) {
+                        Cx<double> md[16];
+                        const int kq = bound_matrix(gates[k], row_values, md);
+                        for (int e = 0; e < 16; ++e) {
+                          const bool in = e < (kq == 1 ? 4 : 16);
+                          // the device reads complex64 gate matrices
+                          m[e] = in ? Cx<double>(double(float(md[e].re)),
+                                                 double(float(md[e].im)))
+                                    : Cx<double>(0.0, 0.0);
+                        }
+                      },
+                      col);
+      for (int r = 0; r < 32; ++r) {
+        mats[i * 2048 + (r * 32 + j) * 2] = col[r].re;
+        mats[i * 2048 + (r * 32 + j) * 2 + 1] = col[r].im;
+      }
+    }
+  }
+  return 0;
 }
 
 // Streamed-row count below which rows of 17+ qubits run as wide rows, for

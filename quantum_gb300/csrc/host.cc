@@ -1197,6 +1197,56 @@ void plan_program(CompiledProgram* p, JobKind kind, bool fuse) {
 // ---------------------------------------------------------------------------
 // measurement passes
 // ---------------------------------------------------------------------------
+bool plan_tc_blocks(const GateTemplate* gates, int num_gates, int n,
+                    std::vector<TcBlock>* blocks, std::vector<int32_t>* members) {
+  if (n < kTcBits + 7 || n > 31) return false;
+  struct Open {
+    uint32_t mask = 0;
+    std::vector<int32_t> gates;
+  };
+  std::vector<Open> open;
+  int last[32];
+  for (int q = 0; q < 32; ++q) last[q] = -1;
+  for (int k = 0; k < num_gates; ++k) {
+    const GateTemplate& g = gates[k];
+    if (g.kind == GK_FUSED || g.cls == GC_SKIP) continue;
+    uint32_t q = g.cmask | (1u << g.b0);
+    if (g.nq == 2) q |= 1u << g.b1;
+    if (__builtin_popcount(q) > kTcBits) return false;
+    int latest = -1;
+    for (int b = 0; b < n; ++b)
+      if ((q >> b) & 1u) latest = std::max(latest, last[b]);
+    int chosen = -1;
+    for (int c = std::max(latest, 0); c < int(open.size()); ++c)
+      if (__builtin_popcount(open[size_t(c)].mask | q) <= kTcBits) {
+        chosen = c;
+        break;
+      }
+    if (chosen < 0) {
+      chosen = int(open.size());
+      open.emplace_back();
+    }
+    open[size_t(chosen)].mask |= q;
+    open[size_t(chosen)].gates.push_back(k);
+    for (int b = 0; b < n; ++b)
+      if ((q >> b) & 1u) last[b] = chosen;
+  }
+  for (const Open& o : open) {
+    TcBlock t{};
+    t.used = uint8_t(__builtin_popcount(o.mask));
+    uint32_t m = o.mask;
+    for (int b = n - 1; b >= 0 && __builtin_popcount(m) < kTcBits; --b) m |= 1u << b;
+    int i = 0;
+    for (int b = 0; b < n; ++b)
+      if ((m >> b) & 1u) t.tgt[i++] = uint8_t(b);
+    t.member_begin = uint32_t(members->size());
+    members->insert(members->end(), o.gates.begin(), o.gates.end());
+    t.member_end = uint32_t(members->size());
+    blocks->push_back(t);
+  }
+  return true;
+}
+
 void plan_measurement(const std::vector<DevTerm>& terms, uint32_t tb,
                       uint32_t te, int n, bool resident,
                       std::vector<DevMeas>* passes,

@@ -167,6 +167,18 @@ cudaError_t launch_wide_chunk_sums(const float2* psi, int n, double* csum, int g
 // (scanned in place) and writes them in the reference bit layout.
 cudaError_t launch_wide_sample(const BatchDevice& b, const RunArgs& a, int row,
                                const float2* psi, int n, double* csum, cudaStream_t s);
+// Tensor-core forward path (tc_gates.cu).  launch_tc_fuse writes the
+// 32 x 32 complex64 matrix of each block (row-major, 1024 entries per block)
+// from the row's bound gate matrices `mats`; launch_tc_apply5 applies one
+// block's matrix U to the 2^n state psi (n in [12, 31]) over `grid` CTAs and
+// sets *status to 1 if an MMA completion wait timed out.
+const void* tc_apply5_kernel_ptr();
+size_t tc_apply5_smem_bytes();
+cudaError_t launch_tc_fuse(const BatchDevice& b, const float2* mats, int row,
+                           const TcBlock* blocks, const int32_t* members, int nblocks,
+                           float2* U, cudaStream_t s);
+cudaError_t launch_tc_apply5(float2* psi, int n, const float2* U, const TcBlock& blk,
+                             int* status, int grid, cudaStream_t s);
 // p[i] = (i == 0 ? first : rest) for i in [0, count).
 cudaError_t launch_fill(float2* p, int64_t count, float2 first, float2 rest, int grid,
                         cudaStream_t s);

@@ -1,0 +1,309 @@
+// Tensor-core forward path for wide rows: gates fused into 5-qubit blocks
+// (plan_tc_blocks on the host), each block applied to the whole state in one
+// launch as a real GEMM on the 5th-generation tensor cores.
+//
+// A block's 32 x 32 complex matrix U acts on the 32 amplitudes of every
+// group (the index bits outside the block's 5 target bits fixed).  In real
+// form, with amplitudes interleaved (re, im), U is a 64 x 64 real matrix R
+// (R[2i][2j] = Re U_ij, R[2i][2j+1] = -Im U_ij, R[2i+1][2j] = Im U_ij,
+// R[2i+1][2j+1] = Re U_ij), and a chunk of 128 groups is the GEMM
+//   D[128 x 64] = A[128 x 64] * R^T,   A[g][2j + c] = component c of amplitude j of group g.
+// The MMA is tcgen05.mma kind::tf32 with fp32 accumulation in TMEM.  Split
+// 3xTF32 keeps fp32 accuracy: A = A_hi + A_lo and R = R_hi + R_lo with
+// *_hi rounded to tf32, and D = A_lo R_hi + A_hi R_lo + A_hi R_hi (the
+// A_lo R_lo term is below fp32 rounding).
+//
+// tc_fuse_kernel builds U for every block in complex128 (one thread per
+// column) from the member gates' bound complex64 matrices; tc_apply5_kernel
+// streams the state: each of 128 threads gathers its group's 32 amplitudes,
+// splits them into the two A operands in shared memory (canonical K-major
+// no-swizzle layout, core matrices of 8 rows x 16 bytes), one thread issues
+// 24 MMAs (3 products x 8 K-steps of 8) and commits them to an mbarrier, and
+// each warp reads its 32 TMEM lanes (its 32 groups) back and stores them in
+// place.  The next chunk's gathers are in flight while the MMAs run.
+//
+// Every wait is bounded: on a timeout the kernel records status 1, waits
+// (bounded) once more for its MMAs, frees its TMEM and returns.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gate_math.cuh"
+#include "kernels.h"
+
+namespace tfqg {
+namespace {
+
+constexpr int kTcRows = 128;            // groups per chunk (MMA M)
+constexpr int kTcKdim = 64;             // real K: 32 complex amplitudes
+constexpr int kTcNdim = 64;             // real N
+constexpr uint32_t kTcTmemCols = 64;    // fp32 accumulator columns
+constexpr uint32_t kTcSpin = 1u << 22;  // bounded mbarrier polls
+constexpr uint32_t kTcSbo = (kTcKdim / 4) * 128u;  // bytes between 8-row groups
+constexpr size_t kTcAbytes = size_t(kTcRows) * kTcKdim * 4;  // 32 KiB
+constexpr size_t kTcBbytes = size_t(kTcNdim) * kTcKdim * 4;  // 16 KiB
+constexpr size_t kTcSmem = 2 * kTcAbytes + 2 * kTcBbytes + 64;
+
+// byte offset of element (row, k) in the K-major no-swizzle layout with 64
+// columns: 8-row groups kTcSbo apart, 16-byte core-matrix rows, 128-byte core
+// matrices along K
+__device__ __forceinline__ uint32_t kmaj(int row, int k) {
+  return uint32_t(row >> 3) * kTcSbo + uint32_t(k >> 2) * 128u + uint32_t(row & 7) * 16u +
+         uint32_t(k & 3) * 4u;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// shared-memory matrix descriptor: start, leading byte offset (along K),
+// stride byte offset (between 8-row groups), version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+         (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+
+// kind::tf32 instruction descriptor: fp32 D, tf32 A and B, K-major, N>>3, M>>4
+__device__ __forceinline__ uint32_t idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(n >> 3) << 17) |
+         (uint32_t(m >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// x rounded to the nearest tf32 value (10 mantissa bits), as an fp32
+__device__ __forceinline__ float tf32_hi(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, "
+      "%9, %10, %11, %12, %13, %14, %15}, [%16];\n"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+        "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+}
+
+// index of group g: g's bits deposited into the bits that are not targets
+// (targets ascending)
+__device__ __forceinline__ int64_t group_base(int64_t g, const int* t) {
+#pragma unroll
+  for (int i = 0; i < kTcBits; ++i) {
+    const int64_t low = (int64_t(1) << t[i]) - 1;
+    g = ((g & ~low) << 1) | (g & low);
+  }
+  return g;
+}
+
+__global__ void tc_fuse_kernel(BatchDevice b, const float2* mats, int row,
+                               const TcBlock* blocks, const int32_t* members, int nblocks,
+                               float2* U) {
+  const int blk = blockIdx.x, j = threadIdx.x;
+  if (blk >= nblocks || j >= 32) return;
+  const DevRow r = b.rows[row];
+  const DevProgram p = b.programs[r.program];
+  const GateTemplate* gates = b.gates + p.gate_begin;
+  const float2* m0 = mats + int64_t(r.mat_offset) * 16;
+  Cx<double> col[32];
+  tc_block_column(gates, members, blocks[blk], j,
+                  [&](int k, Cx<double>* m) {
+                    const float2* src = m0 + int64_t(k) * 16;
+                    for (int i = 0; i < 16; ++i) m[i] = Cx<double>(src[i].x, src[i].y);
+                  },
+                  col);
+  float2* dst = U + int64_t(blk) * 1024;
+  for (int i = 0; i < 32; ++i) dst[i * 32 + j] = make_float2(float(col[i].re), float(col[i].im));
+}
+
+__global__ void __launch_bounds__(kTcRows, 2)
+tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
+                 uint32_t tpack, int* status) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  float* a_hi = reinterpret_cast<float*>(tc_smem);
+  float* a_lo = reinterpret_cast<float*>(tc_smem + kTcAbytes);
+  float* b_hi = reinterpret_cast<float*>(tc_smem + 2 * kTcAbytes);
+  float* b_lo = reinterpret_cast<float*>(tc_smem + 2 * kTcAbytes + kTcBbytes);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tc_smem + 2 * kTcAbytes + 2 * kTcBbytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+  int* timed_out = reinterpret_cast<int*>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  int t[kTcBits];
+#pragma unroll
+  for (int i = 0; i < kTcBits; ++i) t[i] = int((tpack >> (5 * i)) & 31u);
+  uint32_t off[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int i = 0; i < kTcBits; ++i) o |= uint32_t((j >> i) & 1) << t[i];
+    off[j] = o;
+  }
+
+  // B operands: R in real form, split into tf32 hi and lo
+  for (int idx = tid; idx < kTcNdim * kTcKdim; idx += blockDim.x) {
+    const int nr = idx / kTcKdim, k = idx % kTcKdim;
+    const float2 u = U[(nr >> 1) * 32 + (k >> 1)];
+    const float v = (nr & 1) ? ((k & 1) ? u.x : u.y) : ((k & 1) ? -u.y : u.x);
+    const float hi = tf32_hi(v);
+    const uint32_t o = kmaj(nr, k) >> 2;
+    b_hi[o] = hi;
+    b_lo[o] = v - hi;
+  }
+  if (tid == 0) {
+    *timed_out = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTcTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  const int64_t nchunk = int64_t(1) << (n - kTcBits - 7);
+  int64_t chunk = blockIdx.x;
+  float2 v[32];
+  if (chunk < nchunk) {
+    const float2* src = psi + group_base(chunk * kTcRows + tid, t);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
+  }
+  uint32_t parity = 0;
+  bool failed = false;
+  while (chunk < nchunk) {
+    // A operands of this chunk: row tid, 16-byte pieces of two amplitudes
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const float x0 = v[2 * q].x, y0 = v[2 * q].y, x1 = v[2 * q + 1].x, y1 = v[2 * q + 1].y;
+      const float4 hi = make_float4(tf32_hi(x0), tf32_hi(y0), tf32_hi(x1), tf32_hi(y1));
+      const float4 lo = make_float4(x0 - hi.x, y0 - hi.y, x1 - hi.z, y1 - hi.w);
+      const uint32_t o = kmaj(tid, 4 * q);
+      *reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(a_hi) + o) = hi;
+      *reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(a_lo) + o) = lo;
+    }
+    // operands written by the generic proxy are read by the tensor core
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (tid == 0) {
+      const uint32_t idesc = idesc_tf32(kTcRows, kTcNdim);
+      const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
+      const uint32_t bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+      const uint32_t as[3] = {al, ah, ah}, bs[3] = {bh, bl, bh};
+      uint32_t acc = 0;
+      for (int pr = 0; pr < 3; ++pr)
+        for (int s = 0; s < kTcKdim / 8; ++s) {
+          const uint64_t ad = smem_desc(as[pr] + uint32_t(s) * 256u, 128u, kTcSbo);
+          const uint64_t bd = smem_desc(bs[pr] + uint32_t(s) * 256u, 128u, kTcSbo);
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+              : "memory");
+          acc = 1;
+        }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+              smem_u32(bar))
+          : "memory");
+    }
+    const int64_t next = chunk + gridDim.x;
+    if (next < nchunk) {  // the next chunk's gathers overlap the MMAs
+      const float2* src = psi + group_base(next * kTcRows + tid, t);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
+    }
+    bool done = false;
+    for (uint32_t it = 0; it < kTcSpin && !done; ++it) done = mbar_try_wait(smem_u32(bar), parity);
+    if (!done) atomicExch(timed_out, 1);
+    parity ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (*timed_out) {
+      failed = true;
+      break;
+    }
+    // D row tid (TMEM lane tid) back to the group's amplitudes
+    {
+      float2* dst = psi + group_base(chunk * kTcRows + tid, t);
+      const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16);
+      uint32_t d[64];
+      tmem_ld16(taddr, d);
+      tmem_ld16(taddr + 16u, d + 16);
+      tmem_ld16(taddr + 32u, d + 32);
+      tmem_ld16(taddr + 48u, d + 48);
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        dst[off[i]] = make_float2(__uint_as_float(d[2 * i]), __uint_as_float(d[2 * i + 1]));
+    }
+    // TMEM and the A operands are free for the next chunk
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    chunk = next;
+  }
+  if (failed) {
+    // the MMAs may still be running: wait for them (bounded) before freeing
+    bool done = false;
+    for (uint32_t it = 0; it < kTcSpin && !done; ++it)
+      done = mbar_try_wait(smem_u32(bar), parity ^ 1u);
+    if (tid == 0) atomicExch(status, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                 "r"(kTcTmemCols)
+                 : "memory");
+}
+
+}  // namespace
+
+const void* tc_apply5_kernel_ptr() { return reinterpret_cast<const void*>(&tc_apply5_kernel); }
+size_t tc_apply5_smem_bytes() { return kTcSmem; }
+
+cudaError_t launch_tc_fuse(const BatchDevice& b, const float2* mats, int row,
+                           const TcBlock* blocks, const int32_t* members, int nblocks,
+                           float2* U, cudaStream_t s) {
+  if (nblocks <= 0) return cudaSuccess;
+  tc_fuse_kernel<<<nblocks, 32, 0, s>>>(b, mats, row, blocks, members, nblocks, U);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_apply5(float2* psi, int n, const float2* U, const TcBlock& blk,
+                             int* status, int grid, cudaStream_t s) {
+  if (n < kTcBits + 7 || n > 31) return cudaErrorInvalidValue;
+  uint32_t tpack = 0;
+  for (int i = 0; i < kTcBits; ++i) {
+    if (blk.tgt[i] >= n || (i > 0 && blk.tgt[i] <= blk.tgt[i - 1])) return cudaErrorInvalidValue;
+    tpack |= uint32_t(blk.tgt[i]) << (5 * i);
+  }
+  const int64_t nchunk = int64_t(1) << (n - kTcBits - 7);
+  if (grid > nchunk) grid = int(nchunk);
+  tc_apply5_kernel<<<grid, kTcRows, kTcSmem, s>>>(psi, n, U, tpack, status);
+  return cudaGetLastError();
+}
+
+}  // namespace tfqg

@@ -176,6 +176,20 @@ struct DevRow {
   uint64_t dmat_offset;  // first derivative matrix slot of this row
 };
 
+// A fused block of the tensor-core forward path: the gates
+// members[member_begin, member_end) of one program (template indices, time
+// order) act only on the 5 bits tgt[0] < ... < tgt[4]; their product is a
+// 32 x 32 complex matrix whose index bit i is tgt[i].  Bits beyond the
+// members' own are padding (the product is the identity on them).
+constexpr int kTcBits = 5;
+struct TcBlock {
+  uint32_t member_begin, member_end;
+  uint8_t tgt[kTcBits];
+  uint8_t used;        // bits that some member touches (<= 5)
+  uint8_t pad_[2];
+};
+static_assert(sizeof(TcBlock) == 16, "TcBlock layout");
+
 #if defined(__CUDACC__) || defined(__CUDACC_RTC__)
 #define TFQG_TYPES_HD __host__ __device__ __forceinline__
 #else
