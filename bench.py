@@ -47,9 +47,10 @@ def parse():
     ap.add_argument("--c4-grid", default="5x6",
                     help="rows x cols of the C4 grid circuit (5x6 = 30 qubits; a smaller "
                          "grid gives a profiling case of the same kernels)")
-    ap.add_argument("--tensor-cores", action="store_true",
+    ap.add_argument("--tensor-cores", default="auto", choices=["auto", "on", "off"],
                     help="c4: forward passes as 5-qubit fused blocks on the tensor cores "
-                         "(split 3xTF32), one HBM sweep per block")
+                         "(split 3xTF32), one HBM sweep per block; auto (the library "
+                         "default) for rows of 24 qubits and more, off: tile passes")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default): the headline expectation + adjoint line; "
                          "c1, c3, c4, c5: the other benchmark configurations, "
@@ -300,6 +301,7 @@ def tc_kernel_roofline(n, batch, dev, launches=10):
     ok = int(st.item()) == 0
     del psi
     return {"bound": "hbm", "kernel": "tc_apply5_kernel", "targets": list(tgt),
+            "grid": _native.tc_grid(),
             "ms_per_launch": ms, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "status_ok": ok,
             "algorithmic": f"16 B x 2^{n} amplitudes per launch (state > L2)",
@@ -329,9 +331,9 @@ def run_config(args):
         w = workloads.noisy_brickwall(64, 14, 15, 0.01, seed=1)
         units, unit = 64 * 2000, "trajectories/s"
     kind = ops.KIND_NOISY if wl == "c5" else ops.KIND_FORWARD
-    tc = wl == "c4" and args.tensor_cores
-    if tc:
-        __import__("quantum_gb300")._native.set_tensor_core_gates(True)
+    if wl == "c4":
+        __import__("quantum_gb300")._native.set_tensor_core_gates(
+            {"auto": 2, "on": 1, "off": 0}[args.tensor_cores])
     t0 = time.perf_counter()
     batch = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
     parse_s = time.perf_counter() - t0
@@ -379,6 +381,7 @@ def run_config(args):
                                       [w["pauli_sums"][i] for i in rows])
         line["accuracy"] = {"max_abs": float(np.abs(out.cpu().numpy()[rows] - want).max()),
                             "rows": len(rows)}
+    tc = wl == "c4" and __import__("quantum_gb300")._native.tc_blocks(batch._h, 0) > 0
     if tc:
         line["tensor_core_blocks"] = __import__("quantum_gb300")._native.tc_blocks(batch._h, 0)
         line["tc_block_kernel"] = tc_kernel_roofline(w["n"], batch, dev)
@@ -390,15 +393,24 @@ def run_config(args):
         from quantum_gb300 import _native
         fused = float(out.cpu().numpy()[0, 0])
         batch.close()
-        prev = _native.set_gate_fusion(False)
-        try:
-            ub = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
-        finally:
-            _native.set_gate_fusion(prev)
-        unfused = float(ub.expectation(vals).cpu().numpy()[0, 0])
-        ub.close()
-        line["accuracy"] = {"sum_z_fused": fused, "sum_z_unfused": unfused,
-                            "abs_diff_fused_vs_unfused": abs(fused - unfused)}
+        if tc:
+            # tensor-core blocks against the tile passes on the FP32 pipe
+            _native.set_tensor_core_gates(False)
+            tb = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
+            tile = float(tb.expectation(vals).cpu().numpy()[0, 0])
+            tb.close()
+            line["accuracy"] = {"sum_z_tensor_core": fused, "sum_z_tile_passes": tile,
+                                "abs_diff": abs(fused - tile)}
+        else:
+            prev = _native.set_gate_fusion(False)
+            try:
+                ub = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
+            finally:
+                _native.set_gate_fusion(prev)
+            unfused = float(ub.expectation(vals).cpu().numpy()[0, 0])
+            ub.close()
+            line["accuracy"] = {"sum_z_fused": fused, "sum_z_unfused": unfused,
+                                "abs_diff_fused_vs_unfused": abs(fused - unfused)}
     if wl == "c3":
         line["per_n_bucket"] = c3_buckets(w, dev)
     print(json.dumps(line), flush=True)

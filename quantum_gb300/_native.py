@@ -205,14 +205,16 @@ def set_gate_fusion(on):
     return bool(f(1 if on else 0))
 
 
-def set_tensor_core_gates(on):
+def set_tensor_core_gates(mode):
     """Forward passes of wide rows as 5-qubit fused blocks on the tensor
-    cores (on) or as tile passes on the FP32 pipe (off, the default), for
-    calls made from now on; returns the previous setting."""
+    cores: False / 0 never (tile passes on the FP32 pipe), True / 1 always,
+    "auto" / 2 (the default) for rows of 24 qubits and more; for calls made
+    from now on.  Returns the previous mode (0, 1 or 2)."""
     f = lib().tfqg_internal_set_tensor_core_gates
     f.argtypes = [ctypes.c_int]
     f.restype = ctypes.c_int
-    return bool(f(1 if on else 0))
+    m = 2 if mode == "auto" else int(mode)
+    return int(f(m))
 
 
 def tc_apply(psi_ptr, n, u_ptr, targets, status_ptr, stream=0, grid=0):
@@ -230,9 +232,17 @@ def tc_apply(psi_ptr, n, u_ptr, targets, status_ptr, stream=0, grid=0):
         raise RuntimeError(f"tc_apply launch failed: cudaError {rc}")
 
 
+def tc_grid():
+    """CTAs of a tensor-core block launch on the current device."""
+    f = lib().tfqg_internal_tc_grid
+    f.argtypes = []
+    f.restype = ctypes.c_int
+    return int(f())
+
+
 def tc_blocks(handle, k):
-    """Tensor-core blocks of the k-th wide row of a batch (-1: no plan, or
-    the batch has not run on the tensor-core path yet)."""
+    """Tensor-core blocks that the k-th wide row of a batch ran in its last
+    forward call (-1: it ran tile passes, or has not run)."""
     f = lib().tfqg_internal_tc_blocks
     f.argtypes = [c_void_p, ctypes.c_int64]
     f.restype = ctypes.c_int

@@ -139,8 +139,12 @@ int wide_min_qubits() { return g_wide_min_qubits.load(); }
 std::atomic<int> g_gate_fusion{1};
 
 // Forward passes of wide rows as 5-bit fused blocks on the tensor cores
-// (tc_gates.cu) instead of tile passes on the FP32 pipe.
-std::atomic<int> g_tc_gates{0};
+// (tc_gates.cu) instead of tile passes on the FP32 pipe: 0 never, 1 always,
+// 2 (default) for rows of at least kTcAutoMinQubits qubits, whose states
+// (128 MiB and up) no longer fit in L2, so that every pass is an HBM sweep
+// and fewer, fuller sweeps win.
+std::atomic<int> g_tc_gates{2};
+constexpr int kTcAutoMinQubits = 24;
 
 }  // namespace
 
@@ -733,6 +737,7 @@ void tc_prepare(tfqg_batch* b, cudaStream_t s) {
                                    &b->tc_blocks, &b->tc_members);
     b->tc_rows.emplace_back(first, ok ? int32_t(b->tc_blocks.size()) - first : -1);
   }
+  b->tc_ran.assign(b->wide_rows.size(), 0);
   const size_t bb = b->tc_blocks.size() * sizeof(TcBlock);
   const size_t mb = b->tc_members.size() * sizeof(int32_t);
   b->tc_tab.reserve(align256(bb) + mb + 256, b->device);
@@ -748,14 +753,25 @@ void tc_prepare(tfqg_batch* b, cudaStream_t s) {
   b->tc_planned = true;
 }
 
+// Grid of the tensor-core block kernel: its resident CTAs per SM (two: 96
+// KiB of operands each, with the shared-memory carveout at its maximum) x SMs.
+int tc_grid(int dev) {
+  const void* k = tc_apply5_kernel_ptr();
+  TFQG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  return occupancy_grid(k, 128, tc_apply5_smem_bytes(), dev);
+}
+
 // The forward passes of wide row `row` (the k-th wide row) as tensor-core
 // blocks: fused matrices, |0...0>, one launch per block.  False when the row
 // has no block plan (a gate on more than 5 bits).
 bool run_wide_tc(tfqg_batch* b, const BatchDevice& bd, const RunArgs* a, size_t k, int row,
                  float2* psi, int sms, cudaStream_t s) {
   const std::pair<int32_t, int32_t> rp = b->tc_rows[k];
+  b->tc_ran[k] = 0;
   if (rp.second < 0) return false;
   const int n = b->programs[b->rows[size_t(row)].program].n;
+  if (g_tc_gates.load() == 2 && n < kTcAutoMinQubits) return false;
+  b->tc_ran[k] = 1;
   unsigned char* base = static_cast<unsigned char*>(b->tc_tab.p);
   const TcBlock* dblocks = reinterpret_cast<const TcBlock*>(base) + rp.first;
   const int32_t* dmembers = reinterpret_cast<const int32_t*>(
@@ -764,8 +780,7 @@ bool run_wide_tc(tfqg_batch* b, const BatchDevice& bd, const RunArgs* a, size_t 
   TFQG_CUDA(launch_tc_fuse(bd, a->mats, row, dblocks, dmembers, rp.second, U, s));
   TFQG_CUDA(launch_fill(psi, int64_t(1) << n, make_float2(1.f, 0.f), make_float2(0.f, 0.f),
                         sms * 4, s));
-  const int grid = occupancy_grid(tc_apply5_kernel_ptr(), 128, tc_apply5_smem_bytes(),
-                                  b->device);
+  const int grid = tc_grid(b->device);
   for (int i = 0; i < rp.second; ++i)
     TFQG_CUDA(launch_tc_apply5(psi, n, U + int64_t(i) * 1024,
                                b->tc_blocks[size_t(rp.first + i)],
@@ -789,6 +804,7 @@ void run_wide(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a,
   TFQG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const bool tc = g_tc_gates.load() != 0;
   if (tc) tc_prepare(b, s);
+  else if (b->tc_planned) b->tc_ran.assign(b->wide_rows.size(), 0);
   for (size_t wk = 0; wk < b->wide_rows.size(); ++wk) {
     const int32_t row = b->wide_rows[wk];
     const DevRow& r = b->rows[size_t(row)];
@@ -1624,10 +1640,13 @@ int tfqg_internal_set_gate_fusion(int on) {
   return g_gate_fusion.exchange(on ? 1 : 0);
 }
 
-// Forward passes of wide rows on the tensor cores (1: 5-bit fused blocks,
-// tc_gates.cu) or as tile passes (0, the default), for calls made after this
-// one; returns the previous setting.
-int tfqg_internal_set_tensor_core_gates(int on) { return g_tc_gates.exchange(on ? 1 : 0); }
+// Forward passes of wide rows as 5-bit fused blocks on the tensor cores
+// (tc_gates.cu): 0 never (tile passes), 1 always, 2 (default) for rows of
+// 24 qubits and more; for calls made after this one.  Returns the previous
+// setting.
+int tfqg_internal_set_tensor_core_gates(int mode) {
+  return g_tc_gates.exchange(mode < 0 || mode > 2 ? 2 : mode);
+}
 
 // One launch of the tensor-core block kernel on a caller's state: psi (2^n
 // complex64, device), U (32 x 32 complex64 row-major, device), tgt (5
@@ -1645,7 +1664,7 @@ int tfqg_internal_tc_apply(void* psi, int n, const void* U, const int32_t* tgt, 
   if (e != cudaSuccess) return int(e);
   if (grid <= 0) {
     try {
-      grid = occupancy_grid(tc_apply5_kernel_ptr(), 128, tc_apply5_smem_bytes(), dev);
+      grid = tc_grid(dev);
     } catch (const Error&) {
       return int(cudaErrorInvalidValue);
     }
@@ -1654,13 +1673,25 @@ int tfqg_internal_tc_apply(void* psi, int n, const void* U, const int32_t* tgt, 
                               status, grid, static_cast<cudaStream_t>(stream)));
 }
 
-// Tensor-core blocks of the k-th wide row of a batch (-1: no block plan or
-// not planned yet), and the kernels' status word (nonzero: an MMA
-// completion wait timed out); synchronizes the device when reading it.
+// CTAs of a tensor-core block launch on the current device (-1 on error).
+int tfqg_internal_tc_grid() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  try {
+    return tc_grid(dev);
+  } catch (const Error&) {
+    return -1;
+  }
+}
+
+// Tensor-core blocks that the k-th wide row of a batch ran in its last
+// forward call (-1: it ran tile passes, or has not run), and the kernels'
+// status word (nonzero: an MMA completion wait timed out); synchronizes the
+// device when reading it.
 int tfqg_internal_tc_blocks(void* batch, int64_t k) {
   const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
   if (!b || !b->tc_planned || k < 0 || k >= int64_t(b->tc_rows.size())) return -1;
-  return b->tc_rows[size_t(k)].second;
+  return b->tc_ran[size_t(k)] ? b->tc_rows[size_t(k)].second : -1;
 }
 int tfqg_internal_tc_status(void* batch) {
   tfqg_batch* b = static_cast<tfqg_batch*>(batch);

@@ -1200,47 +1200,100 @@ void plan_program(CompiledProgram* p, JobKind kind, bool fuse) {
 bool plan_tc_blocks(const GateTemplate* gates, int num_gates, int n,
                     std::vector<TcBlock>* blocks, std::vector<int32_t>* members) {
   if (n < kTcBits + 7 || n > 31) return false;
-  struct Open {
-    uint32_t mask = 0;
-    std::vector<int32_t> gates;
-  };
-  std::vector<Open> open;
-  int last[32];
-  for (int q = 0; q < 32; ++q) last[q] = -1;
+  // the gates and their bit masks; dependencies: the previous gate on each bit
+  std::vector<int32_t> gi;
+  std::vector<uint32_t> mask;
   for (int k = 0; k < num_gates; ++k) {
     const GateTemplate& g = gates[k];
     if (g.kind == GK_FUSED || g.cls == GC_SKIP) continue;
     uint32_t q = g.cmask | (1u << g.b0);
     if (g.nq == 2) q |= 1u << g.b1;
     if (__builtin_popcount(q) > kTcBits) return false;
-    int latest = -1;
-    for (int b = 0; b < n; ++b)
-      if ((q >> b) & 1u) latest = std::max(latest, last[b]);
-    int chosen = -1;
-    for (int c = std::max(latest, 0); c < int(open.size()); ++c)
-      if (__builtin_popcount(open[size_t(c)].mask | q) <= kTcBits) {
-        chosen = c;
-        break;
-      }
-    if (chosen < 0) {
-      chosen = int(open.size());
-      open.emplace_back();
-    }
-    open[size_t(chosen)].mask |= q;
-    open[size_t(chosen)].gates.push_back(k);
-    for (int b = 0; b < n; ++b)
-      if ((q >> b) & 1u) last[b] = chosen;
+    gi.push_back(k);
+    mask.push_back(q);
   }
-  for (const Open& o : open) {
+  const int G = int(gi.size());
+  std::vector<std::vector<int32_t>> users(static_cast<size_t>(G));
+  std::vector<int32_t> indeg(size_t(G), 0);
+  {
+    int lastg[32];
+    for (int b = 0; b < 32; ++b) lastg[b] = -1;
+    for (int i = 0; i < G; ++i) {
+      int prev[kTcBits], np = 0;
+      for (int b = 0; b < n; ++b) {
+        if (!((mask[size_t(i)] >> b) & 1u)) continue;
+        const int d = lastg[b];
+        bool seen = d < 0;
+        for (int t = 0; t < np && !seen; ++t) seen = prev[t] == d;
+        if (!seen) {
+          prev[np++] = d;
+          users[size_t(d)].push_back(i);
+          ++indeg[size_t(i)];
+        }
+        lastg[b] = i;
+      }
+    }
+  }
+  std::vector<int32_t> front;
+  for (int i = 0; i < G; ++i)
+    if (indeg[size_t(i)] == 0) front.push_back(i);
+  // Grows a block from `seed`: repeatedly takes the front gate that adds the
+  // fewest new bits (the earliest on ties) while the block stays within 5 bits.
+  auto grow = [&](int seed, std::vector<int32_t>* fr, std::vector<int32_t>* deg,
+                  std::vector<int32_t>* taken, uint32_t* bits) {
+    uint32_t S = 0;
+    int pick = seed;
+    while (pick >= 0) {
+      S |= mask[size_t(pick)];
+      taken->push_back(pick);
+      fr->erase(std::find(fr->begin(), fr->end(), pick));
+      for (const int32_t u : users[size_t(pick)])
+        if (--(*deg)[size_t(u)] == 0) fr->insert(std::upper_bound(fr->begin(), fr->end(), u), u);
+      pick = -1;
+      int best_add = kTcBits + 1;
+      for (const int32_t f : *fr) {
+        const int tot = __builtin_popcount(S | mask[size_t(f)]);
+        const int add = tot - __builtin_popcount(S);
+        if (tot <= kTcBits && add < best_add) {
+          best_add = add;
+          pick = f;
+        }
+      }
+    }
+    *bits = S;
+  };
+  // Each block takes the seed (a front gate) whose block absorbs the most gates.
+  int done = 0;
+  std::vector<int32_t> fr, deg, taken, best_fr, best_deg, best_taken;
+  while (done < G) {
+    uint32_t best_bits = 0;
+    best_taken.clear();
+    for (const int32_t seed : front) {
+      fr = front;
+      deg = indeg;
+      taken.clear();
+      uint32_t bits = 0;
+      grow(seed, &fr, &deg, &taken, &bits);
+      if (taken.size() > best_taken.size()) {
+        best_taken.swap(taken);
+        best_fr.swap(fr);
+        best_deg.swap(deg);
+        best_bits = bits;
+      }
+    }
+    if (best_taken.empty()) return false;  // unreachable: any seed takes itself
+    front.swap(best_fr);
+    indeg.swap(best_deg);
+    done += int(best_taken.size());
     TcBlock t{};
-    t.used = uint8_t(__builtin_popcount(o.mask));
-    uint32_t m = o.mask;
+    t.used = uint8_t(__builtin_popcount(best_bits));
+    uint32_t m = best_bits;
     for (int b = n - 1; b >= 0 && __builtin_popcount(m) < kTcBits; --b) m |= 1u << b;
-    int i = 0;
+    int k = 0;
     for (int b = 0; b < n; ++b)
-      if ((m >> b) & 1u) t.tgt[i++] = uint8_t(b);
+      if ((m >> b) & 1u) t.tgt[k++] = uint8_t(b);
     t.member_begin = uint32_t(members->size());
-    members->insert(members->end(), o.gates.begin(), o.gates.end());
+    for (const int32_t x : best_taken) members->push_back(gi[size_t(x)]);
     t.member_end = uint32_t(members->size());
     blocks->push_back(t);
   }

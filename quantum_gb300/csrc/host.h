@@ -119,15 +119,19 @@ uint8_t classify_gate(const GateTemplate& g);
 // Plans forward (and, for the adjoint, backward) passes.
 void plan_program(CompiledProgram* prog, JobKind kind, bool fuse = false);
 
-// Tensor-core blocks of a forward program (tc_gates.cu): its gates in
-// program order (gates[0, num_gates), GK_FUSED products and identities
+// Tensor-core blocks of a forward program (tc_gates.cu): its gates
+// (gates[0, num_gates) in program order, GK_FUSED products and identities
 // skipped) grouped into blocks of at most 5 bits each, appended to `blocks`
-// and `members` (member ranges index `members`).  A gate joins the latest
-// block that touches any of its bits, or a later one, when the union stays
-// within 5 bits (it commutes with every block in between); otherwise it opens
-// a new block.  Blocks are padded to 5 bits with the highest free bits, which
-// keeps the low index bits for coalesced group addressing.  Returns false
-// (and appends nothing) when a gate spans more than 5 bits or n < 5 + 7.
+// and `members` (member ranges index `members`).  A gate depends on the
+// previous gate on each of its bits (targets and controls); the "front" is
+// the gates whose dependencies are all placed.  A block grows from a front
+// gate by taking, again and again, the front gate that adds the fewest new
+// bits while the block stays within 5 bits; of all front gates as seeds,
+// the one whose block takes the most gates wins.  Members are in the order
+// taken, which respects every dependency.  Blocks are padded to 5 bits with
+// the highest free bits, which keeps the low index bits for coalesced group
+// addressing.  Returns false (appending nothing) when a gate spans more than
+// 5 bits or n is outside [12, 31].
 bool plan_tc_blocks(const GateTemplate* gates, int num_gates, int n,
                     std::vector<TcBlock>* blocks, std::vector<int32_t>* members);
 

@@ -106,3 +106,25 @@ def test_grid_fsim_row_matches_oracle_and_tile_passes(tensor_core_wide):
     _native.set_tensor_core_gates(False)
     tile = ops.Batch(w["programs"], [], None).state(values)
     np.testing.assert_allclose(got, tile, atol=1e-5, rtol=0)
+
+
+def test_auto_mode_takes_rows_of_24_qubits():
+    """By default only rows of 24+ qubits (states beyond L2) run the blocks;
+    a 24-qubit grid circuit agrees with the tile passes on <sum Z>."""
+    old_w = _native.set_wide_min_qubits(15)
+    old_t = _native.set_tensor_core_gates("auto")
+    try:
+        small = workloads.grid_fsim(rows=3, cols=6, depth=4, seed=5)
+        b = ops.Batch(small["programs"], [], small["pauli_sums"])
+        b.expectation(small["symbol_values"])
+        assert _native.tc_blocks(b._h, 0) == -1
+        w = workloads.grid_fsim(rows=4, cols=6, depth=8, seed=6)
+        b = ops.Batch(w["programs"], [], w["pauli_sums"])
+        got = b.expectation(w["symbol_values"])
+        assert _native.tc_blocks(b._h, 0) > 0 and _native.tc_status(b._h) == 0
+        _native.set_tensor_core_gates(False)
+        tile = ops.Batch(w["programs"], [], w["pauli_sums"]).expectation(w["symbol_values"])
+        np.testing.assert_allclose(got, tile, atol=1e-5, rtol=0)
+    finally:
+        _native.set_tensor_core_gates(old_t)
+        _native.set_wide_min_qubits(old_w)
