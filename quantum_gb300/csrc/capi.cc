@@ -753,12 +753,19 @@ void tc_prepare(tfqg_batch* b, cudaStream_t s) {
   b->tc_planned = true;
 }
 
-// Grid of the tensor-core block kernel: its resident CTAs per SM (two: 96
-// KiB of operands each, with the shared-memory carveout at its maximum) x SMs.
+// Grid of the tensor-core block kernel: two CTAs per SM x SMs.  Two fit:
+// 2 x (96 KiB of operands + 1 KiB reserved) of the 228 KiB of shared memory
+// (carveout at its maximum), 2 x 128 threads x 208 registers of 64 Ki, and
+// 2 x 64 TMEM columns of 512.  The occupancy query reports one on GB300
+// (ncu reports the shared-memory and register limits as two), and with one
+// CTA per SM the kernel stalls on its gathers.  Chunks are grid-strided, so
+// a grid above the resident CTAs stays correct.
 int tc_grid(int dev) {
   const void* k = tc_apply5_kernel_ptr();
   TFQG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-  return occupancy_grid(k, 128, tc_apply5_smem_bytes(), dev);
+  int sms = 0;
+  TFQG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  return std::max(occupancy_grid(k, 128, tc_apply5_smem_bytes(), dev), 2 * sms);
 }
 
 // The forward passes of wide row `row` (the k-th wide row) as tensor-core
