@@ -83,3 +83,27 @@ def test_small_rows_have_no_plan():
     b = ops.Batch(programs, [], None, kind=ops.KIND_FORWARD)
     assert _native.tc_plan(b._h, 0, np.zeros(0, np.float32)) is None
     b.close()
+
+
+def test_gate_on_six_qubits_has_no_plan():
+    """A gate with 4 controls and 2 targets spans 6 bits: no 5-bit block
+    holds it, so the row keeps the tile passes."""
+    q = S.GridQubit.rect(1, 12)
+    wide_gate = S.CZ(q[0], q[1]).controlled_by(q[2], q[3], q[4], q[5])
+    programs = [S.serialize_circuit(S.Circuit([[S.rx(q[6], 0.3)], [wide_gate]]))]
+    b = ops.Batch(programs, [], None, kind=ops.KIND_FORWARD)
+    assert _native.tc_plan(b._h, 0, np.zeros(0, np.float32)) is None
+    b.close()
+
+
+def test_deep_random_circuits_with_two_controls():
+    """Deeper random circuits on 12 qubits, up to two controls per gate
+    (4-qubit gates): the reordering across blocks must keep every
+    dependency on targets and controls."""
+    rng = np.random.default_rng(23)
+    names = ["a", "b"]
+    qs = S.GridQubit.rect(1, 12)
+    programs = [S.serialize_circuit(random_circuit(qs, 24, rng, names, p_control=0.5))
+                for _ in range(2)]
+    values = rng.uniform(-2, 2, size=(len(programs), len(names))).astype(np.float32)
+    _check(programs, names, values)
