@@ -733,7 +733,9 @@ void tc_prepare(tfqg_batch* b, cudaStream_t s) {
   for (const int32_t row : b->wide_rows) {
     const DevProgram& p = b->programs[b->rows[size_t(row)].program];
     const int32_t first = int32_t(b->tc_blocks.size());
-    const bool ok = plan_tc_blocks(b->gates.data() + p.gate_begin, p.num_gates, p.n,
+    // channels are not gates: a noisy program keeps its tile passes
+    const bool ok = p.num_channels == 0 &&
+                    plan_tc_blocks(b->gates.data() + p.gate_begin, p.num_gates, p.n,
                                    &b->tc_blocks, &b->tc_members);
     b->tc_rows.emplace_back(first, ok ? int32_t(b->tc_blocks.size()) - first : -1);
   }
@@ -1723,7 +1725,7 @@ int tfqg_internal_tc_plan(void* batch, int64_t row, const float* row_values, int
   const GateTemplate* gates = b->gates.data() + p.gate_begin;
   std::vector<TcBlock> blocks;
   std::vector<int32_t> members;
-  if (!plan_tc_blocks(gates, p.num_gates, p.n, &blocks, &members)) {
+  if (p.num_channels != 0 || !plan_tc_blocks(gates, p.num_gates, p.n, &blocks, &members)) {
     *count = -1;
     return 0;
   }

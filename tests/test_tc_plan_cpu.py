@@ -107,3 +107,13 @@ def test_deep_random_circuits_with_two_controls():
                 for _ in range(2)]
     values = rng.uniform(-2, 2, size=(len(programs), len(names))).astype(np.float32)
     _check(programs, names, values)
+
+
+def test_noisy_program_has_no_plan():
+    """Channels are not gates: a noisy program keeps its tile passes."""
+    rng = np.random.default_rng(4)
+    qs = S.GridQubit.rect(1, 12)
+    c = random_circuit(qs, 4, rng, (), channels=("DP", "AD"), p_channel=0.3)
+    b = ops.Batch([S.serialize_circuit(c)], [], None, kind=ops.KIND_NOISY)
+    assert _native.tc_plan(b._h, 0, np.zeros(0, np.float32)) is None
+    b.close()
