@@ -117,3 +117,42 @@ def test_noisy_program_has_no_plan():
     b = ops.Batch([S.serialize_circuit(c)], [], None, kind=ops.KIND_NOISY)
     assert _native.tc_plan(b._h, 0, np.zeros(0, np.float32)) is None
     b.close()
+
+
+def _tf32_rna(x):
+    """fp32 -> nearest tf32 (10 mantissa bits), ties away from zero."""
+    u = x.astype(np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x1000) & 0xFFFFE000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def _tf32_trunc(x):
+    """What the tensor core reads of an fp32 operand: the low 13 bits dropped."""
+    return (x.astype(np.float32).view(np.uint32) & np.uint32(0xFFFFE000)).view(np.float32)
+
+
+def test_split_tf32_arithmetic_of_the_block_kernel():
+    """The block kernel's numerics, restated with numpy: the 32 x 32 complex
+    block in real form (R[2i][2j] = Re U, R[2i][2j+1] = -Im U, R[2i+1][2j] =
+    Im U, R[2i+1][2j+1] = Re U), operands split as hi = rna(x), lo = x - hi,
+    D = A_lo R_hi + A_hi R_lo + A_hi R_hi in fp32.  Its error on unit-norm
+    states stays below the 1e-6 that the GPU test demands, and a plain TF32
+    product misses it by two orders of magnitude."""
+    rng = np.random.default_rng(1)
+    z = rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))
+    U = np.linalg.qr(z)[0].astype(np.complex64)
+    R = np.zeros((64, 64), np.float32)
+    R[0::2, 0::2], R[0::2, 1::2] = U.real, -U.imag
+    R[1::2, 0::2], R[1::2, 1::2] = U.imag, U.real
+    psi = rng.normal(size=(1 << 12)) + 1j * rng.normal(size=(1 << 12))
+    psi = (psi / np.linalg.norm(psi)).astype(np.complex64).reshape(128, 32)
+    A = np.stack([psi.real, psi.imag], axis=-1).reshape(128, 64).astype(np.float32)
+    a_hi, r_hi = _tf32_rna(A), _tf32_rna(R)
+    a_lo, r_lo = _tf32_trunc(A - a_hi), _tf32_trunc(R - r_hi)
+    f32 = lambda x, y: (x.astype(np.float64) @ y.T.astype(np.float64)).astype(np.float32)
+    D = f32(a_lo, r_hi) + f32(a_hi, r_lo) + f32(a_hi, r_hi)
+    want = psi.astype(np.complex128) @ U.astype(np.complex128).T
+    got = D[:, 0::2] + 1j * D[:, 1::2]
+    assert np.abs(got - want).max() < 1e-6
+    plain = f32(_tf32_trunc(A), _tf32_trunc(R))
+    assert np.abs(plain[:, 0::2] + 1j * plain[:, 1::2] - want).max() > 1e-5
