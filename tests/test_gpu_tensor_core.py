@@ -4,9 +4,10 @@ The block kernel alone: a random 5-qubit unitary applied to a random state
 on several target sets (the lowest bits, scattered bits, the highest bits),
 against numpy in complex128.  Split 3xTF32 must keep fp32-level accuracy:
 1e-6 absolute on states of unit norm, where a plain-TF32 product is off by
-about 4e-5 at 12 qubits (test_tc_plan_cpu.py restates both with numpy).  Then whole wide rows with the tensor-core path switched
-on: states and expectations against the oracle at the tolerances of
-test_gpu_parity.py (1e-5 states, 8e-5 expectations)."""
+about 4e-5 at 12 qubits (test_tc_plan_cpu.py restates both with numpy).
+Then whole wide rows with the tensor-core path switched on: states and
+expectations against the oracle at the tolerances of test_gpu_parity.py
+(1e-5 states, 8e-5 expectations)."""
 
 import numpy as np
 import pytest
