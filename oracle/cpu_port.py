@@ -1,6 +1,7 @@
 """Python side of the CPU restatement (TEST INFRASTRUCTURE): flattens a batch
 parsed by the oracle (tfq_oracle.py) and runs oracle/cpu_ref.cc's
-expectation + adjoint loops over host threads."""
+expectation + adjoint loops (fused forward, fused partial blocks in the
+adjoint sweep, vectorized amplitude loops) over host threads."""
 
 import ctypes
 
@@ -16,7 +17,7 @@ def _load():
     global _lib
     if _lib is None:
         _lib = ctypes.CDLL(build_cpu.build())
-        _lib.cpuref_expect_adj.restype = ctypes.c_int
+        _lib.cpuref_run.restype = ctypes.c_int
         _lib.cpuref_num_threads.restype = ctypes.c_int
     return _lib
 
@@ -83,18 +84,21 @@ class Flat:
             tco=np.array(tco, np.float32), foff=np.array(foff, np.int64),
             fbit=i32(fbit), ftyp=np.array(ftyp or [b"Z"], dtype="S1"))
 
-    def run(self, downstream_grads, threads=0):
+    def run(self, downstream_grads, threads=0, expectation=True, adjoint=True):
+        """One expectation op and / or one adjoint-gradient op over the
+        rows; returns (expectations [rows, n_ops], gradients [rows, P])."""
         lib = _load()
         a = self.a
         dg = np.ascontiguousarray(np.asarray(downstream_grads, np.float32))
         exp = np.zeros((self.rows, self.n_ops), np.float32)
         grad = np.zeros((self.rows, self.num_symbols), np.float32)
         p = lambda x: x.ctypes.data_as(ctypes.c_void_p)
-        lib.cpuref_expect_adj(
+        lib.cpuref_run(
             ctypes.c_int(self.rows), p(a["n"]), p(a["goff"]), p(a["nq"]),
             p(a["b0"]), p(a["b1"]), p(a["cm"]), p(a["cv"]), p(a["mats"]),
             p(a["ng"]), p(a["gc"]), p(a["dm"]), p(a["toff"]), p(a["top"]),
             p(a["tco"]), p(a["foff"]), p(a["fbit"]), p(a["ftyp"]),
             ctypes.c_int(self.n_ops), ctypes.c_int(self.num_symbols), p(dg),
-            p(exp), p(grad), ctypes.c_int(threads))
+            p(exp), p(grad), ctypes.c_int(threads), ctypes.c_int(int(expectation)),
+            ctypes.c_int(int(adjoint)))
         return exp, grad
