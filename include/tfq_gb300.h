@@ -212,6 +212,38 @@ int tfqg_simulate_expectation(const char* const* programs,
                               const int64_t* pauli_sum_lens, int64_t num_ops,
                               float* expectations);
 
+/* The largest qubit count among the programs: the output width of the
+ * state op (2^max) and of the samples op (max), which the reference's
+ * Compute derives from the parsed programs before allocate_output
+ * (GetProgramsAndNumQubits, parse_context.cc:268-320; used by
+ * tfq_simulate_state_op.cc:79-87 and tfq_simulate_samples_op.cc:76-87). */
+int tfqg_max_num_qubits(const char* const* programs, const int64_t* program_lens,
+                        int64_t batch, int32_t* max_num_qubits);
+
+/* tfq_simulate_state (tfq_simulate_ops.py:48-70; TfqSimulateStateOp::Compute
+ * tfq_simulate_state_op.cc:48-215, registered at :221-242).  states:
+ * complex64 [batch, 2^max_num_qubits] as (re, im) float pairs; rows of
+ * fewer qubits are padded with -2 (tfq_simulate_state_op.cc:201-207).
+ * max_num_qubits must be tfqg_max_num_qubits() of the programs. */
+int tfqg_simulate_state(const char* const* programs, const int64_t* program_lens,
+                        int64_t batch, const char* const* symbol_names,
+                        const int64_t* symbol_name_lens, int64_t num_symbols,
+                        const float* symbol_values, int32_t max_num_qubits,
+                        void* states);
+
+/* tfq_simulate_samples (tfq_simulate_ops.py:73-98; TfqSimulateSamplesOp::
+ * Compute tfq_simulate_samples_op.cc:53-251, registered at :258-285).
+ * samples: int8 [batch, num_samples, max_num_qubits]; bit k of a sample in
+ * column max_num_qubits-k-1, -2 in the leading columns of smaller rows
+ * (tfq_simulate_samples_op.cc:227-243).  num_samples < 1 is
+ * INVALID_ARGUMENT (parse_context.cc:485-490).  max_num_qubits must be
+ * tfqg_max_num_qubits() of the programs. */
+int tfqg_simulate_samples(const char* const* programs, const int64_t* program_lens,
+                          int64_t batch, const char* const* symbol_names,
+                          const int64_t* symbol_name_lens, int64_t num_symbols,
+                          const float* symbol_values, int32_t num_samples, uint64_t seed,
+                          int32_t max_num_qubits, int8_t* samples);
+
 /* tfq_adj_grad (tfq_adj_grad_op.py:22-48) */
 int tfqg_adj_grad(const char* const* programs, const int64_t* program_lens,
                   int64_t batch, const char* const* symbol_names,

@@ -258,6 +258,17 @@ def tc_status(handle):
     return int(f(handle))
 
 
+def tc_inject_status(status):
+    """Test hook: calls made from now on treat the tensor-core status word
+    as `status` (nonzero: an MMA completion wait timed out), without a
+    timeout on the GPU; 0 restores the real read-back.  Returns the previous
+    setting."""
+    f = lib().tfqg_internal_tc_inject_status
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return int(f(int(status)))
+
+
 def tc_plan(handle, row, row_values, max_blocks=4096):
     """Host copy of a row's tensor-core block plan: a list of (targets,
     matrix) with the 5 target bits ascending and the 32 x 32 complex128

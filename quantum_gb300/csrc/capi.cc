@@ -145,6 +145,10 @@ std::atomic<int> g_gate_fusion{1};
 // and fewer, fuller sweeps win.
 std::atomic<int> g_tc_gates{2};
 constexpr int kTcAutoMinQubits = 24;
+// Test hook: a status value the host treats as read back from the block
+// kernels of the next calls (0: read the real one).  It lets a test take
+// the timeout branch without a timeout on the GPU.
+std::atomic<int> g_tc_status_injected{0};
 
 }  // namespace
 
@@ -770,6 +774,23 @@ int tc_grid(int dev) {
   return std::max(occupancy_grid(k, 128, tc_apply5_smem_bytes(), dev), 2 * sms);
 }
 
+// After the tensor-core rows of a call: a block kernel whose MMA completion
+// wait timed out has left its row partly transformed, so the call fails
+// (INTERNAL) instead of returning that row's results.  Reading the status
+// word synchronizes the stream; calls with tensor-core rows (24 qubits and
+// more, milliseconds of device work each) are synchronous for that reason.
+void check_tc_status(tfqg_batch* b, cudaStream_t s) {
+  int v = 0;
+  TFQG_CUDA(cudaMemcpyAsync(&v, b->tc_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TFQG_CUDA(cudaStreamSynchronize(s));
+  const int injected = g_tc_status_injected.load();
+  if (injected) v = injected;
+  if (v != 0)
+    throw Error(kInternal,
+                "tensor-core block kernel: an MMA completion wait timed out; the wide "
+                "row's state is incomplete and the call's results were discarded");
+}
+
 // The forward passes of wide row `row` (the k-th wide row) as tensor-core
 // blocks: fused matrices, |0...0>, one launch per block.  False when the row
 // has no block plan (a gate on more than 5 bits).
@@ -812,8 +833,14 @@ void run_wide(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a,
   int sms = 0;
   TFQG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const bool tc = g_tc_gates.load() != 0;
-  if (tc) tc_prepare(b, s);
-  else if (b->tc_planned) b->tc_ran.assign(b->wide_rows.size(), 0);
+  if (tc) {
+    tc_prepare(b, s);
+    // each call starts with a clear status word
+    TFQG_CUDA(cudaMemsetAsync(b->tc_status.p, 0, sizeof(int), s));
+  } else if (b->tc_planned) {
+    b->tc_ran.assign(b->wide_rows.size(), 0);
+  }
+  bool any_tc = false;
   for (size_t wk = 0; wk < b->wide_rows.size(); ++wk) {
     const int32_t row = b->wide_rows[wk];
     const DevRow& r = b->rows[size_t(row)];
@@ -827,6 +854,7 @@ void run_wide(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a,
       psi = static_cast<float2*>(b->wide_state.p);
     }
     const bool tc_done = tc && run_wide_tc(b, bd, a, wk, row, psi, sms, s);
+    any_tc = any_tc || tc_done;
     for (uint32_t q = p.fwd_pass_begin; q < p.fwd_pass_end && !tc_done; ++q) {
       const int init = q == p.fwd_pass_begin ? 1 : 0;
       if (jk) {
@@ -868,6 +896,7 @@ void run_wide(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a,
       TFQG_CUDA(launch_wide_sample(bd, *a, row, psi, n, csum, s));
     }
   }
+  if (any_tc) check_tc_status(b, s);
 }
 
 // Adjoint of the wide rows, one row after another on stream s: forward
@@ -1537,6 +1566,69 @@ int tfqg_simulate_expectation(const char* const* programs,
   return rc;
 }
 
+int tfqg_max_num_qubits(const char* const* programs, const int64_t* program_lens,
+                        int64_t batch, int32_t* max_num_qubits) {
+  if (!max_num_qubits) return fail(kInvalidArgument, "max_num_qubits is NULL");
+  tfqg_batch* b = nullptr;
+  int rc = tfqg_batch_create(programs, program_lens, batch, nullptr, nullptr, 0, nullptr,
+                             nullptr, 0, TFQG_KIND_FORWARD, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_max_num_qubits(b, max_num_qubits);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
+namespace {
+// A transient forward batch whose widest program has `max_num_qubits`
+// qubits (the caller sized its output from that), or an error code.
+int forward_batch(const char* const* programs, const int64_t* program_lens, int64_t batch,
+                  const char* const* symbol_names, const int64_t* symbol_name_lens,
+                  int64_t num_symbols, int32_t max_num_qubits, tfqg_batch** out) {
+  int rc = tfqg_batch_create(programs, program_lens, batch, symbol_names, symbol_name_lens,
+                             num_symbols, nullptr, nullptr, 0, TFQG_KIND_FORWARD, out);
+  if (rc) return rc;
+  int32_t mq = 0;
+  rc = tfqg_batch_max_num_qubits(*out, &mq);
+  if (rc == 0 && mq != max_num_qubits)
+    rc = fail(kInvalidArgument, "max_num_qubits is " + std::to_string(max_num_qubits) +
+                                    " but the programs' largest qubit count is " +
+                                    std::to_string(mq));
+  if (rc) {
+    tfqg_batch_destroy(*out);
+    *out = nullptr;
+  }
+  return rc;
+}
+}  // namespace
+
+int tfqg_simulate_state(const char* const* programs, const int64_t* program_lens,
+                        int64_t batch, const char* const* symbol_names,
+                        const int64_t* symbol_name_lens, int64_t num_symbols,
+                        const float* symbol_values, int32_t max_num_qubits,
+                        void* states) {
+  tfqg_batch* b = nullptr;
+  int rc = forward_batch(programs, program_lens, batch, symbol_names, symbol_name_lens,
+                         num_symbols, max_num_qubits, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_state(b, symbol_values, states, 0, nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
+int tfqg_simulate_samples(const char* const* programs, const int64_t* program_lens,
+                          int64_t batch, const char* const* symbol_names,
+                          const int64_t* symbol_name_lens, int64_t num_symbols,
+                          const float* symbol_values, int32_t num_samples, uint64_t seed,
+                          int32_t max_num_qubits, int8_t* samples) {
+  tfqg_batch* b = nullptr;
+  int rc = forward_batch(programs, program_lens, batch, symbol_names, symbol_name_lens,
+                         num_symbols, max_num_qubits, &b);
+  if (rc) return rc;
+  rc = tfqg_batch_samples(b, symbol_values, num_samples, seed, samples, 0, nullptr);
+  tfqg_batch_destroy(b);
+  return rc;
+}
+
 int tfqg_adj_grad(const char* const* programs, const int64_t* program_lens,
                   int64_t batch, const char* const* symbol_names,
                   const int64_t* symbol_name_lens, int64_t num_symbols,
@@ -1702,6 +1794,10 @@ int tfqg_internal_tc_blocks(void* batch, int64_t k) {
   if (!b || !b->tc_planned || k < 0 || k >= int64_t(b->tc_rows.size())) return -1;
   return b->tc_ran[size_t(k)] ? b->tc_rows[size_t(k)].second : -1;
 }
+// Makes the next calls treat the tensor-core status word as `status`
+// (0 restores the real read-back); returns the previous setting.
+int tfqg_internal_tc_inject_status(int status) { return g_tc_status_injected.exchange(status); }
+
 int tfqg_internal_tc_status(void* batch) {
   tfqg_batch* b = static_cast<tfqg_batch*>(batch);
   if (!b || !b->tc_status.p) return 0;

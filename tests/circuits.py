@@ -103,3 +103,29 @@ def random_paulisum(qubits, rng, n_terms=4, identity=True):
     if identity:
         terms.append((float(rng.normal()), []))
     return S.serialize_paulisum(terms)
+
+
+def expectation_atol(pauli_sums, per_unit=1e-5):
+    """Absolute tolerance for expectations of these Pauli sums: 1e-5 per unit
+    of sum_t |c_t| (an error of 1e-5 on each term's <P_t> in [-1, 1]), the
+    largest over the batch; identity terms count, as they add exactly."""
+    from oracle import tfq_oracle as O
+    worst = 1.0
+    for row in pauli_sums:
+        for ps in row:
+            worst = max(worst, sum(abs(float(t["re"])) for t in O.decode_paulisum(ps)))
+    return per_unit * worst
+
+
+def gradient_atol(pauli_sums, downstream_grads, per_unit=1e-5):
+    """Absolute tolerance for adjoint gradients: 1e-5 per unit of the
+    weighted observable's sum_j |g_j| sum_t |c_t| (lambda's scale), the
+    largest over the batch."""
+    from oracle import tfq_oracle as O
+    g = np.abs(np.asarray(downstream_grads, np.float64))
+    worst = 1.0
+    for i, row in enumerate(pauli_sums):
+        w = sum(g[i, j] * sum(abs(float(t["re"])) for t in O.decode_paulisum(ps))
+                for j, ps in enumerate(row))
+        worst = max(worst, w)
+    return per_unit * worst

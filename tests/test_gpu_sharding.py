@@ -7,6 +7,7 @@ import pytest
 
 from oracle import tfq_oracle as O
 from quantum_gb300 import ops, sharding
+from tests.circuits import expectation_atol, gradient_atol
 from tests.test_sharding_gloo import _uneven
 
 pytestmark = pytest.mark.gpu
@@ -20,9 +21,9 @@ def test_three_way_split_reproduces_the_whole_batch():
     exp = np.concatenate([s.expectation(values) for s in shards])
     grad = np.concatenate([s.adj_grad(values, dg) for s in shards])
     np.testing.assert_allclose(exp, O.simulate_expectation(programs, names, values, psums),
-                               atol=8e-5, rtol=0)
+                               atol=expectation_atol(psums), rtol=0)
     want = O.adj_grad(programs, names, values, psums, dg)
-    np.testing.assert_allclose(grad, want, atol=2e-5 * max(1.0, np.abs(want).max()), rtol=0)
+    np.testing.assert_allclose(grad, want, atol=gradient_atol(psums, dg), rtol=0)
     fwd = [sharding.ShardedBatch(programs, names, None, rank=r, world=3) for r in range(3)]
     st = np.concatenate([s.state(values) for s in fwd])
     np.testing.assert_allclose(st, O.simulate_state(programs, names, values), atol=1e-5)

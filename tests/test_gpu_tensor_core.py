@@ -15,7 +15,7 @@ import pytest
 from oracle import tfq_oracle as O
 from quantum_gb300 import _native, ops, workloads
 from quantum_gb300 import serialize as S
-from tests.circuits import random_circuit, random_paulisum
+from tests.circuits import expectation_atol, random_circuit, random_paulisum
 
 pytestmark = pytest.mark.gpu
 
@@ -88,7 +88,7 @@ def test_wide_rows_state_and_expectation(tensor_core_wide):
     got_e = b.expectation(values)
     assert _native.tc_blocks(b._h, 0) > 0 and _native.tc_blocks(b._h, 1) > 0
     np.testing.assert_allclose(got_e, O.simulate_expectation(programs, names, values, psums),
-                               atol=8e-5, rtol=0)
+                               atol=expectation_atol(psums), rtol=0)
     sb = ops.Batch(programs, names, None)
     got_s = sb.state(values)
     np.testing.assert_allclose(got_s, O.simulate_state(programs, names, values),
@@ -129,3 +129,29 @@ def test_auto_mode_takes_rows_of_24_qubits():
     finally:
         _native.set_tensor_core_gates(old_t)
         _native.set_wide_min_qubits(old_w)
+
+
+def test_block_timeout_fails_the_call_and_is_not_sticky(tensor_core_wide):
+    """A block kernel whose MMA wait timed out leaves its row partly
+    transformed: the call must fail with INTERNAL instead of returning that
+    row, and the next call on the same batch must not inherit the failure.
+    The timeout is injected on the host (the status word the host reads
+    back), so nothing waits on the GPU."""
+    rng = np.random.default_rng(31)
+    qs = S.GridQubit.rect(1, 17)
+    programs = [S.serialize_circuit(random_circuit(qs, 6, rng, []))]
+    psums = [[random_paulisum(qs, rng)]]
+    values = np.zeros((1, 0), np.float32)
+    b = ops.Batch(programs, [], psums)
+    prev = _native.tc_inject_status(1)
+    try:
+        with pytest.raises(_native.InternalError, match="timed out"):
+            b.expectation(values)
+        with pytest.raises(_native.InternalError, match="timed out"):
+            ops.Batch(programs, [], None).state(values)
+    finally:
+        _native.tc_inject_status(prev)
+    got = b.expectation(values)
+    assert _native.tc_blocks(b._h, 0) > 0 and _native.tc_status(b._h) == 0
+    np.testing.assert_allclose(got, O.simulate_expectation(programs, [], values, psums),
+                               atol=expectation_atol(psums), rtol=0)

@@ -13,7 +13,7 @@ from scipy import stats
 from oracle import tfq_oracle as O
 from quantum_gb300 import _native, ops
 from quantum_gb300 import serialize as S
-from tests.circuits import random_circuit, random_paulisum
+from tests.circuits import expectation_atol, gradient_atol, random_circuit, random_paulisum
 
 pytestmark = pytest.mark.gpu
 
@@ -50,7 +50,7 @@ def test_expectation_mixed_wide_and_narrow(wide_from_15, jit):
         _, active, err = _native.batch_specialization(b._h)
         assert "wide" in active, err
     want = O.simulate_expectation(programs, names, values, psums)
-    np.testing.assert_allclose(got, want, atol=8e-5, rtol=0)
+    np.testing.assert_allclose(got, want, atol=expectation_atol(psums), rtol=0)
 
 
 def test_adjoint_batch_wide_row_beside_a_queued_row(wide_from_15):
@@ -60,11 +60,11 @@ def test_adjoint_batch_wide_row_beside_a_queued_row(wide_from_15):
     assert _native.batch_wide_rows(b._h) == 1
     np.testing.assert_allclose(b.expectation(values),
                                O.simulate_expectation(programs, names, values, psums),
-                               atol=8e-5, rtol=0)
+                               atol=expectation_atol(psums), rtol=0)
     dg = rng.normal(size=(2, 2)).astype(np.float32)
     want = O.adj_grad(programs, names, values, psums, dg)
     np.testing.assert_allclose(b.adj_grad(values, dg), want,
-                               atol=2e-5 * max(1.0, np.abs(want).max()), rtol=0)
+                               atol=gradient_atol(psums, dg), rtol=0)
 
 
 def test_state_with_padding(wide_from_15):
@@ -109,7 +109,7 @@ def test_default_threshold_22_qubits():
     assert _native.batch_wide_rows(b._h) == 1
     np.testing.assert_allclose(b.expectation(values),
                                O.simulate_expectation(programs, names, values, psums),
-                               atol=8e-5, rtol=0)
+                               atol=expectation_atol(psums), rtol=0)
 
 
 @pytest.mark.parametrize("rule", [ops.GRAD_REFERENCE_FD, ops.GRAD_EXACT])
@@ -125,7 +125,7 @@ def test_wide_adjoint_gradient_mixed_batch(wide_from_15, rule):
     got = b.adj_grad(values, dg, rule)
     want = O.adj_grad(programs, names, values, psums, dg,
                       grad_rule="fd" if rule == ops.GRAD_REFERENCE_FD else "exact")
-    np.testing.assert_allclose(got, want, atol=2e-5 * max(1.0, np.abs(want).max()), rtol=0)
+    np.testing.assert_allclose(got, want, atol=gradient_atol(psums, dg), rtol=0)
 
 
 def test_wide_adjoint_without_terms_is_zero(wide_from_15):
@@ -149,4 +149,4 @@ def test_wide_adjoint_default_threshold_22_qubits():
     dg = np.ones((2, 1), np.float32)
     want = O.adj_grad(programs, names, values, psums, dg)
     np.testing.assert_allclose(b.adj_grad(values, dg), want,
-                               atol=2e-5 * max(1.0, np.abs(want).max()), rtol=0)
+                               atol=gradient_atol(psums, dg), rtol=0)
