@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain GPU path")
     ap.add_argument("--no-e2e", action="store_true", help="skip the one-shot C-ABI leg")
+    ap.add_argument("--no-c4", action="store_true",
+                    help="skip the 30-qubit tensor-core sub-object of the default line")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="circuits per GPU (default 256; smaller only for profiling)")
     ap.add_argument("--c4-grid", default="5x6",
@@ -250,14 +252,12 @@ def config_roofline(wl, w, batch, ms, clk, units):
             nbytes = (fwd * 16 + meas * 8) * 2 ** n
             how = (f"{fwd} forward passes x 16 B + {meas} measurement "
                    f"pass(es) x 8 B, times 2^{n} amplitudes")
-        peak = peaks.get("hbm_gbs") or 6800.0
+        peak, src = _hbm_peak()
         achieved = nbytes * units / (ms / 1e3) / 1e9
         return {"bound": "hbm", "kernel": "wide passes + measurement (whole call)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None,
-                "algorithmic": how,
-                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"
-                               if peaks.get("hbm_gbs") else "fallback 6800 GB/s"}
+                "algorithmic": how, "peak_source": src}
     if wl in ("c1", "c5") and c:
         per = c["one"] * 16 + c["two"] * 32 + c["terms"] * 8
         if wl == "c5":
@@ -276,20 +276,31 @@ def config_roofline(wl, w, batch, ms, clk, units):
     return None
 
 
-def tc_kernel_roofline(n, batch, dev, launches=10):
-    """The tensor-core block kernel alone on a 2^n complex64 state: a random
-    5-qubit unitary on the targets of the row's first block, `launches`
-    launches timed with CUDA events on the launching stream.  Algorithmic
-    bytes per launch: 16 B per amplitude (read + write the state)."""
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def _hbm_peak():
+    peak = _peaks().get("hbm_gbs")
+    return (peak, "measured (MEASURED_PEAKS.json hbm_gbs)") if peak else \
+        (6800.0, "fallback 6800 GB/s (MEASURED_PEAKS.json absent)")
+
+
+def tc_kernel_roofline(n, batch, dev, launches=3):
+    """The tensor-core block kernel alone on a 2^n complex64 state (> L2), on
+    the target sets of every block of the row's plan: a random 5-qubit
+    unitary, one warm-up launch and `launches` timed launches per target set,
+    CUDA events on the launching stream.  Algorithmic bytes per launch: 16 B
+    per amplitude (read + write the state).  Reports the first block's
+    targets, the plan-weighted mean (every block's time summed), the median
+    and the slowest target set."""
     import torch
     from quantum_gb300 import _native
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
     plan = _native.tc_plan(batch._h, 0, np.zeros(0, np.float32))
-    tgt = plan[0][0] if plan else (0, 1, 2, 3, 4)
+    sets = [tuple(int(t) for t in p[0]) for p in plan] or [(0, 1, 2, 3, 4)]
     rng = np.random.default_rng(0)
     z = rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))
     q, _ = np.linalg.qr(z)
@@ -298,27 +309,74 @@ def tc_kernel_roofline(n, batch, dev, launches=10):
     psi[0] = 1
     st = torch.zeros(1, dtype=torch.int32, device=dev)
     s = torch.cuda.current_stream()
-    for _ in range(3):
+    per_set = {}
+    for tgt in dict.fromkeys(sets):
         _native.tc_apply(psi.data_ptr(), n, U.data_ptr(), tgt, st.data_ptr(), s.cuda_stream)
-    s.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(s)
-    for _ in range(launches):
-        _native.tc_apply(psi.data_ptr(), n, U.data_ptr(), tgt, st.data_ptr(), s.cuda_stream)
-    b.record(s)
-    s.synchronize()
-    ms = a.elapsed_time(b) / launches
-    peak = peaks.get("hbm_gbs") or 6800.0
-    achieved = 16 * 2 ** n / (ms / 1e3) / 1e9
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(launches):
+            _native.tc_apply(psi.data_ptr(), n, U.data_ptr(), tgt, st.data_ptr(),
+                             s.cuda_stream)
+        b.record(s)
+        s.synchronize()
+        per_set[tgt] = a.elapsed_time(b) / launches
+    peak, src = _hbm_peak()
+    gbs = lambda ms: 16 * 2 ** n / (ms / 1e3) / 1e9
+    times = [per_set[t] for t in sets]
+    order = sorted(per_set, key=per_set.get)
+    med, worst = order[len(order) // 2], order[-1]
     ok = int(st.item()) == 0
     del psi
-    return {"bound": "hbm", "kernel": "tc_apply5_kernel", "targets": list(tgt),
-            "grid": _native.tc_grid(),
-            "ms_per_launch": ms, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "status_ok": ok,
-            "algorithmic": f"16 B x 2^{n} amplitudes per launch (state > L2)",
-            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"
-                           if peaks.get("hbm_gbs") else "fallback 6800 GB/s"}
+    mean_ms = float(np.mean(times))
+    return {"bound": "hbm", "kernel": "tc_apply5_kernel", "grid": _native.tc_grid(),
+            "blocks": len(sets), "distinct_target_sets": len(per_set),
+            "targets_first": list(sets[0]), "ms_first": per_set[sets[0]],
+            "ms_per_launch": mean_ms, "achieved": gbs(mean_ms), "peak": peak,
+            "unit": "GB/s", "frac": gbs(mean_ms) / peak,
+            "first_frac": gbs(per_set[sets[0]]) / peak,
+            "median": {"targets": list(med), "ms": per_set[med], "frac": gbs(per_set[med]) / peak},
+            "worst": {"targets": list(worst), "ms": per_set[worst],
+                      "frac": gbs(per_set[worst]) / peak},
+            "status_ok": ok,
+            "algorithmic": f"16 B x 2^{n} amplitudes per launch (state > L2); achieved and "
+                           "frac: the mean over the plan's blocks",
+            "peak_source": src}
+
+
+def c4_summary(dev, steps=3, warmup=2, grid="5x6"):
+    """The 30-qubit grid circuit (C4) for the default line: device time of
+    one expectation call (tensor-core blocks, the library default at this
+    width) with its whole-call HBM roofline, plus the block kernel alone on
+    the plan's target sets.  Clocks are sampled during the timed calls."""
+    import torch
+    from quantum_gb300 import _native, ops, workloads
+    gr, gc = (int(x) for x in grid.split("x"))
+    w = workloads.grid_fsim(gr, gc, 24, seed=1)
+    b = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], ops.KIND_FORWARD)
+    vals = torch.tensor(w["symbol_values"], device=dev)
+    for _ in range(warmup):
+        b.expectation(vals)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for a, e in ev:
+        a.record()
+        out = b.expectation(vals)
+        e.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = float(np.mean([a.elapsed_time(e) for a, e in ev]))
+    line = {"workload": f"grid_fsim {grid} depth 24 ({w['n']} qubits, 8 GiB state at 30), "
+                        "expectation of sum Z",
+            "ms_per_call": ms, "circuits_per_s": 1e3 / ms, "clocks": clk,
+            "sum_z": float(out.cpu().numpy()[0, 0]),
+            "roofline": config_roofline("c4", w, b, ms, clk, 1)}
+    if _native.tc_blocks(b._h, 0) > 0:
+        line["tc_block_kernel"] = tc_kernel_roofline(w["n"], b, dev)
+    b.close()
+    return line
 
 
 def run_config(args):
@@ -679,6 +737,10 @@ def main():
         "clocks": clk, "accuracy": err, "plain_gpu": plain,
         "wall_s_timed": wall,
     }
+    if rank == 0 and world == 1 and not args.no_c4:
+        # the single-large-state configuration, timed on the same box in the
+        # same run: whole-call HBM roofline of the 30-qubit tensor-core path
+        line["c4"] = c4_summary(dev, grid=args.c4_grid)
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import cpu_port
         threads = cpu_port.num_threads()

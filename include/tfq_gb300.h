@@ -235,9 +235,9 @@ int tfqg_simulate_state(const char* const* programs, const int64_t* program_lens
  * Compute tfq_simulate_samples_op.cc:53-251, registered at :258-285).
  * samples: int8 [batch, num_samples, max_num_qubits]; bit k of a sample in
  * column max_num_qubits-k-1, -2 in the leading columns of smaller rows
- * (tfq_simulate_samples_op.cc:227-243).  num_samples < 1 is
- * INVALID_ARGUMENT (parse_context.cc:485-490).  max_num_qubits must be
- * tfqg_max_num_qubits() of the programs. */
+ * (tfq_simulate_samples_op.cc:227-243).  num_samples < 0 is
+ * INVALID_ARGUMENT; 0 writes nothing (tfq_simulate_samples_op.cc:113).
+ * max_num_qubits must be tfqg_max_num_qubits() of the programs. */
 int tfqg_simulate_samples(const char* const* programs, const int64_t* program_lens,
                           int64_t batch, const char* const* symbol_names,
                           const int64_t* symbol_name_lens, int64_t num_symbols,

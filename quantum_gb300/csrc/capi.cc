@@ -1568,14 +1568,22 @@ int tfqg_simulate_expectation(const char* const* programs,
 
 int tfqg_max_num_qubits(const char* const* programs, const int64_t* program_lens,
                         int64_t batch, int32_t* max_num_qubits) {
-  if (!max_num_qubits) return fail(kInvalidArgument, "max_num_qubits is NULL");
-  tfqg_batch* b = nullptr;
-  int rc = tfqg_batch_create(programs, program_lens, batch, nullptr, nullptr, 0, nullptr,
-                             nullptr, 0, TFQG_KIND_FORWARD, &b);
-  if (rc) return rc;
-  rc = tfqg_batch_max_num_qubits(b, max_num_qubits);
-  tfqg_batch_destroy(b);
-  return rc;
+  return guarded([&]() {
+    if (!max_num_qubits) throw Error(kInvalidArgument, "max_num_qubits is NULL");
+    if (batch < 0 || (batch > 0 && (!programs || !program_lens)))
+      throw Error(kInvalidArgument, "NULL programs");
+    // decode and resolve qubits only: symbols are bound later, as in
+    // GetProgramsAndNumQubits (parse_context.cc:268-320)
+    int mx = 0;
+    for (int64_t i = 0; i < batch; ++i) {
+      ProgramP p;
+      decode_program(programs[i], size_t(program_lens[i]), &p);
+      std::unordered_map<std::string, int> index;
+      mx = std::max(mx, resolve_qubits(p, &index));
+    }
+    *max_num_qubits = mx;
+    return 0;
+  });
 }
 
 namespace {
@@ -1794,6 +1802,22 @@ int tfqg_internal_tc_blocks(void* batch, int64_t k) {
   if (!b || !b->tc_planned || k < 0 || k >= int64_t(b->tc_rows.size())) return -1;
   return b->tc_ran[size_t(k)] ? b->tc_rows[size_t(k)].second : -1;
 }
+// Chunk geometry of the block kernel for targets tgt[0..4] (ascending) on an
+// n-qubit state: 1 and the transposed variant's tables, or 0 for the direct
+// variant (host only; lets tests check the kernel's index arithmetic).
+int tfqg_internal_tc_geometry(int n, const int32_t* tgt, uint64_t* cb, uint32_t* rpos,
+                              uint32_t* tpos, uint32_t* c) {
+  TcBlock blk{};
+  for (int i = 0; i < kTcBits; ++i) blk.tgt[i] = uint8_t(tgt[i]);
+  TcTrans tr{};
+  if (!tc_transposed_geometry(blk, n, &tr)) return 0;
+  *cb = tr.cb;
+  *rpos = tr.rpos;
+  *tpos = tr.tpos;
+  *c = tr.c;
+  return 1;
+}
+
 // Makes the next calls treat the tensor-core status word as `status`
 // (0 restores the real read-back); returns the previous setting.
 int tfqg_internal_tc_inject_status(int status) { return g_tc_status_injected.exchange(status); }

@@ -179,6 +179,19 @@ cudaError_t launch_tc_fuse(const BatchDevice& b, const float2* mats, int row,
                            float2* U, cudaStream_t s);
 cudaError_t launch_tc_apply5(float2* psi, int n, const float2* U, const TcBlock& blk,
                              int* status, int grid, cudaStream_t s);
+// Chunk geometry of the block kernel's transposed variant (blocks with a
+// target among bits 0-4): the 12 index bits of a chunk in ascending order
+// (cb, 5 bits each), the chunk positions of the 7 row bits and the 5
+// targets (rpos, tpos, 4 bits each) and the staging-buffer swizzle term of
+// chunk positions 4..11 (c, 4 bits each).  Returns false for blocks that
+// take the direct variant.
+struct TcTrans {
+  uint64_t cb;
+  uint32_t rpos;
+  uint32_t tpos;
+  uint32_t c;
+};
+bool tc_transposed_geometry(const TcBlock& blk, int n, TcTrans* out);
 // p[i] = (i == 0 ? first : rest) for i in [0, count).
 cudaError_t launch_fill(float2* p, int64_t count, float2 first, float2 rest, int grid,
                         cudaStream_t s);

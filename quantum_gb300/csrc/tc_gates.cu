@@ -24,6 +24,21 @@
 //
 // Every wait is bounded: on a timeout the kernel records status 1, waits
 // (bounded) once more for its MMAs, frees its TMEM and returns.
+//
+// Blocks with a target among index bits 0-4 take the transposed variant.
+// There a group's amplitudes lie within a few hundred bytes of each other
+// and neighbouring groups are 2^(lowest row bit) apart, so per-thread
+// gathers would touch every 32-byte sector several times.  Instead the CTA
+// moves each chunk of 4096 amplitudes as whole 16-byte vectors in index
+// order (every warp access a contiguous 512 bytes) through a staging buffer
+// in shared memory, and each thread reads or writes its group's amplitudes
+// there.  The chunk's 12 index bits always include bits 0-6 (they are either
+// targets or among the 7 lowest non-target bits), so a chunk is made of
+// 1 KiB runs.  The staging buffer is XOR-swizzled on its 8-byte slots: slot
+// bits 0-3 of chunk position L are XORed with a linear function h of L's
+// bits 4-11, chosen on the host so that the 32 groups of a warp fall on 16
+// distinct bank pairs (2 per pair, the minimum for 8-byte accesses) while
+// 16-byte accesses by consecutive lanes stay on distinct banks.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -128,9 +143,36 @@ __global__ void tc_fuse_kernel(BatchDevice b, const float2* mats, int row,
   for (int i = 0; i < 32; ++i) dst[i * 32 + j] = make_float2(float(col[i].re), float(col[i].im));
 }
 
+// physical offset of the chunk positions set in L
+__device__ __forceinline__ int64_t tr_dep(uint32_t L, uint64_t cb) {
+  int64_t o = 0;
+#pragma unroll
+  for (int p = 0; p < 12; ++p)
+    if ((L >> p) & 1u) o |= int64_t(1) << int((cb >> (5 * p)) & 31u);
+  return o;
+}
+
+// swizzle term of the positions >= 4 set in L
+__device__ __forceinline__ uint32_t tr_h(uint32_t L, uint32_t c) {
+  uint32_t h = 0;
+#pragma unroll
+  for (int p = 4; p < 12; ++p)
+    if ((L >> p) & 1u) h ^= (c >> (4 * (p - 4))) & 15u;
+  return h;
+}
+
+__device__ __forceinline__ uint32_t tr_deposit(uint32_t v, uint32_t pos, int bits) {
+  uint32_t L = 0;
+#pragma unroll
+  for (int i = 0; i < 7; ++i)
+    if (i < bits && ((v >> i) & 1u)) L |= 1u << ((pos >> (4 * i)) & 15u);
+  return L;
+}
+
+template <bool kTrans>
 __global__ void __launch_bounds__(kTcRows, 2)
 tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
-                 uint32_t tpack, int* status) {
+                 uint32_t tpack, TcTrans tr, int* status) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   float* a_hi = reinterpret_cast<float*>(tc_smem);
   float* a_lo = reinterpret_cast<float*>(tc_smem + kTcAbytes);
@@ -139,18 +181,39 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
   uint64_t* bar = reinterpret_cast<uint64_t*>(tc_smem + 2 * kTcAbytes + 2 * kTcBbytes);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
   int* timed_out = reinterpret_cast<int*>(bar + 2);
+  // staging buffers of the transposed variant: the A operands' space, free
+  // whenever no MMA is in flight (loads stage in a_hi, results in a_lo)
+  float2* stage_in = reinterpret_cast<float2*>(a_hi);
+  float2* stage_out = reinterpret_cast<float2*>(a_lo);
   const int tid = threadIdx.x, warp = tid >> 5;
 
   int t[kTcBits];
 #pragma unroll
   for (int i = 0; i < kTcBits; ++i) t[i] = int((tpack >> (5 * i)) & 31u);
+  // gather offsets of a group's amplitudes (direct variant) or their
+  // swizzled staging slots (transposed variant)
   uint32_t off[32];
 #pragma unroll
   for (int j = 0; j < 32; ++j) {
     uint32_t o = 0;
+    if (kTrans) {
+      const uint32_t Lj = tr_deposit(uint32_t(j), tr.tpos, kTcBits);
+      o = Lj ^ tr_h(Lj, tr.c);
+    } else {
 #pragma unroll
-    for (int i = 0; i < kTcBits; ++i) o |= uint32_t((j >> i) & 1) << t[i];
+      for (int i = 0; i < kTcBits; ++i) o |= uint32_t((j >> i) & 1) << t[i];
+    }
     off[j] = o;
+  }
+  // transposed variant: this thread's row slot base, and its part of the
+  // linear 16-byte accesses (chunk positions 2 * (tid + 128 i))
+  uint32_t swr = 0, h_t = 0;
+  int64_t dep_t = 0;
+  if (kTrans) {
+    const uint32_t Lr = tr_deposit(uint32_t(tid), tr.rpos, 7);
+    swr = Lr ^ tr_h(Lr, tr.c);
+    dep_t = tr_dep(uint32_t(2 * tid), tr.cb);
+    h_t = tr_h(uint32_t(2 * tid), tr.c);
   }
 
   // B operands: R in real form, split into tf32 hi and lo
@@ -183,14 +246,49 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
   const int64_t nchunk = int64_t(1) << (n - kTcBits - 7);
   int64_t chunk = blockIdx.x;
   float2 v[32];
-  if (chunk < nchunk) {
-    const float2* src = psi + group_base(chunk * kTcRows + tid, t);
+  float4 raw[16];
+  // chunk c starts at the index of its group 128 c (row and target bits 0)
+  auto chunk_base = [&](int64_t c) { return group_base(c * kTcRows, t); };
+  // linear 16-byte loads of a chunk into registers (transposed variant)
+  auto load_raw = [&](int64_t c) {
+    const float2* src = psi + chunk_base(c) + dep_t;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
+    for (int i = 0; i < 16; ++i)
+      raw[i] = __ldcs(reinterpret_cast<const float4*>(src + tr_dep(uint32_t(256 * i), tr.cb)));
+  };
+  // registers -> swizzled staging slots (transposed variant)
+  auto stage_raw = [&]() {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const uint32_t L = uint32_t(2 * tid + 256 * i);
+      const uint32_t h = h_t ^ tr_h(uint32_t(256 * i), tr.c);
+      const uint32_t sw = L ^ h;
+      float4 x = raw[i];
+      if (h & 1u) x = make_float4(x.z, x.w, x.x, x.y);
+      *reinterpret_cast<float4*>(stage_in + (sw & ~1u)) = x;
+    }
+  };
+  if (chunk < nchunk) {
+    if (kTrans) {
+      load_raw(chunk);
+    } else {
+      const float2* src = psi + group_base(chunk * kTcRows + tid, t);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
+    }
   }
   uint32_t parity = 0;
   bool failed = false;
   while (chunk < nchunk) {
+    if (kTrans) {
+      // staged chunk -> this thread's group (the staging space is the A
+      // operands' space, free here: no MMA is in flight)
+      stage_raw();
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] = stage_in[swr ^ off[j]];
+      __syncthreads();
+    }
     // A operands of this chunk: row tid, 16-byte pieces of two amplitudes
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
@@ -229,10 +327,14 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
           : "memory");
     }
     const int64_t next = chunk + gridDim.x;
-    if (next < nchunk) {  // the next chunk's gathers overlap the MMAs
-      const float2* src = psi + group_base(next * kTcRows + tid, t);
+    if (next < nchunk) {  // the next chunk's loads overlap the MMAs
+      if (kTrans) {
+        load_raw(next);
+      } else {
+        const float2* src = psi + group_base(next * kTcRows + tid, t);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
+        for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
+      }
     }
     bool done = false;
     for (uint32_t it = 0; it < kTcSpin && !done; ++it) done = mbar_try_wait(smem_u32(bar), parity);
@@ -246,7 +348,6 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
     }
     // D row tid (TMEM lane tid) back to the group's amplitudes
     {
-      float2* dst = psi + group_base(chunk * kTcRows + tid, t);
       const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16);
       uint32_t d[64];
       tmem_ld16(taddr, d);
@@ -254,9 +355,28 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
       tmem_ld16(taddr + 32u, d + 32);
       tmem_ld16(taddr + 48u, d + 48);
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (kTrans) {
+        // group -> swizzled staging slots, then linear 16-byte stores
 #pragma unroll
-      for (int i = 0; i < 32; ++i)
-        dst[off[i]] = make_float2(__uint_as_float(d[2 * i]), __uint_as_float(d[2 * i + 1]));
+        for (int i = 0; i < 32; ++i)
+          stage_out[swr ^ off[i]] =
+              make_float2(__uint_as_float(d[2 * i]), __uint_as_float(d[2 * i + 1]));
+        __syncthreads();
+        float2* dst = psi + chunk_base(chunk) + dep_t;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const uint32_t L = uint32_t(2 * tid + 256 * i);
+          const uint32_t h = h_t ^ tr_h(uint32_t(256 * i), tr.c);
+          float4 x = *reinterpret_cast<const float4*>(stage_out + ((L ^ h) & ~1u));
+          if (h & 1u) x = make_float4(x.z, x.w, x.x, x.y);
+          __stcs(reinterpret_cast<float4*>(dst + tr_dep(uint32_t(256 * i), tr.cb)), x);
+        }
+      } else {
+        float2* dst = psi + group_base(chunk * kTcRows + tid, t);
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+          dst[off[i]] = make_float2(__uint_as_float(d[2 * i]), __uint_as_float(d[2 * i + 1]));
+      }
     }
     // TMEM and the A operands are free for the next chunk
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -281,7 +401,9 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
 
 }  // namespace
 
-const void* tc_apply5_kernel_ptr() { return reinterpret_cast<const void*>(&tc_apply5_kernel); }
+const void* tc_apply5_kernel_ptr() {
+  return reinterpret_cast<const void*>(&tc_apply5_kernel<false>);
+}
 size_t tc_apply5_smem_bytes() { return kTcSmem; }
 
 cudaError_t launch_tc_fuse(const BatchDevice& b, const float2* mats, int row,
@@ -290,6 +412,59 @@ cudaError_t launch_tc_fuse(const BatchDevice& b, const float2* mats, int row,
   if (nblocks <= 0) return cudaSuccess;
   tc_fuse_kernel<<<nblocks, 32, 0, s>>>(b, mats, row, blocks, members, nblocks, U);
   return cudaGetLastError();
+}
+
+// Chunk geometry of the transposed variant for a block, or false when the
+// block's targets are all at bit 5 or above (the direct variant: the 32
+// groups of a warp are then 32 consecutive amplitudes).
+bool tc_transposed_geometry(const TcBlock& blk, int n, TcTrans* out) {
+  if (blk.tgt[0] >= 5) return false;
+  bool is_t[64] = {};
+  for (int i = 0; i < kTcBits; ++i) is_t[blk.tgt[i]] = true;
+  int rows[7], nr = 0;
+  for (int b = 0; b < n && nr < 7; ++b)
+    if (!is_t[b]) rows[nr++] = b;
+  int cb[12], np = 0;
+  int role[12];  // >= 0: target index; < 0: -1 - row index
+  {
+    int ti = 0, ri = 0;
+    while (ti < kTcBits || ri < 7) {
+      const bool take_t = ri == 7 || (ti < kTcBits && blk.tgt[ti] < rows[ri]);
+      if (take_t) {
+        cb[np] = blk.tgt[ti];
+        role[np++] = ti++;
+      } else {
+        cb[np] = rows[ri];
+        role[np++] = -1 - ri++;
+      }
+    }
+  }
+  TcTrans tr{};
+  for (int p = 0; p < 12; ++p) {
+    tr.cb |= uint64_t(cb[p]) << (5 * p);
+    if (role[p] >= 0) tr.tpos |= uint32_t(p) << (4 * role[p]);
+    else tr.rpos |= uint32_t(p) << (4 * (-1 - role[p]));
+  }
+  // swizzle: the 5 lowest row bits (a warp's lanes) must reach every slot
+  // bit 0-3; positions below 4 contribute their own bit, positions above
+  // take the slot bits still missing
+  uint32_t covered = 0;
+  for (int i = 0; i < 5; ++i) {
+    const int p = int((tr.rpos >> (4 * i)) & 15u);
+    if (p < 4) covered |= 1u << p;
+  }
+  for (int i = 0; i < 5; ++i) {
+    const int p = int((tr.rpos >> (4 * i)) & 15u);
+    if (p < 4) continue;
+    for (int q = 0; q < 4; ++q)
+      if (!(covered & (1u << q))) {
+        covered |= 1u << q;
+        tr.c |= (1u << q) << (4 * (p - 4));
+        break;
+      }
+  }
+  *out = tr;
+  return true;
 }
 
 cudaError_t launch_tc_apply5(float2* psi, int n, const float2* U, const TcBlock& blk,
@@ -302,7 +477,17 @@ cudaError_t launch_tc_apply5(float2* psi, int n, const float2* U, const TcBlock&
   }
   const int64_t nchunk = int64_t(1) << (n - kTcBits - 7);
   if (grid > nchunk) grid = int(nchunk);
-  tc_apply5_kernel<<<grid, kTcRows, kTcSmem, s>>>(psi, n, U, tpack, status);
+  TcTrans tr{};
+  const bool trans = tc_transposed_geometry(blk, n, &tr);
+  const void* k = trans ? reinterpret_cast<const void*>(&tc_apply5_kernel<true>)
+                        : reinterpret_cast<const void*>(&tc_apply5_kernel<false>);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(kTcSmem));
+  if (e != cudaSuccess) return e;
+  if (trans)
+    tc_apply5_kernel<true><<<grid, kTcRows, kTcSmem, s>>>(psi, n, U, tpack, tr, status);
+  else
+    tc_apply5_kernel<false><<<grid, kTcRows, kTcSmem, s>>>(psi, n, U, tpack, tr, status);
   return cudaGetLastError();
 }
 

@@ -183,3 +183,22 @@ def test_wide_row_rule_follows_the_batch():
         b = ops.Batch(progs, [], None)
         assert _native.batch_wide_rows(b._h) == want, (len(progs), want)
         b.close()
+
+
+def test_max_num_qubits_of_symbolic_programs_without_a_gpu():
+    """tfqg_max_num_qubits decodes and resolves qubits only (symbols are bound
+    later, as GetProgramsAndNumQubits does), so it needs no symbol values and
+    no GPU."""
+    import ctypes
+    from quantum_gb300 import _native
+    from quantum_gb300 import serialize as S
+    progs = [S.serialize_circuit(S.Circuit([[S.rx(q, S.Symbol("a"))
+                                             for q in S.GridQubit.rect(1, n)]]))
+             for n in (3, 9, 5)]
+    pp, pl, keep = _native.string_array(progs)
+    f = _native.lib().tfqg_max_num_qubits
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+    mq = ctypes.c_int32()
+    assert f(pp, pl, 3, ctypes.byref(mq)) == 0 and mq.value == 9
+    bad, bl, keep2 = _native.string_array([b"\x0a\x05garbage"])
+    assert f(bad, bl, 1, ctypes.byref(mq)) == 3

@@ -16,17 +16,19 @@ expectation op on shifted symbol values (one batch row per shift):
   f(t) = a + b cos(pi t) + c sin(pi t) and
   df/dx = s * (pi/2) * (f(t + 1/2) - f(t - 1/2)), a shift of x by 0.5/s.
 
-Tolerances, stated against max|grad| (about 5 here):
-- parameter shift against the exact-derivative adjoint (grad_rule=1): 2e-5
-  relative. Both are exact rules, and only float32 rounding of the state,
-  of x +- 0.5/s and of x*s separates them;
+Tolerances, relative to max(1, max|grad|) (the gradients here are a few
+tenths):
+- parameter shift against the exact-derivative adjoint (grad_rule=1): 2e-6.
+  Both are exact rules, and only float32 rounding of the state, of
+  x +- 0.5/s and of x*s separates them (measured on GB300: 2.8e-7);
 - parameter shift against the reference's finite-difference gradient gates
-  (grad_rule=0, eps = 5e-3 inside the gate): 1e-4 relative. The gate rule
-  scales every derivative by sin(pi eps s)/(pi eps s), 1 - 4e-6 for these
-  gates;
-- central differences against both adjoint rules: 2e-3 relative. With
-  eps = 1e-3 in float32, the 1e-7 relative rounding of the 31-term
-  expectation and of x +- eps (spacing 2.4e-7 near 2pi) is divided by 2e-3.
+  (grad_rule=0, eps = 5e-3 inside the gate): 5e-5.  The gate rule's
+  (G(x+eps) - G(x-eps)) / 2eps in float32 loses about 6e-6 relative to
+  cancellation, besides its sin(pi eps s)/(pi eps s) truncation (measured:
+  9.3e-6);
+- central differences against both adjoint rules: 3e-4.  With eps = 1e-3
+  in float32, the 1e-7 relative rounding of the 31-term expectation and of
+  x +- eps (spacing 2.4e-7 near 2pi) is divided by 2e-3 (measured: 5.8e-5).
 """
 
 import numpy as np
@@ -76,9 +78,12 @@ def test_adjoint_matches_central_differences(hea, row):
     fp, fm, step, _, _ = _shifted_expectations(hea, row, 1e-3)
     fd = (fp - fm) / step
     scale = max(1.0, float(np.abs(hea["g_ex"][row]).max()))
-    assert np.abs(fd).max() > 0.5
-    np.testing.assert_allclose(hea["g_ex"][row], fd, atol=2e-3 * scale, rtol=0)
-    np.testing.assert_allclose(hea["g_fd"][row], fd, atol=2e-3 * scale, rtol=0)
+    assert np.abs(fd).max() > 0.05  # a nonzero gradient is being compared
+    print(f"row {row}: central differences vs adjoint: exact rule "
+          f"{np.abs(hea['g_ex'][row] - fd).max():.2e}, reference rule "
+          f"{np.abs(hea['g_fd'][row] - fd).max():.2e}")
+    np.testing.assert_allclose(hea["g_ex"][row], fd, atol=3e-4 * scale, rtol=0)
+    np.testing.assert_allclose(hea["g_fd"][row], fd, atol=3e-4 * scale, rtol=0)
 
 
 @pytest.mark.parametrize("row", [0, 1])
@@ -93,6 +98,9 @@ def test_adjoint_matches_parameter_shift(hea, row):
     assert np.abs(tp - 0.5).max() < 1e-6 and np.abs(tm - 0.5).max() < 1e-6
     ps = float(SCALAR) * (np.pi / 2) * (fp - fm)
     scale = max(1.0, float(np.abs(ps).max()))
-    assert np.abs(ps).max() > 0.5
-    np.testing.assert_allclose(hea["g_ex"][row], ps, atol=2e-5 * scale, rtol=0)
-    np.testing.assert_allclose(hea["g_fd"][row], ps, atol=1e-4 * scale, rtol=0)
+    assert np.abs(ps).max() > 0.05
+    print(f"row {row}: parameter shift vs adjoint: exact rule "
+          f"{np.abs(hea['g_ex'][row] - ps).max():.2e}, reference rule "
+          f"{np.abs(hea['g_fd'][row] - ps).max():.2e}")
+    np.testing.assert_allclose(hea["g_ex"][row], ps, atol=2e-6 * scale, rtol=0)
+    np.testing.assert_allclose(hea["g_fd"][row], ps, atol=5e-5 * scale, rtol=0)

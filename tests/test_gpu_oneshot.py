@@ -82,7 +82,9 @@ def test_samples_layout_and_distribution():
         counts = np.bincount(bits_to_index(out[r], n), minlength=2 ** n)
         p, _, _ = chi2_pvalue(counts, probs, shots)
         assert p > 1e-3
-    assert lib.tfqg_simulate_samples(pp, pl, 2, npp, npl, 3, _p(v), 0, 99, 6, _p(out)) == 3
+    assert lib.tfqg_simulate_samples(pp, pl, 2, npp, npl, 3, _p(v), -1, 99, 6, _p(out)) == 3
+    # zero samples: an empty output, as the reference op returns
+    assert lib.tfqg_simulate_samples(pp, pl, 2, npp, npl, 3, _p(v), 0, 99, 6, _p(out)) == 0
 
 
 def test_expectation_and_adjoint_gradient():

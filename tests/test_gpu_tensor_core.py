@@ -1,7 +1,8 @@
 """Tensor-core forward path of wide rows (tc_gates.cu) on the GPU.
 
 The block kernel alone: a random 5-qubit unitary applied to a random state
-on several target sets (the lowest bits, scattered bits, the highest bits),
+on several target sets (the lowest bits, scattered bits, the highest bits;
+sets with a target among bits 0-4 take the kernel's transposed variant),
 against numpy in complex128.  Split 3xTF32 must keep fp32-level accuracy:
 1e-6 absolute on states of unit norm, where a plain-TF32 product is off by
 about 4e-5 at 12 qubits (test_tc_plan_cpu.py restates both with numpy).
@@ -42,6 +43,9 @@ def _apply_np(psi, n, tgt, U):
     (14, (3, 7, 8, 12, 13), 0),
     (14, (9, 10, 11, 12, 13), 1),
     (13, (0, 5, 6, 11, 12), 2),
+    (13, (2, 3, 4, 5, 6), 0),
+    (14, (4, 10, 11, 12, 13), 0),
+    (12, (1, 2, 7, 8, 11), 3),
 ])
 def test_block_kernel_matches_complex128(n, tgt, grid):
     torch = pytest.importorskip("torch")
