@@ -354,6 +354,36 @@ def row_sweeps(handle, row):
     return a.value, m.value
 
 
+def set_lock_min_qubits(n):
+    """Qubit count from which streamed rows (not wide) of batches created
+    from now on run in lockstep over the whole grid in the forward modes;
+    above 21 turns lockstep off.  Returns the previous value."""
+    f = lib().tfqg_internal_set_lock_min_qubits
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return int(f(int(n)))
+
+
+def set_lock_arena_amps(amps):
+    """Largest lockstep group (amplitudes of its rows' states together) for
+    batches created from now on; returns the previous value."""
+    f = lib().tfqg_internal_set_lock_arena_amps
+    f.argtypes = [ctypes.c_int64]
+    f.restype = ctypes.c_int64
+    return int(f(int(amps)))
+
+
+def batch_lock_rows(handle):
+    """(lockstep rows, lockstep groups) of a batch."""
+    f = lib().tfqg_internal_batch_lock_rows
+    f.argtypes = [c_void_p]
+    f.restype = ctypes.c_int
+    g = lib().tfqg_internal_batch_lock_groups
+    g.argtypes = [c_void_p]
+    g.restype = ctypes.c_int
+    return int(f(handle)), int(g(handle))
+
+
 def set_wide_few_rows(rows):
     """Batches that stream fewer than `rows` rows run their rows of 17+
     qubits as wide rows (0: never); for batches created from now on.

@@ -57,7 +57,8 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Offsets of the device tables inside one packed blob.
 struct TableOffsets {
-  size_t prog, rows, gates, pass, ops, terms, chan, kraus, gc, order, order_fwd, meas, mterms;
+  size_t prog, rows, gates, pass, ops, terms, chan, kraus, gc, order, order_fwd, meas, mterms,
+      order_lock, lock_items;
 };
 
 int set_last_error(int code, const std::string& msg);
@@ -81,6 +82,24 @@ struct tfqg_batch {
   int max_wide_n = 0;
   bool any_streamed_fwd = false;
   int max_streamed_n_fwd = 0;
+  // forward modes run lockstep rows (lock_min..21 qubits, not wide, in a
+  // batch with many of them) group by group over the whole grid, one launch
+  // per pass (kernels.h LockItem); the queue then takes order_lock
+  struct LockLaunch {
+    int32_t begin = 0, count = 0;  // items
+    int64_t ntiles = 0;            // tiles (or chunks) the launch covers
+  };
+  struct LockGroup {
+    int64_t arena_amps = 0;        // states of the group's rows
+    LockLaunch rows;               // one item per row (chunk prefix, offset)
+    std::vector<LockLaunch> fwd, meas;
+  };
+  std::vector<int32_t> lock_rows;
+  std::vector<int32_t> order_lock;
+  std::vector<tfqg::LockItem> lock_items;
+  std::vector<LockGroup> lock_groups;
+  bool any_streamed_lock = false;
+  int max_streamed_n_lock = 0;
   int max_grads = 0;
   int64_t total_gates = 0, total_grads = 0;
   bool any_fused = false;  // forward plans hold GK_FUSED gates
@@ -112,6 +131,7 @@ struct tfqg_batch {
   int device = -1;
   tfqg::DevBuf tables, mats, dmats, work, counter, values, out, aux, aux2;
   tfqg::DevBuf wide_state, wide_acc;
+  tfqg::DevBuf lock_state, lock_acc;
   // tensor-core forward path of wide rows (tc_gates.cu): per wide row its
   // first block and block count (count -1: the row has no 5-bit plan)
   bool tc_planned = false;
@@ -124,11 +144,14 @@ struct tfqg_batch {
   void release_buffers() noexcept {
     tfqg::DevBuf* all[] = {&tables,     &mats,     &dmats,     &work,   &counter,
                            &values,     &out,      &aux,       &aux2,   &wide_state,
-                           &wide_acc,   &inner_tmp, &tc_tab,   &tc_mats, &tc_status};
+                           &wide_acc,   &inner_tmp, &tc_tab,   &tc_mats, &tc_status,
+                           &lock_state, &lock_acc};
     for (tfqg::DevBuf* d : all) d->release(true);
   }
   tfqg::BatchDevice bd;
   const int32_t* d_order_fwd = nullptr;
+  const int32_t* d_order_lock = nullptr;
+  const tfqg::LockItem* d_lock_items = nullptr;
 };
 
 namespace tfqg {

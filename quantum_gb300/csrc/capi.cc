@@ -132,6 +132,14 @@ namespace {
 
 std::atomic<int> g_wide_min_qubits{kWideMinQubits};
 std::atomic<int> g_wide_few_rows{kWideFewRows};
+// Streamed rows of at least this many qubits that do not run wide run in
+// lockstep over the whole grid in the forward modes (kernels.h LockItem);
+// a value above 21 turns lockstep rows off.
+constexpr int kLockMinQubits = 17;
+std::atomic<int> g_lock_min_qubits{kLockMinQubits};
+// States of one lockstep group (amplitudes): 2^30 = 8 GiB of complex64.
+constexpr int64_t kLockArenaAmps = int64_t(1) << 30;
+std::atomic<int64_t> g_lock_arena_amps{kLockArenaAmps};
 
 int wide_min_qubits() { return g_wide_min_qubits.load(); }
 
@@ -288,6 +296,71 @@ void program_cache_clear() {
 // TFQG_KIND_INNER: `others` holds batch x num_others paired programs
 // (tfq_inner_product's other_programs); they become rows batch + i *
 // num_others + j, resolved with the qubit map of their reference row i.
+// Lockstep schedule of the batch's lock rows: groups of rows whose states
+// fit g_lock_arena_amps together; per group one item per row (its chunk
+// prefix and arena offset), then per launch k the items of forward pass k of
+// every row that has one, then per launch m those of measurement pass m.
+void build_lock_schedule(tfqg_batch* b) {
+  const size_t nr = b->lock_rows.size();
+  size_t i = 0;
+  auto prog = [&](int32_t row) -> const DevProgram& {
+    return b->programs[b->rows[size_t(row)].program];
+  };
+  while (i < nr) {
+    tfqg_batch::LockGroup g;
+    size_t j = i;
+    while (j < nr) {
+      const int64_t a = int64_t(1) << prog(b->lock_rows[j]).n;
+      // (a group's rows are one grid dimension of its padding launch)
+      if (j > i && (g.arena_amps + a > g_lock_arena_amps.load() || j - i >= 65535)) break;
+      g.arena_amps += a;
+      ++j;
+    }
+    std::vector<int64_t> off(j - i);
+    g.rows.begin = int32_t(b->lock_items.size());
+    int64_t o = 0, chunks = 0;
+    for (size_t k = i; k < j; ++k) {
+      const int32_t row = b->lock_rows[k];
+      const int n = prog(row).n;
+      off[k - i] = o;
+      b->lock_items.push_back(LockItem{row, 0u, chunks, o, n, 0});
+      o += int64_t(1) << n;
+      chunks += int64_t(1) << (n - kStreamTileBits);
+    }
+    g.rows.count = int32_t(j - i);
+    g.rows.ntiles = chunks;
+    uint32_t max_fwd = 0, max_meas = 0;
+    for (size_t k = i; k < j; ++k) {
+      const DevProgram& p = prog(b->lock_rows[k]);
+      const DevRow& r = b->rows[size_t(b->lock_rows[k])];
+      max_fwd = std::max(max_fwd, p.fwd_pass_end - p.fwd_pass_begin);
+      max_meas = std::max(max_meas, r.meas_end - r.meas_begin);
+    }
+    for (int meas = 0; meas < 2; ++meas) {
+      const uint32_t launches = meas ? max_meas : max_fwd;
+      for (uint32_t q = 0; q < launches; ++q) {
+        tfqg_batch::LockLaunch L;
+        L.begin = int32_t(b->lock_items.size());
+        for (size_t k = i; k < j; ++k) {
+          const int32_t row = b->lock_rows[k];
+          const DevProgram& p = prog(row);
+          const DevRow& r = b->rows[size_t(row)];
+          const uint32_t first = meas ? r.meas_begin : p.fwd_pass_begin;
+          const uint32_t count = meas ? r.meas_end - r.meas_begin
+                                      : p.fwd_pass_end - p.fwd_pass_begin;
+          if (q >= count) continue;
+          b->lock_items.push_back(LockItem{row, first + q, L.ntiles, off[k - i], p.n, 0});
+          L.ntiles += int64_t(1) << (p.n - kStreamTileBits);
+        }
+        L.count = int32_t(b->lock_items.size()) - L.begin;
+        (meas ? g.meas : g.fwd).push_back(L);
+      }
+    }
+    b->lock_groups.push_back(std::move(g));
+    i = j;
+  }
+}
+
 void build_batch(tfqg_batch* b, const char* const* programs,
                  const int64_t* program_lens, int64_t batch,
                  const char* const* symbol_names, const int64_t* name_lens,
@@ -611,6 +684,29 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     b->wide_rows.push_back(int32_t(i));
     b->max_wide_n = std::max(b->max_wide_n, int(p.n));
   }
+  // lockstep rows: streamed rows of lock_min..21 qubits that are not wide.
+  // In the queue each would stream through one CTA's slot (one SM for the
+  // whole circuit); in lockstep every launch keeps the tiles of all of them
+  // in flight over the whole grid.
+  const int lock_min = std::max(g_lock_min_qubits.load(), kStreamTileBits + 1);
+  auto is_lock = [&](const DevProgram& p) {
+    return !inner && !is_wide(p) && !p.resident && p.num_channels == 0 &&
+           p.fwd_pass_begin != p.fwd_pass_end && p.n >= lock_min;
+  };
+  for (const int32_t i : b->order) {
+    const DevProgram& p = b->programs[b->rows[i].program];
+    if (is_wide(p)) continue;
+    if (is_lock(p)) {
+      b->lock_rows.push_back(i);
+      continue;
+    }
+    b->order_lock.push_back(i);
+    if (p.n > 0 && !p.resident) {
+      b->any_streamed_lock = true;
+      b->max_streamed_n_lock = std::max(b->max_streamed_n_lock, int(p.n));
+    }
+  }
+  build_lock_schedule(b);
   jit_assign_signatures(b);
   if (b->max_grads > 6144)
     throw Error(kResourceExhausted,
@@ -640,6 +736,10 @@ void ensure_device(tfqg_batch* b, cudaStream_t s) {
   b->bd = table_view(b, static_cast<unsigned char*>(b->tables.p), o);
   b->d_order_fwd = reinterpret_cast<const int32_t*>(
       static_cast<unsigned char*>(b->tables.p) + o.order_fwd);
+  b->d_order_lock = reinterpret_cast<const int32_t*>(
+      static_cast<unsigned char*>(b->tables.p) + o.order_lock);
+  b->d_lock_items = reinterpret_cast<const LockItem*>(
+      static_cast<unsigned char*>(b->tables.p) + o.lock_items);
   b->device = dev;
 }
 
@@ -658,6 +758,8 @@ TableOffsets tfqg::pack_tables(const tfqg_batch* b, std::vector<unsigned char>* 
   o.gc = put(blob, b->grad_cols);
   o.order = put(blob, b->order);
   o.order_fwd = put(blob, b->order_fwd);
+  o.order_lock = put(blob, b->order_lock);
+  o.lock_items = put(blob, b->lock_items);
   o.meas = put(blob, b->meas);
   o.mterms = put(blob, b->meas_terms);
   blob->resize(align256(blob->size()));
@@ -951,22 +1053,82 @@ void run_wide_adjoint(tfqg_batch* b, const BatchDevice& bd, RunArgs* a, cudaStre
   }
 }
 
+// Forward-mode work of the lockstep rows, group after group on stream s:
+// one launch per forward pass index over every row of the group, then the
+// group's measurement, state padding or sampling.
+void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaStream_t s) {
+  const int dev = b->device;
+  const int state_amps = 1 << kStreamTileBits;
+  const size_t smem = sim_smem_bytes(kModeState, -1, true, 0);
+  const int grid = occupancy_grid(sim_kernel_lock(), kWideThreads, smem, dev);
+  const int mgrid = occupancy_grid(lock_measure_kernel_ptr(), kWideThreads, smem, dev);
+  int sms = 0;
+  TFQG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  int64_t arena = 0, chunks = 0;
+  int32_t rows = 0;
+  for (const auto& g : b->lock_groups) {
+    arena = std::max(arena, g.arena_amps);
+    chunks = std::max(chunks, g.rows.ntiles);
+    rows = std::max(rows, g.rows.count);
+  }
+  float2* state = nullptr;
+  if (mode != kModeState) {
+    b->lock_state.reserve(size_t(arena) * sizeof(float2), dev);
+    state = static_cast<float2*>(b->lock_state.p);
+  }
+  double* acc = nullptr;
+  const size_t nwacc = 2 * b->meas_terms.size();
+  if (mode == kModeExpect) {
+    b->lock_acc.reserve((nwacc + size_t(rows) * size_t(std::max<int64_t>(b->n_ops, 1))) *
+                            sizeof(double),
+                        dev);
+    acc = static_cast<double*>(b->lock_acc.p);
+  } else if (mode == kModeSample) {
+    b->lock_acc.reserve(size_t(chunks) * sizeof(double), dev);
+    acc = static_cast<double*>(b->lock_acc.p);
+  }
+  const LockItem* items = b->d_lock_items;
+  for (const auto& g : b->lock_groups) {
+    for (size_t k = 0; k < g.fwd.size(); ++k)
+      TFQG_CUDA(sim_launch_lock(bd, *a, items + g.fwd[k].begin, g.fwd[k].count,
+                                g.fwd[k].ntiles, state, k == 0 ? 1 : 0,
+                                mode == kModeState ? 1 : 0, grid, smem, state_amps, s));
+    const LockItem* rws = items + g.rows.begin;
+    if (mode == kModeExpect) {
+      if (nwacc) TFQG_CUDA(cudaMemsetAsync(acc, 0, nwacc * sizeof(double), s));
+      for (const auto& L : g.meas)
+        TFQG_CUDA(launch_lock_measure(bd, *a, items + L.begin, L.count, L.ntiles, state, acc,
+                                      mgrid, smem, state_amps, s));
+      TFQG_CUDA(launch_lock_expect_finalize(bd, *a, rws, g.rows.count, acc, acc + nwacc, s));
+    } else if (mode == kModeState) {
+      TFQG_CUDA(launch_lock_pad(bd, *a, rws, g.rows.count, s));
+    } else {
+      TFQG_CUDA(launch_lock_chunk_sums(rws, g.rows.count, g.rows.ntiles, state, acc, sms * 4,
+                                       s));
+      TFQG_CUDA(launch_lock_sample(bd, *a, rws, g.rows.count, state, acc, s));
+    }
+  }
+}
+
 int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
   // forward modes: wide rows run on the whole grid, the rest in the queue;
   // so does the adjoint of tfq_adj_grad (not the inner-product gradient,
   // whose lambda comes from a buffer)
   const bool fwd = mode == kModeExpect || mode == kModeState || mode == kModeSample;
   const bool wide_adj = mode == kModeAdjoint && b->kind != TFQG_KIND_INNER && !a->lambda_init;
-  const bool split = (fwd || wide_adj) && !b->wide_rows.empty();
+  const bool lock = fwd && !b->lock_rows.empty();
+  const bool split = (fwd || wide_adj) && (!b->wide_rows.empty() || lock);
   BatchDevice bd = b->bd;
   if (split) {
-    bd.order = b->d_order_fwd;
-    bd.num_queue = int32_t(b->order_fwd.size());
+    bd.order = lock ? b->d_order_lock : b->d_order_fwd;
+    bd.num_queue = int32_t(lock ? b->order_lock.size() : b->order_fwd.size());
   }
   // an inner-product gradient sweeps only the reference rows (first in order)
   if (b->kind == TFQG_KIND_INNER && mode == kModeAdjoint) bd.num_queue = int32_t(b->inner_rows);
-  const bool any_streamed = split ? b->any_streamed_fwd : b->any_streamed;
-  const int max_streamed_n = split ? b->max_streamed_n_fwd : b->max_streamed_n;
+  const bool any_streamed =
+      lock ? b->any_streamed_lock : split ? b->any_streamed_fwd : b->any_streamed;
+  const int max_streamed_n =
+      lock ? b->max_streamed_n_lock : split ? b->max_streamed_n_fwd : b->max_streamed_n;
   int grid = 0;
   if (mode == kModeNoisy || bd.num_queue > 0) {
     const int max_grads = mode == kModeAdjoint ? b->max_grads : 0;
@@ -1001,8 +1163,12 @@ int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
     }
     if (!launched) TFQG_CUDA(launch_simulate(mode, bd, *a, grid, smem, state_amps, s));
   }
-  if (split && wide_adj) run_wide_adjoint(b, bd, a, s);
-  else if (split) run_wide(b, mode, bd, a, s);
+  if (split && wide_adj) {
+    run_wide_adjoint(b, bd, a, s);
+  } else if (split) {
+    if (!b->wide_rows.empty()) run_wide(b, mode, bd, a, s);
+    if (lock) run_lock(b, mode, bd, a, s);
+  }
   return grid;
 }
 
@@ -1879,6 +2045,28 @@ int tfqg_internal_tc_plan(void* batch, int64_t row, const float* row_values, int
 // Streamed-row count below which rows of 17+ qubits run as wide rows, for
 // batches created after the call (0: never); returns the previous value.
 int tfqg_internal_set_wide_few_rows(int rows) { return g_wide_few_rows.exchange(rows); }
+
+// Qubit count from which streamed rows of batches created from now on run in
+// lockstep in the forward modes (above 21: never); returns the previous value.
+int tfqg_internal_set_lock_min_qubits(int n) { return g_lock_min_qubits.exchange(n); }
+
+// Largest lockstep group (amplitudes of its rows' states) for batches created
+// from now on; returns the previous value.
+int64_t tfqg_internal_set_lock_arena_amps(int64_t amps) {
+  return g_lock_arena_amps.exchange(amps);
+}
+
+// Lockstep groups of a batch.
+int tfqg_internal_batch_lock_groups(void* batch) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  return b ? int(b->lock_groups.size()) : -1;
+}
+
+// Lockstep rows of a batch (forward modes).
+int tfqg_internal_batch_lock_rows(void* batch) {
+  tfqg_batch* b = static_cast<tfqg_batch*>(batch);
+  return b ? int(b->lock_rows.size()) : -1;
+}
 
 // Number of wide rows of a batch (forward modes).
 int tfqg_internal_batch_wide_rows(void* batch) {

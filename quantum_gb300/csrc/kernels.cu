@@ -269,9 +269,8 @@ wide_measure_kernel(BatchDevice b, RunArgs a, int row, int mp, const float2* psi
 // Combines the term sums of a wide row into out_f[row, :] in double, with the
 // measure_passes rules: Re(i^ny * sum) times the coefficient, identity terms
 // contribute their coefficient (util_qsim.h:152-186).
-__global__ void wide_expect_finalize_kernel(BatchDevice b, RunArgs a, int row,
-                                            const double* wacc, int term0,
-                                            double* acc) {
+__device__ void expect_finalize_body(const BatchDevice& b, const RunArgs& a, int row,
+                                     const double* wacc, int term0, double* acc) {
   const DevRow r = b.rows[row];
   for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x) acc[j] = 0.0;
   __syncthreads();
@@ -303,39 +302,48 @@ __global__ void wide_expect_finalize_kernel(BatchDevice b, RunArgs a, int row,
     a.out_f[int64_t(row) * b.num_ops + j] = float(acc[j]);
 }
 
+__global__ void wide_expect_finalize_kernel(BatchDevice b, RunArgs a, int row,
+                                            const double* wacc, int term0,
+                                            double* acc) {
+  expect_finalize_body(b, a, row, wacc, term0, acc);
+}
+
+// *out = sum of |psi|^2 over the 2^13 amplitudes at `chunk` (256 threads;
+// `part` is shared scratch of 8 doubles).
+__device__ void chunk_sum_body(const float2* chunk, double* out, double* part) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const float4* p = reinterpret_cast<const float4*>(chunk);
+  float f = 0.f;
+  for (uint32_t k = threadIdx.x; k < (1u << (kTile - 1)); k += blockDim.x) {
+    const float4 v = __ldcg(p + k);
+    f = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, f))));
+  }
+  double d = f;
+  for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  if (lane == 0) part[w] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) t += part[i];
+    *out = t;
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(256)
 wide_chunk_sums_kernel(const float2* psi, int n, double* csum) {
   __shared__ double part[8];
   const uint32_t nch = 1u << (n - kTile);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
-    const float4* p = reinterpret_cast<const float4*>(psi + (size_t(c) << kTile));
-    float f = 0.f;
-    for (uint32_t k = threadIdx.x; k < (1u << (kTile - 1)); k += blockDim.x) {
-      const float4 v = __ldcg(p + k);
-      f = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, f))));
-    }
-    double d = f;
-    for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if (lane == 0) part[w] = d;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int i = 0; i < int(blockDim.x >> 5); ++i) t += part[i];
-      csum[c] = t;
-    }
-    __syncthreads();
-  }
+  for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x)
+    chunk_sum_body(psi + (size_t(c) << kTile), csum + c, part);
 }
 
 // One CTA: inclusive scan of the chunk sums, then one thread per sample finds
 // its chunk by binary search and its index by a scan inside the chunk
 // (StateSpace::Sample semantics: index x with probability |psi_x|^2; bit k
 // of x goes to column max_n - k - 1, tfq_simulate_samples_op.cc:226-243).
-__global__ void __launch_bounds__(512)
-wide_sample_kernel(BatchDevice b, RunArgs a, int row, const float2* psi, int n,
-                   double* csum) {
-  __shared__ double seg[512];
+__device__ void sample_row_body(const BatchDevice& b, const RunArgs& a, int row,
+                                const float2* psi, int n, double* csum, double* seg) {
   const uint32_t nch = 1u << (n - kTile);
   const uint32_t per = (nch + blockDim.x - 1) / blockDim.x;
   const uint32_t lo = min(threadIdx.x * per, nch), hi = min(lo + per, nch);
@@ -386,6 +394,100 @@ wide_sample_kernel(BatchDevice b, RunArgs a, int row, const float2* psi, int n,
       o[c] = k >= n ? int8_t(-2) : int8_t((x >> k) & 1);
     }
   }
+}
+
+__global__ void __launch_bounds__(512)
+wide_sample_kernel(BatchDevice b, RunArgs a, int row, const float2* psi, int n,
+                   double* csum) {
+  __shared__ double seg[512];
+  sample_row_body(b, a, row, psi, n, csum, seg);
+}
+
+// ---- lockstep rows ------------------------------------------------------------
+// Rows of one lockstep group run side by side, each over its own state
+// (arena + off); every launch covers the tiles or chunks of all the group's
+// rows, `items` giving each row's first global tile or chunk (prefix) in
+// ascending order.
+
+__device__ __forceinline__ int lock_find(const LockItem* items, int nitems, int64_t T) {
+  int lo = 0, hi = nitems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (items[mid].prefix <= T) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Measurement pass items[i].pass of every row: each tile's term sums go to
+// wacc[2 * term + {0, 1}] (term: the batch-wide measurement-term index).
+__global__ void __launch_bounds__(kWideThreads, 2)
+lock_measure_kernel(BatchDevice b, RunArgs a, const LockItem* items, int nitems,
+                    int64_t ntiles, const float2* arena, double* wacc, int state_amps) {
+  const Smem sm = carve_smem<kModeState>(state_amps, 1);
+  for (int64_t T = blockIdx.x; T < ntiles; T += gridDim.x) {
+    const LockItem it = items[lock_find(items, nitems, T)];
+    RowCtx rc;
+    rc.row = it.row;
+    rc.traj = 0;
+    rc.r = b.rows[it.row];
+    rc.p = b.programs[rc.r.program];
+    const int n = rc.p.n;
+    const DevMeas M = b.meas[it.pass];
+    const int nt = int(M.end - M.begin);
+    stage_terms(b, a, sm, rc, M, false);
+    for (int i = threadIdx.x; i < 2 * nt; i += blockDim.x) sm.macc[i] = 0.0;
+    build_hi_table(sm.hi, M.tile_mask);
+    __syncthreads();
+    const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+    const uint32_t base = deposit(uint32_t(T - it.prefix), all & ~M.tile_mask);
+    tile_load_async(sm.psi, arena + it.off, sm.hi, base);
+    tile_load_wait();
+    __syncthreads();
+    measure_tile(sm, nt, 1u << kTile, base, false);
+    __syncthreads();
+    double* dst = wacc + 2 * int64_t(M.begin);
+    for (int i = threadIdx.x; i < 2 * nt; i += blockDim.x)
+      if (sm.macc[i] != 0.0) atomicAdd(dst + i, sm.macc[i]);
+    __syncthreads();
+  }
+}
+
+// out_f of every row of the group: one CTA per row (acc: num_ops doubles per row)
+__global__ void lock_expect_finalize_kernel(BatchDevice b, RunArgs a, const LockItem* rows,
+                                            const double* wacc, double* acc) {
+  const LockItem it = rows[blockIdx.x];
+  expect_finalize_body(b, a, it.row, wacc, 0, acc + int64_t(blockIdx.x) * b.num_ops);
+}
+
+// chunk sums of every row: global chunk C of item i -> csum[C]
+__global__ void __launch_bounds__(256)
+lock_chunk_sums_kernel(const LockItem* rows, int nrows, int64_t nchunks, const float2* arena,
+                       double* csum) {
+  __shared__ double part[8];
+  for (int64_t C = blockIdx.x; C < nchunks; C += gridDim.x) {
+    const LockItem it = rows[lock_find(rows, nrows, C)];
+    chunk_sum_body(arena + it.off + ((C - it.prefix) << kTile), csum + C, part);
+  }
+}
+
+// samples of every row: one CTA per row
+__global__ void __launch_bounds__(512)
+lock_sample_kernel(BatchDevice b, RunArgs a, const LockItem* rows, const float2* arena,
+                   double* csum) {
+  __shared__ double seg[512];
+  const LockItem it = rows[blockIdx.x];
+  sample_row_body(b, a, it.row, arena + it.off, it.n, csum + it.prefix, seg);
+}
+
+// -2 padding of the state rows: amplitudes [2^n, 2^max_n) of every row
+__global__ void lock_pad_kernel(BatchDevice b, RunArgs a, const LockItem* rows) {
+  const LockItem it = rows[blockIdx.y];
+  float2* out = a.out_state + (int64_t(it.row) << b.max_n);
+  const int64_t lo = int64_t(1) << it.n, hi = int64_t(1) << b.max_n;
+  for (int64_t k = lo + int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < hi;
+       k += int64_t(gridDim.x) * blockDim.x)
+    out[k] = make_float2(-2.f, 0.f);
 }
 
 __global__ void fill_kernel(float2* p, int64_t count, float2 first, float2 rest) {
@@ -545,6 +647,51 @@ cudaError_t launch_wide_chunk_sums(const float2* psi, int n, double* csum, int g
 cudaError_t launch_wide_sample(const BatchDevice& b, const RunArgs& a, int row,
                                const float2* psi, int n, double* csum, cudaStream_t s) {
   wide_sample_kernel<<<1, 512, 0, s>>>(b, a, row, psi, n, csum);
+  return cudaGetLastError();
+}
+
+const void* lock_measure_kernel_ptr() {
+  return reinterpret_cast<const void*>(&lock_measure_kernel);
+}
+
+cudaError_t launch_lock_measure(const BatchDevice& b, const RunArgs& a, const LockItem* items,
+                                int nitems, int64_t ntiles, const float2* arena,
+                                double* wacc, int grid, size_t smem, int state_amps,
+                                cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  lock_measure_kernel<<<grid, kWideThreads, smem, s>>>(b, a, items, nitems, ntiles, arena,
+                                                      wacc, state_amps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lock_expect_finalize(const BatchDevice& b, const RunArgs& a,
+                                        const LockItem* rows, int nrows, const double* wacc,
+                                        double* scratch, cudaStream_t s) {
+  if (nrows <= 0) return cudaSuccess;
+  lock_expect_finalize_kernel<<<nrows, 256, 0, s>>>(b, a, rows, wacc, scratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lock_chunk_sums(const LockItem* rows, int nrows, int64_t nchunks,
+                                   const float2* arena, double* csum, int grid,
+                                   cudaStream_t s) {
+  if (nchunks <= 0) return cudaSuccess;
+  lock_chunk_sums_kernel<<<grid, 256, 0, s>>>(rows, nrows, nchunks, arena, csum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lock_sample(const BatchDevice& b, const RunArgs& a, const LockItem* rows,
+                               int nrows, const float2* arena, double* csum,
+                               cudaStream_t s) {
+  if (nrows <= 0) return cudaSuccess;
+  lock_sample_kernel<<<nrows, 512, 0, s>>>(b, a, rows, arena, csum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lock_pad(const BatchDevice& b, const RunArgs& a, const LockItem* rows,
+                            int nrows, cudaStream_t s) {
+  if (nrows <= 0) return cudaSuccess;
+  lock_pad_kernel<<<dim3(8, unsigned(nrows)), 256, 0, s>>>(b, a, rows);
   return cudaGetLastError();
 }
 

@@ -167,6 +167,45 @@ cudaError_t launch_wide_chunk_sums(const float2* psi, int n, double* csum, int g
 // (scanned in place) and writes them in the reference bit layout.
 cudaError_t launch_wide_sample(const BatchDevice& b, const RunArgs& a, int row,
                                const float2* psi, int n, double* csum, cudaStream_t s);
+// Lockstep rows (forward modes): streamed rows of lock_min..21 qubits in a
+// batch with many of them run side by side over the whole grid instead of
+// one CTA each: launch k runs forward pass k of every row of a group, tile
+// by tile (the launch boundary orders the passes), then the measurement
+// passes, the expectation finalize or the sampling, all over the group's
+// rows at once.  An item is one row of a launch: its pass (forward or
+// measurement), the global index of its first tile or chunk (prefix,
+// ascending over the items), its state offset in the arena and its qubits.
+struct LockItem {
+  int32_t row;
+  uint32_t pass;
+  int64_t prefix;
+  int64_t off;
+  int32_t n;
+  int32_t pad_;
+};
+static_assert(sizeof(LockItem) == 32, "LockItem layout");
+const void* sim_kernel_lock();
+cudaError_t sim_launch_lock(const BatchDevice& b, const RunArgs& a, const LockItem* items,
+                            int nitems, int64_t ntiles, float2* arena, int init,
+                            int to_out_state, int grid, size_t smem, int state_amps,
+                            cudaStream_t s);
+const void* lock_measure_kernel_ptr();
+cudaError_t launch_lock_measure(const BatchDevice& b, const RunArgs& a, const LockItem* items,
+                                int nitems, int64_t ntiles, const float2* arena,
+                                double* wacc, int grid, size_t smem, int state_amps,
+                                cudaStream_t s);
+// out_f of the rows; `scratch` holds nrows * num_ops doubles.
+cudaError_t launch_lock_expect_finalize(const BatchDevice& b, const RunArgs& a,
+                                        const LockItem* rows, int nrows, const double* wacc,
+                                        double* scratch, cudaStream_t s);
+cudaError_t launch_lock_chunk_sums(const LockItem* rows, int nrows, int64_t nchunks,
+                                   const float2* arena, double* csum, int grid,
+                                   cudaStream_t s);
+cudaError_t launch_lock_sample(const BatchDevice& b, const RunArgs& a, const LockItem* rows,
+                               int nrows, const float2* arena, double* csum,
+                               cudaStream_t s);
+cudaError_t launch_lock_pad(const BatchDevice& b, const RunArgs& a, const LockItem* rows,
+                            int nrows, cudaStream_t s);
 // Tensor-core forward path (tc_gates.cu).  launch_tc_fuse writes the
 // 32 x 32 complex64 matrix of each block (row-major, 1024 entries per block)
 // from the row's bound gate matrices `mats`; launch_tc_apply5 applies one

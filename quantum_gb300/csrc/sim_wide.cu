@@ -13,6 +13,61 @@ simulate_wide_pass_kernel(BatchDevice b, RunArgs a, int row, int pass, int init,
   wide_pass_body<InterpExec>(b, a, row, pass, init, psi, state_amps);
 }
 
+// Lockstep rows: one forward pass of every row of a group (items[i].pass of
+// row items[i].row), tile by tile over the whole grid; the state of a row is
+// its output row (tfq_simulate_state) or arena + items[i].off.  `init`
+// starts each row from |0...0> instead of loading its state.
+__global__ void __launch_bounds__(kWideThreads, 2)
+simulate_lock_pass_kernel(BatchDevice b, RunArgs a, const LockItem* items, int nitems,
+                          int64_t ntiles, float2* arena, int init, int to_out_state,
+                          int state_amps) {
+  const Smem sm = carve_smem<kModeState>(state_amps, 1);
+  int kc = 0;  // sub-pass counter (staging buffer parity)
+  for (int64_t T = blockIdx.x; T < ntiles; T += gridDim.x) {
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (items[mid].prefix <= T) lo = mid;
+      else hi = mid - 1;
+    }
+    const LockItem it = items[lo];
+    RowCtx rc;
+    rc.row = it.row;
+    rc.traj = 0;
+    rc.r = b.rows[it.row];
+    rc.p = b.programs[rc.r.program];
+    const int n = rc.p.n;
+    float2* psi = to_out_state ? a.out_state + (int64_t(it.row) << b.max_n) : arena + it.off;
+    const DevPass ps = b.passes[it.pass];
+    build_hi_table(sm.hi, ps.tile_mask);
+    __syncthreads();
+    const uint32_t all = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+    const uint32_t base = deposit(uint32_t(T - it.prefix), all & ~ps.tile_mask);
+    if (init) tile_zero(sm.psi, base == 0);
+    else tile_load_async(sm.psi, psi, sm.hi, base);
+    tile_load_wait();
+    __syncthreads();
+    run_ops<kModeState, InterpExec>(b, a, sm, rc, ps.op_begin, ps.op_end, sm.psi, sm.lam,
+                                    kTile, base, kc);
+    tile_store(psi, sm.psi, sm.hi, base);
+    __syncthreads();
+  }
+}
+
+const void* sim_kernel_lock() {
+  return reinterpret_cast<const void*>(&simulate_lock_pass_kernel);
+}
+
+cudaError_t sim_launch_lock(const BatchDevice& b, const RunArgs& a, const LockItem* items,
+                            int nitems, int64_t ntiles, float2* arena, int init,
+                            int to_out_state, int grid, size_t smem, int state_amps,
+                            cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  simulate_lock_pass_kernel<<<grid, kWideThreads, smem, s>>>(
+      b, a, items, nitems, ntiles, arena, init, to_out_state, state_amps);
+  return cudaGetLastError();
+}
+
 // Wide rows in the adjoint (interpreter): lambda accumulation and backward
 // passes, one launch per pass, then the gradient finalize.
 __global__ void __launch_bounds__(kSimThreads, 1)
