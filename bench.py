@@ -434,6 +434,38 @@ def run_config(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    graph = None
+    if wl == "c3":
+        # the same step as two CUDA-graph launches (expectation, samples):
+        # each captures the whole batched call, queue kernel and lockstep
+        # launches included
+        direct_ms = ms
+        ge = batch.capture("expectation", vals)
+        gs = batch.capture("samples", vals, num_samples=1000, seed=7)
+        for _ in range(2):
+            ge.replay()
+            gs.replay()
+        torch.cuda.synchronize()
+        gev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        clocks = ClockSampler(0)
+        clocks.start()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            gev[k][0].record()
+            out = ge.replay()
+            gs.replay()
+            gev[k][1].record()
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        ms = float(np.mean([a.elapsed_time(b) for a, b in gev]))
+        graph = {"graph_launches_per_step": 2, "ms_per_step": ms,
+                 "direct_calls_ms_per_step": direct_ms,
+                 "lockstep_rows": __import__("quantum_gb300")._native.batch_lock_rows(
+                     batch._h)[0]}
+        out = out.clone()
+        ge.close()
+        gs.close()
     line = {"metric": f"{wl} throughput", "value": units / (ms / 1e3), "unit": unit,
             "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "dtype": "c64 (f32 state, f64 reductions)",
@@ -442,6 +474,8 @@ def run_config(args):
             "host_parse_plan_s": parse_s, "clocks": clk,
             "specialized": sorted(__import__("quantum_gb300")._native.batch_specialization(
                 batch._h)[1])}
+    if graph:
+        line["cuda_graph"] = graph
     line["roofline"] = config_roofline(wl, w, batch, ms, clk, units)
     if wl in ("c1", "c3", "c5"):
         line["accuracy"] = config_accuracy(wl, w, batch, vals, out)

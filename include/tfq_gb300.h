@@ -198,6 +198,28 @@ int tfqg_batch_expectation_noalloc(tfqg_batch* b, const float* symbol_values,
                                    float* expectations, void* stream);
 
 /* ---------------------------------------------------------------------
+ * CUDA graphs of a batch's forward calls: one call (0 expectation, 1 state,
+ * 2 samples) with DEVICE buffers captured once and replayed per step.  The
+ * reference runs each op call as a fresh Compute (ComputeSmall/Large of
+ * tfq_simulate_expectation_op.cc:182-250, tfq_simulate_samples_op.cc:191-251);
+ * here a whole batched call -- matrix build, the persistent queue kernel,
+ * the lockstep and wide-row launches -- becomes one graph launch.
+ * tfqg_batch_graph_create runs the call once normally (buffers, tables and
+ * compiled modules in place), then captures it on `stream` (not the legacy
+ * default stream).  A replay reads the symbol values and writes the output
+ * at the captured device pointers, so new values written there are used;
+ * samples replay with the captured seed.  A replay is refused (INVALID_ARGUMENT)
+ * once another call on the batch has replaced one of its device buffers.
+ * The graph must be destroyed before its batch.
+ * ------------------------------------------------------------------- */
+typedef struct tfqg_graph tfqg_graph;
+int tfqg_batch_graph_create(tfqg_batch* b, int what, const float* symbol_values,
+                            int32_t num_samples, uint64_t seed, void* out, void* stream,
+                            tfqg_graph** graph);
+int tfqg_graph_launch(tfqg_graph* g, void* stream);
+void tfqg_graph_destroy(tfqg_graph* g);
+
+/* ---------------------------------------------------------------------
  * One-shot entry points with the reference op signatures and HOST buffers
  * (what a TF CPU-side OpKernel::Compute holds).  They create a transient
  * batch, run it and destroy it.

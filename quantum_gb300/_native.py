@@ -59,6 +59,12 @@ EXPORTED = (
 def _declare(lib):
     lib.tfqg_last_error.restype = ctypes.c_char_p
     lib.tfqg_version.restype = ctypes.c_char_p
+    lib.tfqg_batch_graph_create.argtypes = [c_void_p, ctypes.c_int, c_void_p, ctypes.c_int32,
+                                            ctypes.c_uint64, c_void_p, c_void_p,
+                                            ctypes.POINTER(c_void_p)]
+    lib.tfqg_graph_launch.argtypes = [c_void_p, c_void_p]
+    lib.tfqg_graph_destroy.argtypes = [c_void_p]
+    lib.tfqg_graph_destroy.restype = None
     lib.tfqg_batch_create.argtypes = [
         c_char_pp, c_int64_p, ctypes.c_int64, c_char_pp, c_int64_p,
         ctypes.c_int64, c_char_pp, c_int64_p, ctypes.c_int64, ctypes.c_int,

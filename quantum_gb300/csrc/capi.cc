@@ -325,7 +325,7 @@ void build_lock_schedule(tfqg_batch* b) {
       off[k - i] = o;
       b->lock_items.push_back(LockItem{row, 0u, chunks, o, n, 0});
       o += int64_t(1) << n;
-      chunks += int64_t(1) << (n - kStreamTileBits);
+      chunks += int64_t(1) << (n - kLockChunkBits);
     }
     g.rows.count = int32_t(j - i);
     g.rows.ntiles = chunks;
@@ -1730,6 +1730,106 @@ int tfqg_simulate_expectation(const char* const* programs,
   rc = tfqg_batch_expectation(b, symbol_values, expectations, 0, nullptr);
   tfqg_batch_destroy(b);
   return rc;
+}
+
+// ---- CUDA graphs of a batch's forward calls ----------------------------------
+
+}  // extern "C"
+
+struct tfqg_graph {
+  tfqg_batch* batch = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<void*> buffers;  // the batch's device buffers at capture
+};
+
+namespace {
+// Device buffers a captured call may address; a graph replays only while
+// every one of them is still the buffer it captured.
+std::vector<void*> batch_buffers(tfqg_batch* b) {
+  return {b->tables.p,     b->mats.p,      b->dmats.p,     b->work.p,     b->counter.p,
+          b->values.p,     b->out.p,       b->aux.p,       b->aux2.p,     b->wide_state.p,
+          b->wide_acc.p,   b->tc_tab.p,    b->tc_mats.p,   b->tc_status.p, b->lock_state.p,
+          b->lock_acc.p};
+}
+
+int run_forward(tfqg_batch* b, int what, const float* values, int32_t num_samples,
+                uint64_t seed, void* out, void* stream) {
+  if (what == 0)
+    return tfqg_batch_expectation(b, values, static_cast<float*>(out), 1, stream);
+  if (what == 1) return tfqg_batch_state(b, values, out, 1, stream);
+  return tfqg_batch_samples(b, values, num_samples, seed, static_cast<int8_t*>(out), 1, stream);
+}
+}  // namespace
+
+extern "C" {
+
+int tfqg_batch_graph_create(tfqg_batch* b, int what, const float* symbol_values,
+                            int32_t num_samples, uint64_t seed, void* out, void* stream,
+                            tfqg_graph** graph) {
+  if (!b || !graph) return fail(kInvalidArgument, "NULL argument");
+  if (what < 0 || what > 2) return fail(kInvalidArgument, "unknown call to capture");
+  *graph = nullptr;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!s) return fail(kInvalidArgument, "capture needs a stream other than the legacy default");
+  // one ordinary call first: tables, buffers and compiled modules in place
+  int rc = run_forward(b, what, symbol_values, num_samples, seed, out, stream);
+  if (rc) return rc;
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return fail(kInternal, "stream synchronize failed before capture");
+  std::unique_ptr<tfqg_graph> g(new tfqg_graph());
+  g->batch = b;
+  g->buffers = batch_buffers(b);
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess)
+    return fail(kInternal, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
+  rc = run_forward(b, what, symbol_values, num_samples, seed, out, stream);
+  cudaGraph_t cg = nullptr;
+  e = cudaStreamEndCapture(s, &cg);
+  if (rc) {
+    if (cg) cudaGraphDestroy(cg);
+    return rc;
+  }
+  if (e != cudaSuccess || !cg) {
+    cudaGetLastError();
+    return fail(kInternal, std::string("this call cannot be captured: ") +
+                               cudaGetErrorString(e));
+  }
+  if (batch_buffers(b) != g->buffers) {
+    cudaGraphDestroy(cg);
+    return fail(kInternal, "the captured call moved the batch's buffers");
+  }
+  g->graph = cg;
+  e = cudaGraphInstantiate(&g->exec, cg, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(cg);
+    g->graph = nullptr;
+    return fail(kInternal, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  *graph = g.release();
+  return 0;
+}
+
+int tfqg_graph_launch(tfqg_graph* g, void* stream) {
+  if (!g || !g->exec) return fail(kInvalidArgument, "NULL graph");
+  {
+    std::lock_guard<std::mutex> lk(g->batch->mu);
+    if (batch_buffers(g->batch) != g->buffers)
+      return fail(kInvalidArgument,
+                  "the batch's device buffers changed since the graph was captured "
+                  "(another call on the batch needed larger ones); capture it again");
+  }
+  const cudaError_t e = cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess)
+    return fail(kInternal, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+void tfqg_graph_destroy(tfqg_graph* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
 }
 
 int tfqg_max_num_qubits(const char* const* programs, const int64_t* program_lens,

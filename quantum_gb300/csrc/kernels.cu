@@ -342,9 +342,11 @@ wide_chunk_sums_kernel(const float2* psi, int n, double* csum) {
 // its chunk by binary search and its index by a scan inside the chunk
 // (StateSpace::Sample semantics: index x with probability |psi_x|^2; bit k
 // of x goes to column max_n - k - 1, tfq_simulate_samples_op.cc:226-243).
+// Samples of one row from its chunk sums (chunks of 2^cbits amplitudes).
 __device__ void sample_row_body(const BatchDevice& b, const RunArgs& a, int row,
-                                const float2* psi, int n, double* csum, double* seg) {
-  const uint32_t nch = 1u << (n - kTile);
+                                const float2* psi, int n, double* csum, double* seg,
+                                int cbits = kTile) {
+  const uint32_t nch = 1u << (n - cbits);
   const uint32_t per = (nch + blockDim.x - 1) / blockDim.x;
   const uint32_t lo = min(threadIdx.x * per, nch), hi = min(lo + per, nch);
   double run = 0.0;
@@ -367,7 +369,7 @@ __device__ void sample_row_body(const BatchDevice& b, const RunArgs& a, int row,
   __syncthreads();
   const double total = csum[nch - 1];
   const int maxn = b.max_n, S = a.num_samples;
-  const uint32_t L = 1u << kTile;
+  const uint32_t L = 1u << cbits;
   int8_t* out = a.out_samples + int64_t(row) * S * maxn;
   for (int s = threadIdx.x; s < S; s += blockDim.x) {
     const double u = uniform01(a.seed, uint32_t(row), uint32_t(s), 0x5A3Fu) * total;
@@ -460,14 +462,30 @@ __global__ void lock_expect_finalize_kernel(BatchDevice b, RunArgs a, const Lock
   expect_finalize_body(b, a, it.row, wacc, 0, acc + int64_t(blockIdx.x) * b.num_ops);
 }
 
-// chunk sums of every row: global chunk C of item i -> csum[C]
+// Sampling of lockstep rows uses chunks of 2^kLockChunkBits (kernels.h)
+// amplitudes, so that a sample's search ends in a short scan (the chunk)
+// after a binary search over the row's chunk sums.
+// chunk sums of every row, one warp per chunk: chunk C of the launch (row
+// item i: its chunks from rows[i].prefix) -> csum[C]
 __global__ void __launch_bounds__(256)
 lock_chunk_sums_kernel(const LockItem* rows, int nrows, int64_t nchunks, const float2* arena,
                        double* csum) {
-  __shared__ double part[8];
-  for (int64_t C = blockIdx.x; C < nchunks; C += gridDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t C = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); C < nchunks;
+       C += warps) {
     const LockItem it = rows[lock_find(rows, nrows, C)];
-    chunk_sum_body(arena + it.off + ((C - it.prefix) << kTile), csum + C, part);
+    const float4* p = reinterpret_cast<const float4*>(
+        arena + it.off + ((C - it.prefix) << kLockChunkBits));
+    float f = 0.f;
+#pragma unroll
+    for (int k = 0; k < (1 << (kLockChunkBits - 1)) / 32; ++k) {
+      const float4 v = __ldcg(p + lane + 32 * k);
+      f = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, f))));
+    }
+    double d = f;
+    for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) csum[C] = d;
   }
 }
 
@@ -477,7 +495,7 @@ lock_sample_kernel(BatchDevice b, RunArgs a, const LockItem* rows, const float2*
                    double* csum) {
   __shared__ double seg[512];
   const LockItem it = rows[blockIdx.x];
-  sample_row_body(b, a, it.row, arena + it.off, it.n, csum + it.prefix, seg);
+  sample_row_body(b, a, it.row, arena + it.off, it.n, csum + it.prefix, seg, kLockChunkBits);
 }
 
 // -2 padding of the state rows: amplitudes [2^n, 2^max_n) of every row

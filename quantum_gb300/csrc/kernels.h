@@ -184,6 +184,9 @@ struct LockItem {
   int32_t pad_;
 };
 static_assert(sizeof(LockItem) == 32, "LockItem layout");
+// Lockstep sampling sums |psi|^2 over chunks of 2^kLockChunkBits amplitudes
+// (a row item's prefix counts these chunks).
+constexpr int kLockChunkBits = 8;
 const void* sim_kernel_lock();
 cudaError_t sim_launch_lock(const BatchDevice& b, const RunArgs& a, const LockItem* items,
                             int nitems, int64_t ntiles, float2* arena, int init,

@@ -284,11 +284,75 @@ class Batch:
         return self._counts_call(_native.lib().tfqg_batch_sampled_expectation,
                                  symbol_values, num_samples, seed)
 
+    def capture(self, what, values, num_samples=0, seed=0, stream=None):
+        """A Graph of one forward call ("expectation", "state" or
+        "samples") on CUDA `values`; close it before the batch."""
+        return Graph(self, what, values, num_samples, seed, stream)
+
     @staticmethod
     def _wrap(symbol_values, out):
         if _is_torch(symbol_values) and not _is_torch(out):
             return torch.from_numpy(out)
         return out
+
+
+class Graph:
+    """One forward call of a Batch (expectation, state or samples) captured
+    in a CUDA graph (tfqg_batch_graph_create): `replay()` relaunches the
+    whole batched call -- matrix build, persistent queue kernel, lockstep and
+    wide-row launches -- as one graph launch on the capture stream.  The
+    graph reads `values` and writes `out` (torch CUDA tensors held here), so
+    writing new symbol values into `values` and replaying gives their
+    results; samples replay with the captured seed."""
+
+    _WHAT = {"expectation": 0, "state": 1, "samples": 2}
+
+    def __init__(self, batch, what, values, num_samples=0, seed=0, stream=None):
+        if not (_is_torch(values) and values.is_cuda):
+            raise InvalidArgumentError("a graph captures device buffers: values must be a "
+                                       "CUDA tensor")
+        batch._check_values(values)
+        self.batch = batch
+        self.values = values
+        self.stream = stream or torch.cuda.Stream(device=values.device)
+        if what == "expectation":
+            self.out = torch.empty((batch.batch_size, batch.num_ops), dtype=torch.float32,
+                                   device=values.device)
+        elif what == "state":
+            self.out = torch.empty((batch.batch_size, 2 ** batch.max_num_qubits),
+                                   dtype=torch.complex64, device=values.device)
+        else:
+            self.out = torch.empty((batch.batch_size, int(num_samples),
+                                    batch.max_num_qubits), dtype=torch.int8,
+                                   device=values.device)
+        self.stream.wait_stream(torch.cuda.current_stream(values.device))
+        h = ctypes.c_void_p()
+        _native.check(_native.lib().tfqg_batch_graph_create(
+            batch._h, self._WHAT[what], ctypes.c_void_p(values.data_ptr()), int(num_samples),
+            int(seed) & (2 ** 64 - 1), ctypes.c_void_p(self.out.data_ptr()),
+            ctypes.c_void_p(self.stream.cuda_stream), ctypes.byref(h)))
+        self._g = h
+
+    def replay(self):
+        """One graph launch on the capture stream (ordered after the current
+        stream's work); returns `out`."""
+        cur = torch.cuda.current_stream(self.values.device)
+        self.stream.wait_stream(cur)
+        _native.check(_native.lib().tfqg_graph_launch(
+            self._g, ctypes.c_void_p(self.stream.cuda_stream)))
+        cur.wait_stream(self.stream)
+        return self.out
+
+    def close(self):
+        if getattr(self, "_g", None):
+            _native.lib().tfqg_graph_destroy(self._g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class InnerProductBatch(Batch):
