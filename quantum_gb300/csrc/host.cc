@@ -1162,34 +1162,42 @@ void plan_program(CompiledProgram* p, JobKind kind, bool fuse) {
   std::vector<int> chan_bits(p->channels.size(), 0);
   // a re-plan starts again from the program's own gates
   while (!p->gates.empty() && p->gates.back().kind == GK_FUSED) p->gates.pop_back();
+  // the forward passes run the fused gates (also the adjoint's forward
+  // recompute of psi, as the reference's full_fuse does); the adjoint's
+  // backward passes keep one step per gate, since every symbolic gate needs
+  // its own lambda step
   std::vector<int32_t> fused;
-  const bool fusing = fuse && kind == kJobForward;
+  const bool fusing = fuse && (kind == kJobForward || kind == kJobAdjoint);
   if (fusing) fuse_forward(p, &fused);
-  const std::vector<int32_t>& sequence = fusing ? fused : p->sequence;
-  std::vector<PlanItem> items;
-  items.reserve(sequence.size());
-  for (int32_t s : sequence) {
-    PlanItem it;
-    it.seq = s;
-    if (s >= 0) {
-      const GateTemplate& g = p->gates[s];
-      // identity gates do nothing, also in the adjoint (no parameters)
-      if (g.cls == GC_SKIP) continue;
-      uint32_t targets, cmask, cval;
-      gate_bits(g, &targets, &cmask, &cval);
-      it.targets = targets;
-      it.deps = targets | cmask;
-    } else {
-      int bit = p->channels[~s].bit;
-      chan_bits[~s] = bit;
-      it.targets = 1u << bit;
-      it.deps = it.targets;
+  auto make_items = [&](const std::vector<int32_t>& sequence) {
+    std::vector<PlanItem> items;
+    items.reserve(sequence.size());
+    for (int32_t s : sequence) {
+      PlanItem it;
+      it.seq = s;
+      if (s >= 0) {
+        const GateTemplate& g = p->gates[s];
+        // identity gates do nothing, also in the adjoint (no parameters)
+        if (g.cls == GC_SKIP) continue;
+        uint32_t targets, cmask, cval;
+        gate_bits(g, &targets, &cmask, &cval);
+        it.targets = targets;
+        it.deps = targets | cmask;
+      } else {
+        int bit = p->channels[~s].bit;
+        chan_bits[~s] = bit;
+        it.targets = 1u << bit;
+        it.deps = it.targets;
+      }
+      items.push_back(it);
     }
-    items.push_back(it);
-  }
+    return items;
+  };
+  const std::vector<PlanItem> items = make_items(fusing ? fused : p->sequence);
   plan_sequence(*p, items, tile_bits, false, chan_bits, &p->fwd_passes, &p->fwd_ops);
   if (kind == kJobAdjoint) {
-    std::vector<PlanItem> rev(items.rbegin(), items.rend());
+    const std::vector<PlanItem> per_gate = fusing ? make_items(p->sequence) : items;
+    std::vector<PlanItem> rev(per_gate.rbegin(), per_gate.rend());
     plan_sequence(*p, rev, tile_bits, true, chan_bits, &p->bwd_passes, &p->bwd_ops);
   }
 }
