@@ -152,16 +152,21 @@ def adjoint_flop_per_circuit(w):
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "tfqg_jit_adjoint_adjoint_hea_16q.md")
 
 
-def profiled_traffic_per_circuit():
-    """DRAM bytes (read + write) per circuit of the adjoint launch, from the
-    committed ncu summary (a line `dram_bytes_per_circuit: <int>`)."""
+def profiled_value(key, cast=int):
+    """A figure of the committed ncu summary of the adjoint launch (a line
+    `<key>: <value>`): dram_bytes_per_circuit (DRAM read + write bytes per
+    circuit) or fma_pipe_active (fraction of cycles the FMA pipe was busy)."""
     try:
         for ln in open(PROFILE_TRAFFIC):
-            if ln.strip().startswith("dram_bytes_per_circuit:"):
-                return int(ln.split(":", 1)[1].strip())
+            if ln.strip().startswith(key + ":"):
+                return cast(ln.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
+
+
+def profiled_traffic_per_circuit():
+    return profiled_value("dram_bytes_per_circuit")
 
 
 def run_reference(args, rank, world):
@@ -404,6 +409,20 @@ def run_config(args):
     if wl == "c4":
         __import__("quantum_gb300")._native.set_tensor_core_gates(
             {"auto": 2, "on": 1, "off": 0}[args.tensor_cores])
+    tuned = None
+    if wl == "c3":
+        # the autotuner picks fusion width and tile schedule per qubit count
+        # on this GPU (untimed, before the batch is built)
+        from quantum_gb300 import autotune
+        t0 = time.perf_counter()
+        res = autotune.tune(w["programs"], w["pauli_sums"], samples=1000, use_cache=False)
+        tuned = {"seconds": time.perf_counter() - t0,
+                 "per_qubit_count": {str(n): {"fusion_width": 2 if r["fuse"] else 1,
+                                              "schedule": ("lockstep" if r["lock"] == 1 else
+                                                           "queue" if r["lock"] == 0 else
+                                                           "default"),
+                                              "ms_sample": r["ms"], "rows_timed": r["rows"]}
+                                     for n, r in res.items()}}
     t0 = time.perf_counter()
     batch = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
     parse_s = time.perf_counter() - t0
@@ -476,6 +495,8 @@ def run_config(args):
                 batch._h)[1])}
     if graph:
         line["cuda_graph"] = graph
+    if tuned:
+        line["autotune"] = tuned
     line["roofline"] = config_roofline(wl, w, batch, ms, clk, units)
     if wl in ("c1", "c3", "c5"):
         line["accuracy"] = config_accuracy(wl, w, batch, vals, out)
@@ -828,6 +849,13 @@ def main():
             "bound": "fp32", "kernel": adj_kernel,
             "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": achieved_tflops / fp32_peak, "traffic": traffic,
+            "traffic_source": "not measured in this run: ncu DRAM bytes per circuit from the "
+                              "committed summary profiles/tfqg_jit_adjoint_adjoint_hea_16q.md, "
+                              "scaled to the circuits of one launch",
+            "fma_pipe_frac_ncu": profiled_value("fma_pipe_active", float),
+            "fma_pipe_note": "the dense-matrix flop count overstates the FMAs the specialized "
+                             "gate classes issue; ncu's FMA-pipe activity of the same kernel "
+                             "(same summary) is the direct utilisation figure",
             "algorithmic": f"{adjoint_flop_per_circuit(w) / 1e9:.4f} GFLOP per circuit "
                            f"x {BATCH} circuits per launch",
             "peak_source": f"derived: {props.multi_processor_count} SMs x 128 FP32 lanes x 2 flop "

@@ -145,6 +145,28 @@ int wide_min_qubits() { return g_wide_min_qubits.load(); }
 
 // Gate fusion of forward plans (on by default).
 std::atomic<int> g_gate_fusion{1};
+// Row policy per qubit count, set by an autotuner (quantum_gb300/autotune.py)
+// for batches created from then on: gate fusion of the forward plans
+// (-1: the global setting, 0 off, 1 on) and lockstep rows (-1: the
+// lock_min rule, 0 never, 1 when the row is streamed and not wide).  Each
+// change starts a new epoch, which is part of the compiled-program cache key.
+constexpr int kPolicyMaxQubits = 64;
+std::atomic<int> g_fuse_by_n[kPolicyMaxQubits];
+std::atomic<int> g_lock_by_n[kPolicyMaxQubits];
+std::atomic<int> g_policy_epoch{0};
+struct PolicyInit {
+  PolicyInit() {
+    for (int i = 0; i < kPolicyMaxQubits; ++i) {
+      g_fuse_by_n[i].store(-1);
+      g_lock_by_n[i].store(-1);
+    }
+  }
+} g_policy_init;
+
+bool fuse_for(int n, bool dflt) {
+  const int v = (n >= 0 && n < kPolicyMaxQubits) ? g_fuse_by_n[n].load() : -1;
+  return v < 0 ? dflt : v != 0;
+}
 
 // Forward passes of wide rows as 5-bit fused blocks on the tensor cores
 // (tc_gates.cu) instead of tile passes on the FP32 pipe: 0 never, 1 always,
@@ -217,7 +239,7 @@ struct ProgramCacheEntry {
   std::string bytes;
   std::string names;  // length-prefixed symbol names, column order
   int job = 0;
-  bool fuse = false;
+  int plan_key = 0;    // fusion setting and row-policy epoch
   bool empty = false;  // no moments: expectation -2 (#679)
   CompiledProgram cp;
   std::unordered_map<std::string, int> index;
@@ -235,23 +257,23 @@ std::atomic<int> g_pc_on{1};
 std::atomic<int64_t> g_pc_hits{0}, g_pc_misses{0};
 
 uint64_t program_cache_hash(const char* p, size_t n, const std::string& names, int job,
-                            bool fuse) {
+                            int plan_key) {
   uint64_t h = ProtoKeyHash()(ProtoKey{p, n, -1});
-  h ^= ProtoKeyHash()(ProtoKey{names.data(), names.size(), job * 2 + (fuse ? 1 : 0)}) +
+  h ^= ProtoKeyHash()(ProtoKey{names.data(), names.size(), job * 4096 + plan_key}) +
        0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
   return h;
 }
 
 std::shared_ptr<const ProgramCacheEntry> program_cache_find(const char* p, size_t n,
                                                             const std::string& names,
-                                                            int job, bool fuse) {
+                                                            int job, int plan_key) {
   if (!g_pc_on.load()) return nullptr;
-  const uint64_t h = program_cache_hash(p, n, names, job, fuse);
+  const uint64_t h = program_cache_hash(p, n, names, job, plan_key);
   std::lock_guard<std::mutex> lk(g_pc_mu);
   auto range = g_pc.equal_range(h);
   for (auto it = range.first; it != range.second; ++it) {
     const ProgramCacheEntry& e = *it->second;
-    if (e.job == job && e.fuse == fuse && e.bytes.size() == n && e.names == names &&
+    if (e.job == job && e.plan_key == plan_key && e.bytes.size() == n && e.names == names &&
         memcmp(e.bytes.data(), p, n) == 0) {
       const_cast<ProgramCacheEntry&>(e).stamp = ++g_pc_clock;
       g_pc_hits.fetch_add(1);
@@ -271,7 +293,7 @@ void program_cache_insert(std::shared_ptr<ProgramCacheEntry> e) {
             e->index.size() * 48 + 256;
   if (e->cost > kProgramCacheBytes / 4) return;
   const uint64_t h = program_cache_hash(e->bytes.data(), e->bytes.size(), e->names, e->job,
-                                        e->fuse);
+                                        e->plan_key);
   std::lock_guard<std::mutex> lk(g_pc_mu);
   while (!g_pc.empty() &&
          (g_pc_bytes + e->cost > kProgramCacheBytes || g_pc.size() >= kProgramCacheEntries)) {
@@ -400,6 +422,8 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     names_key.append(symbol_names[j], size_t(name_lens[j]));
   }
   const bool fuse = g_gate_fusion.load() != 0;
+  // the cache key of a plan: the fusion setting and the row-policy epoch
+  const int plan_key = (fuse ? 1 : 0) | ((g_policy_epoch.load() & 2047) << 1);
 
   // 1. parse programs (ParsePrograms, parse_context.cc:174-206), deduplicated;
   // programs found in the compiled-program cache are not decoded
@@ -423,7 +447,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     }
     ProgramP p;
     std::shared_ptr<const ProgramCacheEntry> hit;
-    if (!inner) hit = program_cache_find(data, size_t(len), names_key, int(job), fuse);
+    if (!inner) hit = program_cache_find(data, size_t(len), names_key, int(job), plan_key);
     if (!hit) decode_program(data, size_t(len), &p);
     int id = int(parsed.size());
     parsed.push_back(std::move(p));
@@ -512,13 +536,13 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       continue;
     }
     compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
-    plan_program(&compiled[pid], job, fuse);
+    plan_program(&compiled[pid], job, fuse_for(compiled[pid].n, fuse));
     if (!inner) {
       auto e = std::make_shared<ProgramCacheEntry>();
       e->bytes.assign(src[pid].p, src[pid].n);
       e->names = names_key;
       e->job = int(job);
-      e->fuse = fuse;
+      e->plan_key = plan_key;
       e->empty = parsed[pid].moments.empty();
       e->cp = compiled[pid];
       e->index = index[pid];
@@ -533,7 +557,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       throw Error(kInvalidArgument,
                   "Found symbols in other_programs.No symbols are allowed in these circuits.");
     }
-    plan_program(&compiled[pid], kJobForward, fuse);
+    plan_program(&compiled[pid], kJobForward, fuse_for(compiled[pid].n, fuse));
   }
 
   // 5. pack programs
@@ -690,8 +714,11 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   // in flight over the whole grid.
   const int lock_min = std::max(g_lock_min_qubits.load(), kStreamTileBits + 1);
   auto is_lock = [&](const DevProgram& p) {
-    return !inner && !is_wide(p) && !p.resident && p.num_channels == 0 &&
-           p.fwd_pass_begin != p.fwd_pass_end && p.n >= lock_min;
+    if (inner || is_wide(p) || p.resident || p.num_channels != 0 ||
+        p.fwd_pass_begin == p.fwd_pass_end || p.n < kStreamTileBits + 1)
+      return false;
+    const int pol = p.n < kPolicyMaxQubits ? g_lock_by_n[p.n].load() : -1;
+    return pol < 0 ? p.n >= lock_min : pol != 0;
   };
   for (const int32_t i : b->order) {
     const DevProgram& p = b->programs[b->rows[i].program];
@@ -2145,6 +2172,22 @@ int tfqg_internal_tc_plan(void* batch, int64_t row, const float* row_values, int
 // Streamed-row count below which rows of 17+ qubits run as wide rows, for
 // batches created after the call (0: never); returns the previous value.
 int tfqg_internal_set_wide_few_rows(int rows) { return g_wide_few_rows.exchange(rows); }
+
+// Row policy for rows of n qubits in batches created from now on (see
+// g_fuse_by_n): fuse / lock -1 default, 0 off, 1 on; n < 0 resets every
+// qubit count.  Returns the new policy epoch.
+int tfqg_internal_set_row_policy(int n, int fuse, int lock) {
+  if (n < 0) {
+    for (int i = 0; i < kPolicyMaxQubits; ++i) {
+      g_fuse_by_n[i].store(-1);
+      g_lock_by_n[i].store(-1);
+    }
+  } else if (n < kPolicyMaxQubits) {
+    g_fuse_by_n[n].store(fuse < 0 ? -1 : fuse != 0);
+    g_lock_by_n[n].store(lock < 0 ? -1 : lock != 0);
+  }
+  return g_policy_epoch.fetch_add(1) + 1;
+}
 
 // Qubit count from which streamed rows of batches created from now on run in
 // lockstep in the forward modes (above 21: never); returns the previous value.
