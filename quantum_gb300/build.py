@@ -130,7 +130,7 @@ def build(force=False, verbose=False):
                                    "-MD", "-MF", obj + ".d",
                                    "-c", src, "-o", obj] + inc
         else:
-            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall",
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-pthread",
                    f'-DTFQG_CUDA_LIB_DIR="{cuda_lib}"', "-MMD", "-MF", obj + ".d",
                    "-c", src, "-o", obj] + inc
         cmds.append(cmd)
@@ -142,7 +142,7 @@ def build(force=False, verbose=False):
                 sys.stdout.write(log)
     tmp = out + ".tmp"
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs +
-         ["-L" + cuda_lib, "-ldl"])
+         ["-L" + cuda_lib, "-ldl", "-lpthread"])
     os.replace(tmp, out)
     return out
 

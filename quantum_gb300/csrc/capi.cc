@@ -11,6 +11,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -383,6 +384,34 @@ void build_lock_schedule(tfqg_batch* b) {
   }
 }
 
+// Runs f(i) for i in [0, n) on the host's cores (serially for small n).  f
+// must not throw: callers keep one exception slot per index and rethrow the
+// first one in index order, so errors surface as a serial loop would raise
+// them.
+template <class F>
+void parallel_for(size_t n, F&& f) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t workers = std::min<size_t>({size_t(hw), size_t(32), n});
+  if (n < 32 || workers <= 1) {
+    for (size_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  auto run = [&]() {
+    for (size_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
+  };
+  std::vector<std::thread> pool;
+  pool.reserve(workers - 1);
+  for (size_t w = 1; w < workers; ++w) pool.emplace_back(run);
+  run();
+  for (std::thread& t : pool) t.join();
+}
+
+void rethrow_first(const std::vector<std::exception_ptr>& errs) {
+  for (const std::exception_ptr& e : errs)
+    if (e) std::rethrow_exception(e);
+}
+
 void build_batch(tfqg_batch* b, const char* const* programs,
                  const int64_t* program_lens, int64_t batch,
                  const char* const* symbol_names, const int64_t* name_lens,
@@ -445,17 +474,29 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       row_prog[i] = it->second;
       continue;
     }
-    ProgramP p;
-    std::shared_ptr<const ProgramCacheEntry> hit;
-    if (!inner) hit = program_cache_find(data, size_t(len), names_key, int(job), plan_key);
-    if (!hit) decode_program(data, size_t(len), &p);
     int id = int(parsed.size());
-    parsed.push_back(std::move(p));
-    cached.push_back(std::move(hit));
+    parsed.emplace_back();
+    cached.emplace_back();
     src.push_back(key);
     pair_of.push_back(paired ? row_prog[k / num_others] : -1);
     prog_ids.emplace(key, id);
     row_prog[i] = id;
+  }
+  // the distinct programs: cache lookups and decoding on the host's cores;
+  // the first failing program in row order raises its error
+  {
+    std::vector<std::exception_ptr> errs(parsed.size());
+    parallel_for(parsed.size(), [&](size_t pid) {
+      try {
+        if (!inner)
+          cached[pid] = program_cache_find(src[pid].p, src[pid].n, names_key, int(job),
+                                           plan_key);
+        if (!cached[pid]) decode_program(src[pid].p, src[pid].n, &parsed[pid]);
+      } catch (...) {
+        errs[pid] = std::current_exception();
+      }
+    });
+    rethrow_first(errs);
   }
   // 2. parse pauli sums (GetPauliSums, parse_context.cc:367-403)
   std::unordered_map<ProtoKey, int, ProtoKeyHash> psum_ids;
@@ -504,9 +545,28 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       resolved[pid] = 1;
     }
   };
+  // outside inner-product batches every distinct program resolves on its
+  // own: on the host's cores, errors raised below in row order
+  std::vector<std::exception_ptr> resolve_errs(parsed.size());
+  if (!inner) {
+    parallel_for(parsed.size(), [&](size_t pid) {
+      try {
+        if (cached[pid]) {
+          index[pid] = cached[pid]->index;
+          compiled[pid] = cached[pid]->cp;
+        } else {
+          resolve_qubits(parsed[pid], &index[pid]);
+        }
+        resolved[pid] = 1;
+      } catch (...) {
+        resolve_errs[pid] = std::current_exception();
+      }
+    });
+  }
   for (int64_t i = 0; i < batch; ++i) {
     int pid = row_prog[i];
     if (i >= main_rows) break;  // paired rows: resolved with their reference
+    if (resolve_errs[pid]) std::rethrow_exception(resolve_errs[pid]);
     if (!resolved[pid]) {
       if (cached[pid]) index[pid] = cached[pid]->index;
       else resolve_qubits(parsed[pid], &index[pid]);
@@ -529,14 +589,31 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   // ones, which may not hold symbols (tfq_inner_product.cc: any construction
   // error of an other_program reports the symbols message)
   const SymbolTable no_symbols;
+  // compile and plan the programs that were not cached (on the host's cores
+  // outside inner-product batches; the first error in program order raises)
+  std::vector<std::exception_ptr> compile_errs(parsed.size());
+  if (!inner) {
+    parallel_for(parsed.size(), [&](size_t pid) {
+      if (cached[pid]) return;
+      try {
+        compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
+        plan_program(&compiled[pid], job, fuse_for(compiled[pid].n, fuse));
+      } catch (...) {
+        compile_errs[pid] = std::current_exception();
+      }
+    });
+    rethrow_first(compile_errs);
+  }
   for (size_t pid = 0; pid < parsed.size(); ++pid) {
     if (inner && pair_of[pid] >= 0) continue;
     if (cached[pid]) {
-      compiled[pid] = cached[pid]->cp;
+      if (inner) compiled[pid] = cached[pid]->cp;
       continue;
     }
-    compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
-    plan_program(&compiled[pid], job, fuse_for(compiled[pid].n, fuse));
+    if (inner) {
+      compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
+      plan_program(&compiled[pid], job, fuse_for(compiled[pid].n, fuse));
+    }
     if (!inner) {
       auto e = std::make_shared<ProgramCacheEntry>();
       e->bytes.assign(src[pid].p, src[pid].n);

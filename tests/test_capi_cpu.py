@@ -202,3 +202,27 @@ def test_max_num_qubits_of_symbolic_programs_without_a_gpu():
     assert f(pp, pl, 3, ctypes.byref(mq)) == 0 and mq.value == 9
     bad, bl, keep2 = _native.string_array([b"\x0a\x05garbage"])
     assert f(bad, bl, 1, ctypes.byref(mq)) == 3
+
+
+def test_parallel_parse_reports_the_first_error_in_row_order():
+    """Distinct programs are decoded, resolved and compiled on the host's
+    cores; the error raised is still the one a row-order loop meets first."""
+    import pytest
+    from quantum_gb300 import _native, ops
+    from quantum_gb300 import serialize as S
+    progs = []
+    for i in range(64):
+        q = S.GridQubit.rect(1, 2 + i % 5)
+        progs.append(S.serialize_circuit(S.Circuit([[S.rx(q[0], 0.1 * (i + 1))],
+                                                    [S.CNOT(q[0], q[1])]])))
+    bad = list(progs)
+    bad[50] = b"not a proto A"
+    bad[20] = b"not a proto B"
+    with pytest.raises(_native.InvalidArgumentError, match="not a proto B"):
+        ops.Batch(bad, [], None)
+    bad = list(progs)
+    q = S.GridQubit.rect(1, 2)
+    bad[45] = S.serialize_circuit(S.Circuit([[S.rx(q[0], S.Symbol("late"))]]))
+    bad[30] = S.serialize_circuit(S.Circuit([[S.rx(q[1], S.Symbol("early"))]]))
+    with pytest.raises(_native.InvalidArgumentError, match="early"):
+        ops.Batch(bad, ["x"], None)
