@@ -553,7 +553,6 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       try {
         if (cached[pid]) {
           index[pid] = cached[pid]->index;
-          compiled[pid] = cached[pid]->cp;
         } else {
           resolve_qubits(parsed[pid], &index[pid]);
         }
@@ -606,10 +605,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   }
   for (size_t pid = 0; pid < parsed.size(); ++pid) {
     if (inner && pair_of[pid] >= 0) continue;
-    if (cached[pid]) {
-      if (inner) compiled[pid] = cached[pid]->cp;
-      continue;
-    }
+    if (cached[pid]) continue;
     if (inner) {
       compile_program(parsed[pid], names, job, &compiled[pid], &index[pid]);
       plan_program(&compiled[pid], job, fuse_for(compiled[pid].n, fuse));
@@ -638,9 +634,10 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   }
 
   // 5. pack programs
+  // (a cached program is packed straight from its cache entry)
   b->programs.resize(compiled.size());
   for (size_t pid = 0; pid < compiled.size(); ++pid) {
-    const CompiledProgram& cp = compiled[pid];
+    const CompiledProgram& cp = cached[pid] ? cached[pid]->cp : compiled[pid];
     DevProgram& dp = b->programs[pid];
     memset(&dp, 0, sizeof(dp));
     dp.n = cp.empty() ? 0 : cp.n;
@@ -1943,14 +1940,23 @@ int tfqg_max_num_qubits(const char* const* programs, const int64_t* program_lens
     if (batch < 0 || (batch > 0 && (!programs || !program_lens)))
       throw Error(kInvalidArgument, "NULL programs");
     // decode and resolve qubits only: symbols are bound later, as in
-    // GetProgramsAndNumQubits (parse_context.cc:268-320)
+    // GetProgramsAndNumQubits (parse_context.cc:268-320); on the host's
+    // cores, the first error in row order raised
+    std::vector<int> nq(size_t(batch), 0);
+    std::vector<std::exception_ptr> errs(static_cast<size_t>(batch));
+    parallel_for(size_t(batch), [&](size_t i) {
+      try {
+        ProgramP p;
+        decode_program(programs[i], size_t(program_lens[i]), &p);
+        std::unordered_map<std::string, int> index;
+        nq[i] = resolve_qubits(p, &index);
+      } catch (...) {
+        errs[i] = std::current_exception();
+      }
+    });
+    rethrow_first(errs);
     int mx = 0;
-    for (int64_t i = 0; i < batch; ++i) {
-      ProgramP p;
-      decode_program(programs[i], size_t(program_lens[i]), &p);
-      std::unordered_map<std::string, int> index;
-      mx = std::max(mx, resolve_qubits(p, &index));
-    }
+    for (const int n : nq) mx = std::max(mx, n);
     *max_num_qubits = mx;
     return 0;
   });
