@@ -238,6 +238,22 @@ def tc_apply(psi_ptr, n, u_ptr, targets, status_ptr, stream=0, grid=0):
         raise RuntimeError(f"tc_apply launch failed: cudaError {rc}")
 
 
+def tc_sweep(psi_ptr, n, u0_ptr, u1_ptr, targets0, targets1, status_ptr, stream=0, grid=0):
+    """One two-block tensor-core sweep on device buffers: psi (2^n complex64)
+    <- U1 (targets1) U0 (targets0), 32 x 32 complex64 row-major each;
+    status (device int32) is set to 1 on a timed-out wait.  Raises on a
+    launch error (including blocks that cannot share a sweep)."""
+    f = lib().tfqg_internal_tc_sweep
+    f.argtypes = [c_void_p, ctypes.c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                  ctypes.c_int, c_void_p]
+    f.restype = ctypes.c_int
+    t0 = (ctypes.c_int32 * 5)(*[int(t) for t in targets0])
+    t1 = (ctypes.c_int32 * 5)(*[int(t) for t in targets1])
+    rc = f(psi_ptr, int(n), u0_ptr, u1_ptr, t0, t1, status_ptr, int(grid), stream)
+    if rc != 0:
+        raise RuntimeError(f"tc_sweep launch failed: cudaError {rc}")
+
+
 def tc_grid():
     """CTAs of a tensor-core block launch on the current device."""
     f = lib().tfqg_internal_tc_grid

@@ -2194,6 +2194,51 @@ int tfqg_internal_tc_geometry(int n, const int32_t* tgt, uint64_t* cb, uint32_t*
   return 1;
 }
 
+// Geometry of a two-block sweep for targets tgt0 / tgt1 (5 each, ascending)
+// on an n-qubit state: 1 and its tables (host only; lets tests check the
+// sweep kernel's index arithmetic), or 0 when the blocks cannot share one.
+// out[0..8]: cb (low 32 bits), cb (high 32 bits), cb12, smask, tpos0, tpos1,
+// rpos0, rpos1, hmask; out[9]: r0.
+int tfqg_internal_tc_sweep_geometry(int n, const int32_t* tgt0, const int32_t* tgt1,
+                                    uint32_t* out) {
+  TcBlock b0{}, b1{};
+  for (int i = 0; i < kTcBits; ++i) {
+    b0.tgt[i] = uint8_t(tgt0[i]);
+    b1.tgt[i] = uint8_t(tgt1[i]);
+  }
+  TcSweep g{};
+  if (!tc_sweep_geometry(b0, b1, n, &g)) return 0;
+  const uint32_t v[10] = {uint32_t(g.cb), uint32_t(g.cb >> 32), g.cb12, g.smask, g.tpos[0],
+                          g.tpos[1], g.rpos[0], g.rpos[1], g.hmask, g.r0};
+  for (int i = 0; i < 10; ++i) out[i] = v[i];
+  return 1;
+}
+
+// One two-block sweep (U0 on tgt0, then U1 on tgt1) on a device state psi
+// of 2^n complex64 amplitudes; grid <= 0 picks one CTA per SM.  Returns a
+// cudaError_t (cudaErrorInvalidValue when the blocks cannot share a sweep).
+int tfqg_internal_tc_sweep(void* psi, int n, const void* U0, const void* U1,
+                           const int32_t* tgt0, const int32_t* tgt1, int* status, int grid,
+                           void* stream) {
+  TcBlock b0{}, b1{};
+  for (int i = 0; i < kTcBits; ++i) {
+    if (tgt0[i] < 0 || tgt0[i] > 31 || tgt1[i] < 0 || tgt1[i] > 31)
+      return int(cudaErrorInvalidValue);
+    b0.tgt[i] = uint8_t(tgt0[i]);
+    b1.tgt[i] = uint8_t(tgt1[i]);
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return int(e);
+  if (grid <= 0) {
+    e = cudaDeviceGetAttribute(&grid, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return int(e);
+  }
+  return int(launch_tc_sweep2(static_cast<float2*>(psi), n, static_cast<const float2*>(U0),
+                              static_cast<const float2*>(U1), b0, b1, status, grid,
+                              static_cast<cudaStream_t>(stream)));
+}
+
 // Makes the next calls treat the tensor-core status word as `status`
 // (0 restores the real read-back); returns the previous setting.
 int tfqg_internal_tc_inject_status(int status) { return g_tc_status_injected.exchange(status); }

@@ -234,6 +234,34 @@ struct TcTrans {
   uint32_t c;
 };
 bool tc_transposed_geometry(const TcBlock& blk, int n, TcTrans* out);
+// Two blocks in one sweep over the state (tc_sweep_kernel): tiles of 13
+// index bits -- bits 0-2, both blocks' targets and the lowest free bits --
+// staged through shared memory by bulk copies (cp.async.bulk, the TMA
+// engine) and written back the same way, with both blocks applied to each
+// tile on the tensor cores (A operands in tensor memory).  The geometry:
+// the physical bit of every tile position (cb, 5 bits each, positions 0-11;
+// cb12 position 12), the tile bits as a mask, per block its target and row
+// positions (4 bits each), the staging swizzle (tile positions whose parity
+// flips 8-byte slot bit 3) and the length r0 of the tile's lowest run of
+// consecutive bits.  False when the blocks cannot share a sweep (a target
+// below bit 4, or more than 13 tile bits).
+struct TcSweep {
+  uint64_t cb;
+  uint32_t cb12;
+  uint32_t smask;
+  uint32_t tpos[2];
+  uint32_t rpos[2];
+  uint32_t hmask;
+  uint32_t r0;
+};
+bool tc_sweep_geometry(const TcBlock& b0, const TcBlock& b1, int n, TcSweep* out);
+size_t tc_sweep_smem_bytes();
+const void* tc_sweep_kernel_ptr();
+// Applies U0 (block b0) then U1 (block b1) to the 2^n state in one sweep;
+// `grid` CTAs (one per SM); *status set to 1 on a timed-out wait.
+cudaError_t launch_tc_sweep2(float2* psi, int n, const float2* U0, const float2* U1,
+                             const TcBlock& b0, const TcBlock& b1, int* status, int grid,
+                             cudaStream_t s);
 // p[i] = (i == 0 ? first : rest) for i in [0, count).
 cudaError_t launch_fill(float2* p, int64_t count, float2 first, float2 rest, int grid,
                         cudaStream_t s);

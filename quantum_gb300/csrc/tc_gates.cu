@@ -399,6 +399,307 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
                  : "memory");
 }
 
+// ---- two blocks per sweep ------------------------------------------------------
+// tc_sweep_kernel: 256 threads, one CTA per SM, tiles taken grid-strided.
+// Per tile: bulk copies (cp.async.bulk, completing on an mbarrier) bring the
+// tile's runs of 2^r0 contiguous amplitudes into one of two 64 KiB staging
+// buffers while the other buffer's tile is processed; then for each block
+// every thread gathers its group's 32 amplitudes from the tile, splits them
+// into tf32 hi / lo and stores them into tensor memory (A operands of its
+// 128-row chunk: warps 0-3 chunk 0, warps 4-7 chunk 1), one thread issues
+// the 2 x 24 MMAs (A from TMEM, B from shared memory), and every thread
+// writes its group's results back into the tile; finally bulk copies write
+// the tile back.  TMEM: per chunk A_hi, A_lo and D, 64 columns each.
+constexpr int kSwThreads = 256;
+constexpr int kSwTileBits = 13;
+constexpr size_t kSwTileBytes = size_t(8) << kSwTileBits;             // 64 KiB
+constexpr size_t kSwBBytes = 2 * kTcBbytes;                           // hi + lo
+constexpr size_t kSwSmem = 2 * kSwTileBytes + 2 * kSwBBytes + 64;
+constexpr uint32_t kSwTmemCols = 512;
+constexpr uint32_t kSwChunkCols = 192;
+
+__device__ __forceinline__ int sw_cb(const TcSweep& g, int p) {
+  return p < 12 ? int((g.cb >> (5 * p)) & 31u) : int(g.cb12);
+}
+
+// physical offset of the tile positions set in L
+__device__ __forceinline__ int64_t sw_dep(const TcSweep& g, uint32_t L) {
+  int64_t o = 0;
+#pragma unroll
+  for (int p = 0; p < kSwTileBits; ++p)
+    if ((L >> p) & 1u) o |= int64_t(1) << sw_cb(g, p);
+  return o;
+}
+
+// staging slot of tile position L (an 8-byte slot; bit 3 flipped by the
+// parity of L's bits in hmask)
+__device__ __forceinline__ uint32_t sw_slot(const TcSweep& g, uint32_t L) {
+  return L ^ ((uint32_t(__popc(L & g.hmask)) & 1u) << 3);
+}
+
+__device__ __forceinline__ uint32_t sw_deposit(uint32_t v, uint32_t pos, int bits) {
+  uint32_t L = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    if (i < bits && ((v >> i) & 1u)) L |= 1u << ((pos >> (4 * i)) & 15u);
+  return L;
+}
+
+// the index bits outside the tile receive tile index t (ascending)
+__device__ __forceinline__ int64_t sw_tile_base(uint32_t smask, int n, int64_t t) {
+  int64_t o = 0;
+  int k = 0;
+  for (int b = 0; b < n; ++b)
+    if (!((smask >> b) & 1u)) {
+      if ((t >> k) & 1) o |= int64_t(1) << b;
+      ++k;
+    }
+  return o;
+}
+
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, "
+      "%10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, "
+      "%26, %27, %28, %29, %30, %31, %32};\n" ::"r"(taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+      "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+      "r"(v[15]), "r"(v[16]), "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]),
+      "r"(v[22]), "r"(v[23]), "r"(v[24]), "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]),
+      "r"(v[29]), "r"(v[30]), "r"(v[31])
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kSwThreads, 1)
+tc_sweep_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U0,
+                const float2* __restrict__ U1, TcSweep g, int* status) {
+  extern __shared__ __align__(1024) unsigned char sw_smem[];
+  float2* tiles = reinterpret_cast<float2*>(sw_smem);
+  float* bsm = reinterpret_cast<float*>(sw_smem + 2 * kSwTileBytes);
+  uint64_t* lbar = reinterpret_cast<uint64_t*>(sw_smem + 2 * kSwTileBytes + 2 * kSwBBytes);
+  uint64_t* mbar = lbar + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(lbar + 3);
+  int* timed_out = reinterpret_cast<int*>(lbar + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int chunk = warp >> 2;
+  const uint32_t lane_field = uint32_t((warp & 3) * 32) << 16;
+
+  // B operands of both blocks: R in real form, split into tf32 hi and lo
+  for (int b = 0; b < 2; ++b) {
+    const float2* U = b ? U1 : U0;
+    float* bh = bsm + b * (kSwBBytes / 4);
+    float* bl = bh + kTcBbytes / 4;
+    for (int idx = tid; idx < kTcNdim * kTcKdim; idx += blockDim.x) {
+      const int nr = idx / kTcKdim, k = idx % kTcKdim;
+      const float2 u = U[(nr >> 1) * 32 + (k >> 1)];
+      const float v = (nr & 1) ? ((k & 1) ? u.x : u.y) : ((k & 1) ? -u.y : u.x);
+      const float hi = tf32_hi(v);
+      const uint32_t o = kmaj(nr, k) >> 2;
+      bh[o] = hi;
+      bl[o] = v - hi;
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  if (tid == 0) {
+    *timed_out = 0;
+    for (int i = 0; i < 2; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(lbar + i)),
+                   "r"(kSwThreads)
+                   : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kSwTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  const int64_t ntiles = int64_t(1) << (n - kSwTileBits);
+  const int r0 = int(g.r0);
+  const int runs = 1 << (kSwTileBits - r0);
+  const uint32_t run_bytes = 8u << r0;
+
+  auto issue_load = [&](int64_t t, int buf) {
+    const int64_t base = sw_tile_base(g.smask, n, t);
+    uint32_t mine = 0;
+    for (int q = tid; q < runs; q += kSwThreads) mine += run_bytes;
+    const uint32_t bar = smem_u32(lbar + buf);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                 "r"(mine)
+                 : "memory");
+    float2* tile = tiles + (size_t(buf) << kSwTileBits);
+    for (int q = tid; q < runs; q += kSwThreads) {
+      const uint32_t L0 = uint32_t(q) << r0;
+      const float2* src = psi + base + sw_dep(g, L0);
+      const uint32_t dst = smem_u32(tile + sw_slot(g, L0));
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+          "[%3];\n" ::"r"(dst),
+          "l"(src), "r"(run_bytes), "r"(bar)
+          : "memory");
+    }
+  };
+  auto issue_store = [&](int64_t t, int buf) {
+    const int64_t base = sw_tile_base(g.smask, n, t);
+    const float2* tile = tiles + (size_t(buf) << kSwTileBits);
+    for (int q = tid; q < runs; q += kSwThreads) {
+      const uint32_t L0 = uint32_t(q) << r0;
+      float2* dst = psi + base + sw_dep(g, L0);
+      const uint32_t src = smem_u32(tile + sw_slot(g, L0));
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst),
+                   "r"(src), "r"(run_bytes)
+                   : "memory");
+    }
+    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+  };
+
+  uint32_t lpar[2] = {0u, 0u}, mpar = 0u;
+  bool failed = false, load_pending[2] = {false, false};
+  int64_t t = blockIdx.x;
+  if (t < ntiles) {
+    issue_load(t, 0);
+    load_pending[0] = true;
+  }
+  for (int k = 0; t < ntiles && !failed; t += gridDim.x, ++k) {
+    const int buf = k & 1;
+    const int64_t next = t + gridDim.x;
+    if (next < ntiles) {
+      // the other buffer's store (tile k - 1) must have read shared memory
+      asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+      __syncthreads();
+      issue_load(next, buf ^ 1);
+      load_pending[buf ^ 1] = true;
+    }
+    {
+      bool done = false;
+      for (uint32_t it = 0; it < kTcSpin && !done; ++it)
+        done = mbar_try_wait(smem_u32(lbar + buf), lpar[buf]);
+      if (!done) atomicExch(timed_out, 1);
+      else load_pending[buf] = false;
+      lpar[buf] ^= 1u;
+    }
+    __syncthreads();
+    if (*timed_out) {
+      failed = true;
+      break;
+    }
+    float2* tile = tiles + (size_t(buf) << kSwTileBits);
+    for (int b = 0; b < 2 && !failed; ++b) {
+      const uint32_t grp = uint32_t(chunk * 128 + (warp & 3) * 32 + lane);
+      const uint32_t Lr = sw_deposit(grp, g.rpos[b], 8);
+      uint32_t Lj[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) Lj[j] = Lr | sw_deposit(uint32_t(j), g.tpos[b], 5);
+      // A operands of this thread's row: amplitudes 16 h .. 16 h + 15
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        uint32_t hi[32], lo[32];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const float2 v = tile[sw_slot(g, Lj[16 * h + i])];
+          const float hx = tf32_hi(v.x), hy = tf32_hi(v.y);
+          hi[2 * i] = __float_as_uint(hx);
+          hi[2 * i + 1] = __float_as_uint(hy);
+          lo[2 * i] = __float_as_uint(v.x - hx);
+          lo[2 * i + 1] = __float_as_uint(v.y - hy);
+        }
+        const uint32_t col = uint32_t(chunk) * kSwChunkCols + 32u * uint32_t(h);
+        tmem_st32(tmem + lane_field + col, hi);
+        tmem_st32(tmem + lane_field + col + 64u, lo);
+      }
+      asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      if (tid == 0) {
+        const uint32_t idesc = idesc_tf32(kTcRows, kTcNdim);
+        const float* bh = bsm + b * (kSwBBytes / 4);
+        const uint32_t bhi = smem_u32(bh), blo = smem_u32(bh + kTcBbytes / 4);
+        for (int c = 0; c < 2; ++c) {
+          const uint32_t a_hi = tmem + uint32_t(c) * kSwChunkCols;
+          const uint32_t a_lo = a_hi + 64u, d = a_hi + 128u;
+          const uint32_t as[3] = {a_lo, a_hi, a_hi}, bs[3] = {bhi, blo, bhi};
+          uint32_t acc = 0;
+          for (int pr = 0; pr < 3; ++pr)
+            for (int st = 0; st < kTcKdim / 8; ++st) {
+              const uint64_t bd = smem_desc(bs[pr] + uint32_t(st) * 256u, 128u, kTcSbo);
+              asm volatile(
+                  "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                  " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+                  "r"(as[pr] + uint32_t(8 * st)), "l"(bd), "r"(idesc), "r"(acc)
+                  : "memory");
+              acc = 1;
+            }
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                smem_u32(mbar))
+            : "memory");
+      }
+      bool done = false;
+      for (uint32_t it = 0; it < kTcSpin && !done; ++it)
+        done = mbar_try_wait(smem_u32(mbar), mpar);
+      if (!done) atomicExch(timed_out, 1);
+      mpar ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      __syncthreads();
+      if (*timed_out) {
+        failed = true;
+        break;
+      }
+      {
+        uint32_t dv[64];
+        const uint32_t taddr = tmem + lane_field + uint32_t(chunk) * kSwChunkCols + 128u;
+        tmem_ld16(taddr, dv);
+        tmem_ld16(taddr + 16u, dv + 16);
+        tmem_ld16(taddr + 32u, dv + 32);
+        tmem_ld16(taddr + 48u, dv + 48);
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          tile[sw_slot(g, Lj[j])] =
+              make_float2(__uint_as_float(dv[2 * j]), __uint_as_float(dv[2 * j + 1]));
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    }
+    if (failed) break;
+    // the tile's generic-proxy writes are read by the bulk copies
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    issue_store(t, buf);
+  }
+  // every bulk store has completed; a prefetched load still in flight after
+  // a failure is waited for (bounded) before the CTA's shared memory goes
+  asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+  if (failed) {
+    for (int b = 0; b < 2; ++b)
+      if (load_pending[b]) {
+        bool done = false;
+        for (uint32_t it = 0; it < kTcSpin && !done; ++it)
+          done = mbar_try_wait(smem_u32(lbar + b), lpar[b]);
+      }
+    bool done = false;
+    for (uint32_t it = 0; it < kTcSpin && !done; ++it)
+      done = mbar_try_wait(smem_u32(mbar), mpar ^ 1u);
+    if (tid == 0) atomicExch(status, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                 "r"(kSwTmemCols)
+                 : "memory");
+}
+
 }  // namespace
 
 const void* tc_apply5_kernel_ptr() {
@@ -488,6 +789,78 @@ cudaError_t launch_tc_apply5(float2* psi, int n, const float2* U, const TcBlock&
     tc_apply5_kernel<true><<<grid, kTcRows, kTcSmem, s>>>(psi, n, U, tpack, tr, status);
   else
     tc_apply5_kernel<false><<<grid, kTcRows, kTcSmem, s>>>(psi, n, U, tpack, tr, status);
+  return cudaGetLastError();
+}
+
+bool tc_sweep_geometry(const TcBlock& b0, const TcBlock& b1, int n, TcSweep* out) {
+  if (n < kSwTileBits + 1 || n > 31) return false;
+  const TcBlock* bl[2] = {&b0, &b1};
+  uint32_t smask = 0x7u;  // bits 0-2
+  for (int b = 0; b < 2; ++b)
+    for (int i = 0; i < kTcBits; ++i) {
+      if (bl[b]->tgt[i] < 4 || bl[b]->tgt[i] >= n) return false;
+      smask |= 1u << bl[b]->tgt[i];
+    }
+  if (__builtin_popcount(smask) > kSwTileBits) return false;
+  for (int bit = 3; bit < n && __builtin_popcount(smask) < kSwTileBits; ++bit)
+    smask |= 1u << bit;
+  if (__builtin_popcount(smask) != kSwTileBits) return false;
+  TcSweep g{};
+  g.smask = smask;
+  int cb[kSwTileBits], np = 0;
+  for (int bit = 0; bit < n; ++bit)
+    if ((smask >> bit) & 1u) cb[np++] = bit;
+  for (int p = 0; p < 12; ++p) g.cb |= uint64_t(cb[p]) << (5 * p);
+  g.cb12 = uint32_t(cb[12]);
+  int r0 = 0;
+  while (r0 < kSwTileBits && cb[r0] == r0) ++r0;
+  g.r0 = uint32_t(r0);
+  for (int b = 0; b < 2; ++b) {
+    int ti = 0, ri = 0;
+    for (int p = 0; p < kSwTileBits; ++p) {
+      bool is_t = false;
+      for (int i = 0; i < kTcBits; ++i) is_t = is_t || bl[b]->tgt[i] == cb[p];
+      if (is_t) g.tpos[b] |= uint32_t(p) << (4 * ti++);
+      else g.rpos[b] |= uint32_t(p) << (4 * ri++);
+    }
+    if (ti != kTcBits || ri != 8) return false;
+  }
+  // swizzle: a warp's lanes are a block's 5 lowest row positions; slot bits
+  // 0-2 are positions 0-2 (never targets); where position 3 is one of the
+  // block's targets, one of its lane positions >= 4 must flip slot bit 3
+  for (int b = 0; b < 2; ++b) {
+    bool pos3_lane = false;
+    uint32_t lanes_hi = 0;
+    for (int i = 0; i < 5; ++i) {
+      const int p = int((g.rpos[b] >> (4 * i)) & 15u);
+      if (p == 3) pos3_lane = true;
+      if (p >= 4) lanes_hi |= 1u << p;
+    }
+    if (pos3_lane || (g.hmask & lanes_hi)) continue;
+    g.hmask |= lanes_hi & (~lanes_hi + 1u);  // its lowest lane position >= 4
+  }
+  // a flipped slot bit 3 must not split a run of contiguous amplitudes
+  if (g.hmask && r0 > 3) return false;
+  *out = g;
+  return true;
+}
+
+size_t tc_sweep_smem_bytes() { return kSwSmem; }
+const void* tc_sweep_kernel_ptr() { return reinterpret_cast<const void*>(&tc_sweep_kernel); }
+
+cudaError_t launch_tc_sweep2(float2* psi, int n, const float2* U0, const float2* U1,
+                             const TcBlock& b0, const TcBlock& b1, int* status, int grid,
+                             cudaStream_t s) {
+  TcSweep g{};
+  if (!tc_sweep_geometry(b0, b1, n, &g)) return cudaErrorInvalidValue;
+  const int64_t ntiles = int64_t(1) << (n - kSwTileBits);
+  if (grid > ntiles) grid = int(ntiles);
+  if (grid < 1) grid = 1;
+  cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(&tc_sweep_kernel),
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(kSwSmem));
+  if (e != cudaSuccess) return e;
+  tc_sweep_kernel<<<grid, kSwThreads, kSwSmem, s>>>(psi, n, U0, U1, g, status);
   return cudaGetLastError();
 }
 
