@@ -248,11 +248,13 @@ def config_roofline(wl, w, batch, ms, clk, units):
         from quantum_gb300 import _native
         fwd, meas = _native.row_sweeps(batch._h, 0)
         blocks = _native.tc_blocks(batch._h, 0)
+        sweeps = _native.tc_sweeps(batch._h, 0)
         if blocks > 0:
-            # tensor-core blocks: one read+write sweep each, plus the |0> fill
-            nbytes = (blocks * 16 + 8 + meas * 8) * 2 ** n
-            how = (f"{blocks} tensor-core block sweeps x 16 B + |0> fill 8 B + {meas} "
-                   f"measurement pass(es) x 8 B, times 2^{n} amplitudes")
+            # tensor-core blocks: one read+write sweep per launch (one block,
+            # or two sharing a sweep), plus the |0> fill
+            nbytes = (sweeps * 16 + 8 + meas * 8) * 2 ** n
+            how = (f"{sweeps} tensor-core sweeps ({blocks} blocks) x 16 B + |0> fill 8 B + "
+                   f"{meas} measurement pass(es) x 8 B, times 2^{n} amplitudes")
         else:
             nbytes = (fwd * 16 + meas * 8) * 2 ** n
             how = (f"{fwd} forward passes x 16 B + {meas} measurement "
@@ -348,6 +350,60 @@ def tc_kernel_roofline(n, batch, dev, launches=3):
             "peak_source": src}
 
 
+def tc_sweep_roofline(n, batch, dev, launches=3):
+    """The two-block sweep kernel alone on a 2^n complex64 state (> L2), on
+    the consecutive block pairs of the row's plan that share a sweep: random
+    5-qubit unitaries, one warm-up and `launches` timed launches per pair.
+    Algorithmic bytes per launch: 16 B per amplitude (one read and one write
+    of the state for two blocks)."""
+    import torch
+    from quantum_gb300 import _native
+    plan = [tuple(int(t) for t in p[0])
+            for p in _native.tc_plan(batch._h, 0, np.zeros(0, np.float32))]
+    pairs, i = [], 0
+    while i + 1 < len(plan):
+        if min(plan[i]) >= 4 and min(plan[i + 1]) >= 4:
+            pairs.append((plan[i], plan[i + 1]))
+            i += 2
+        else:
+            i += 1
+    if not pairs:
+        return None
+    rng = np.random.default_rng(1)
+    us = []
+    for _ in range(2):
+        z = rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))
+        q, _ = np.linalg.qr(z)
+        us.append(torch.tensor(q.astype(np.complex64), device=dev))
+    psi = torch.zeros(2 ** n, dtype=torch.complex64, device=dev)
+    psi[0] = 1
+    st = torch.zeros(1, dtype=torch.int32, device=dev)
+    s = torch.cuda.current_stream()
+    times = []
+    for t0, t1 in pairs:
+        args = (psi.data_ptr(), n, us[0].data_ptr(), us[1].data_ptr(), t0, t1, st.data_ptr(),
+                s.cuda_stream)
+        _native.tc_sweep(*args)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(launches):
+            _native.tc_sweep(*args)
+        b.record(s)
+        s.synchronize()
+        times.append(a.elapsed_time(b) / launches)
+    peak, src = _hbm_peak()
+    gbs = lambda ms: 16 * 2 ** n / (ms / 1e3) / 1e9
+    mean_ms = float(np.mean(times))
+    ok = int(st.item()) == 0
+    del psi
+    return {"bound": "hbm", "kernel": "tc_sweep_kernel (2 blocks per sweep)",
+            "pairs": len(pairs), "ms_per_launch": mean_ms, "achieved": gbs(mean_ms),
+            "peak": peak, "unit": "GB/s", "frac": gbs(mean_ms) / peak,
+            "slowest_frac": gbs(max(times)) / peak, "status_ok": ok,
+            "algorithmic": f"16 B x 2^{n} amplitudes per launch (two blocks, one sweep)",
+            "peak_source": src}
+
+
 def c4_summary(dev, steps=3, warmup=2, grid="5x6"):
     """The 30-qubit grid circuit (C4) for the default line: device time of
     one expectation call (tensor-core blocks, the library default at this
@@ -379,7 +435,10 @@ def c4_summary(dev, steps=3, warmup=2, grid="5x6"):
             "sum_z": float(out.cpu().numpy()[0, 0]),
             "roofline": config_roofline("c4", w, b, ms, clk, 1)}
     if _native.tc_blocks(b._h, 0) > 0:
+        line["tensor_core_blocks"] = _native.tc_blocks(b._h, 0)
+        line["tensor_core_sweeps"] = _native.tc_sweeps(b._h, 0)
         line["tc_block_kernel"] = tc_kernel_roofline(w["n"], b, dev)
+        line["tc_sweep_kernel"] = tc_sweep_roofline(w["n"], b, dev)
     b.close()
     return line
 
@@ -508,7 +567,9 @@ def run_config(args):
     tc = wl == "c4" and __import__("quantum_gb300")._native.tc_blocks(batch._h, 0) > 0
     if tc:
         line["tensor_core_blocks"] = __import__("quantum_gb300")._native.tc_blocks(batch._h, 0)
+        line["tensor_core_sweeps"] = __import__("quantum_gb300")._native.tc_sweeps(batch._h, 0)
         line["tc_block_kernel"] = tc_kernel_roofline(w["n"], batch, dev)
+        line["tc_sweep_kernel"] = tc_sweep_roofline(w["n"], batch, dev)
         line["config"]["tensor_cores"] = "5-qubit blocks, split 3xTF32 (tcgen05 kind::tf32)"
     if wl == "c4":
         # a 30-qubit complex128 oracle run is out of reach: the fused plan is

@@ -271,6 +271,25 @@ def tc_blocks(handle, k):
     return int(f(handle, int(k)))
 
 
+def tc_sweeps(handle, k):
+    """State sweeps (kernel launches) of the tensor-core blocks of the k-th
+    wide row in its last forward call (-1: it ran tile passes)."""
+    f = lib().tfqg_internal_tc_sweeps
+    f.argtypes = [c_void_p, ctypes.c_int64]
+    f.restype = ctypes.c_int
+    return int(f(handle, int(k)))
+
+
+def set_tc_sweep(on):
+    """Two consecutive tensor-core blocks share one state sweep where their
+    targets allow it (True, the default) or every block sweeps alone, for
+    calls made from now on; returns the previous setting."""
+    f = lib().tfqg_internal_set_tc_sweep
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return bool(f(1 if on else 0))
+
+
 def tc_status(handle):
     """Status word of the batch's tensor-core kernels: 0, or 1 when an MMA
     completion wait timed out (synchronizes the device)."""

@@ -139,6 +139,7 @@ struct tfqg_batch {
   std::vector<int32_t> tc_members;
   std::vector<std::pair<int32_t, int32_t>> tc_rows;  // parallel to wide_rows
   std::vector<uint8_t> tc_ran;  // the row's last forward call ran the blocks
+  std::vector<int32_t> tc_sweeps;  // state sweeps (launches) of that call
   tfqg::DevBuf tc_tab, tc_mats, tc_status;
   // gives every device buffer back to the pool (the device is synchronized)
   void release_buffers() noexcept {

@@ -180,6 +180,10 @@ constexpr int kTcAutoMinQubits = 24;
 // kernels of the next calls (0: read the real one).  It lets a test take
 // the timeout branch without a timeout on the GPU.
 std::atomic<int> g_tc_status_injected{0};
+// Two consecutive blocks share one state sweep (tc_sweep_kernel) where
+// their targets allow it (1, the default), or every block has its own
+// sweep (0).
+std::atomic<int> g_tc_sweep{1};
 
 }  // namespace
 
@@ -947,6 +951,7 @@ void tc_prepare(tfqg_batch* b, cudaStream_t s) {
     b->tc_rows.emplace_back(first, ok ? int32_t(b->tc_blocks.size()) - first : -1);
   }
   b->tc_ran.assign(b->wide_rows.size(), 0);
+  b->tc_sweeps.assign(b->wide_rows.size(), 0);
   const size_t bb = b->tc_blocks.size() * sizeof(TcBlock);
   const size_t mb = b->tc_members.size() * sizeof(int32_t);
   b->tc_tab.reserve(align256(bb) + mb + 256, b->device);
@@ -1014,10 +1019,24 @@ bool run_wide_tc(tfqg_batch* b, const BatchDevice& bd, const RunArgs* a, size_t 
   TFQG_CUDA(launch_fill(psi, int64_t(1) << n, make_float2(1.f, 0.f), make_float2(0.f, 0.f),
                         sms * 4, s));
   const int grid = tc_grid(b->device);
-  for (int i = 0; i < rp.second; ++i)
-    TFQG_CUDA(launch_tc_apply5(psi, n, U + int64_t(i) * 1024,
-                               b->tc_blocks[size_t(rp.first + i)],
-                               static_cast<int*>(b->tc_status.p), grid, s));
+  int* st = static_cast<int*>(b->tc_status.p);
+  const bool pair = g_tc_sweep.load() != 0;
+  int sweeps = 0;
+  for (int i = 0; i < rp.second; ++sweeps) {
+    const TcBlock& b0 = b->tc_blocks[size_t(rp.first + i)];
+    TcSweep geo;
+    if (pair && i + 1 < rp.second &&
+        tc_sweep_geometry(b0, b->tc_blocks[size_t(rp.first + i + 1)], n, &geo)) {
+      // two blocks in one sweep: one CTA per SM
+      TFQG_CUDA(launch_tc_sweep2(psi, n, U + int64_t(i) * 1024, U + int64_t(i + 1) * 1024, b0,
+                                 b->tc_blocks[size_t(rp.first + i + 1)], st, sms, s));
+      i += 2;
+    } else {
+      TFQG_CUDA(launch_tc_apply5(psi, n, U + int64_t(i) * 1024, b0, st, grid, s));
+      i += 1;
+    }
+  }
+  b->tc_sweeps[k] = sweeps;
   return true;
 }
 
@@ -2178,6 +2197,18 @@ int tfqg_internal_tc_blocks(void* batch, int64_t k) {
   if (!b || !b->tc_planned || k < 0 || k >= int64_t(b->tc_rows.size())) return -1;
   return b->tc_ran[size_t(k)] ? b->tc_rows[size_t(k)].second : -1;
 }
+
+// State sweeps (kernel launches) of the tensor-core blocks of the k-th wide
+// row in its last forward call (-1: it ran tile passes, or has not run).
+int tfqg_internal_tc_sweeps(void* batch, int64_t k) {
+  const tfqg_batch* b = static_cast<const tfqg_batch*>(batch);
+  if (!b || !b->tc_planned || k < 0 || k >= int64_t(b->tc_rows.size())) return -1;
+  return b->tc_ran[size_t(k)] ? b->tc_sweeps[size_t(k)] : -1;
+}
+
+// Two blocks per sweep where their targets allow it (1) or one (0), for
+// calls made from now on; returns the previous setting.
+int tfqg_internal_set_tc_sweep(int on) { return g_tc_sweep.exchange(on ? 1 : 0); }
 // Chunk geometry of the block kernel for targets tgt[0..4] (ascending) on an
 // n-qubit state: 1 and the transposed variant's tables, or 0 for the direct
 // variant (host only; lets tests check the kernel's index arithmetic).

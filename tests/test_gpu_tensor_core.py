@@ -159,3 +159,23 @@ def test_block_timeout_fails_the_call_and_is_not_sticky(tensor_core_wide):
     assert _native.tc_blocks(b._h, 0) > 0 and _native.tc_status(b._h) == 0
     np.testing.assert_allclose(got, O.simulate_expectation(programs, [], values, psums),
                                atol=expectation_atol(psums), rtol=0)
+
+
+def test_two_block_sweeps_match_single_block_sweeps(tensor_core_wide):
+    """A wide row whose consecutive blocks share sweeps (tc_sweep_kernel)
+    gives the state of one sweep per block, with fewer sweeps."""
+    w = workloads.grid_fsim(rows=4, cols=5, depth=12, seed=8)
+    values = np.zeros((1, 0), np.float32)
+    b = ops.Batch(w["programs"], [], None)
+    paired = b.state(values)
+    blocks, sweeps = _native.tc_blocks(b._h, 0), _native.tc_sweeps(b._h, 0)
+    assert blocks > 0 and 0 < sweeps < blocks and _native.tc_status(b._h) == 0
+    prev = _native.set_tc_sweep(False)
+    try:
+        single = b.state(values)
+        assert _native.tc_sweeps(b._h, 0) == blocks
+    finally:
+        _native.set_tc_sweep(prev)
+    np.testing.assert_allclose(paired, single, atol=1e-6, rtol=0)
+    np.testing.assert_allclose(paired, O.simulate_state(w["programs"], [], values),
+                               atol=1e-5, rtol=0)
