@@ -414,7 +414,10 @@ constexpr int kSwThreads = 256;
 constexpr int kSwTileBits = 13;
 constexpr size_t kSwTileBytes = size_t(8) << kSwTileBits;             // 64 KiB
 constexpr size_t kSwBBytes = 2 * kTcBbytes;                           // hi + lo
-constexpr size_t kSwSmem = 2 * kSwTileBytes + 2 * kSwBBytes + 64;
+// tables: tile bases (2 x 512 int64: low and high 9 bits of the tile index)
+// and both blocks' target slot offsets (2 x 32 uint32)
+constexpr size_t kSwTabBytes = 2 * 512 * 8 + 2 * 32 * 4;
+constexpr size_t kSwSmem = 2 * kSwTileBytes + 2 * kSwBBytes + kSwTabBytes + 64;
 constexpr uint32_t kSwTmemCols = 512;
 constexpr uint32_t kSwChunkCols = 192;
 
@@ -476,7 +479,11 @@ tc_sweep_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U0,
   extern __shared__ __align__(1024) unsigned char sw_smem[];
   float2* tiles = reinterpret_cast<float2*>(sw_smem);
   float* bsm = reinterpret_cast<float*>(sw_smem + 2 * kSwTileBytes);
-  uint64_t* lbar = reinterpret_cast<uint64_t*>(sw_smem + 2 * kSwTileBytes + 2 * kSwBBytes);
+  int64_t* base_lo = reinterpret_cast<int64_t*>(sw_smem + 2 * kSwTileBytes + 2 * kSwBBytes);
+  int64_t* base_hi = base_lo + 512;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(base_hi + 512);  // [block][j]
+  uint64_t* lbar =
+      reinterpret_cast<uint64_t*>(sw_smem + 2 * kSwTileBytes + 2 * kSwBBytes + kSwTabBytes);
   uint64_t* mbar = lbar + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(lbar + 3);
   int* timed_out = reinterpret_cast<int*>(lbar + 4);
@@ -499,6 +506,15 @@ tc_sweep_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U0,
       bl[o] = v - hi;
     }
   }
+  // tile bases: the tile index's low and high 9 bits deposited into the
+  // index bits outside the tile; target slot offsets of both blocks (the
+  // staging slot is XOR-linear in the tile position)
+  for (int i = tid; i < 1024; i += blockDim.x) {
+    const int half = i >> 9;
+    base_lo[i] = sw_tile_base(g.smask, n, int64_t(i & 511) << (9 * half));
+  }
+  for (int i = tid; i < 64; i += blockDim.x)
+    tslot[i] = sw_slot(g, sw_deposit(uint32_t(i & 31), g.tpos[i >> 5], 5));
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
   if (tid == 0) {
     *timed_out = 0;
@@ -526,19 +542,27 @@ tc_sweep_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U0,
   const int runs = 1 << (kSwTileBits - r0);
   const uint32_t run_bytes = 8u << r0;
 
+  // this thread's runs (at most 4): state offsets and staging slots
+  int64_t run_off[4];
+  uint32_t run_slot[4];
+  int my_runs = 0;
+  for (int q = tid; q < runs && my_runs < 4; q += kSwThreads, ++my_runs) {
+    const uint32_t L0 = uint32_t(q) << r0;
+    run_off[my_runs] = sw_dep(g, L0);
+    run_slot[my_runs] = sw_slot(g, L0);
+  }
+  auto tile_base = [&](int64_t t) { return base_lo[t & 511] | base_hi[(t >> 9) & 511]; };
   auto issue_load = [&](int64_t t, int buf) {
-    const int64_t base = sw_tile_base(g.smask, n, t);
-    uint32_t mine = 0;
-    for (int q = tid; q < runs; q += kSwThreads) mine += run_bytes;
+    const int64_t base = tile_base(t);
+    const uint32_t mine = uint32_t(my_runs) * run_bytes;
     const uint32_t bar = smem_u32(lbar + buf);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
                  "r"(mine)
                  : "memory");
     float2* tile = tiles + (size_t(buf) << kSwTileBits);
-    for (int q = tid; q < runs; q += kSwThreads) {
-      const uint32_t L0 = uint32_t(q) << r0;
-      const float2* src = psi + base + sw_dep(g, L0);
-      const uint32_t dst = smem_u32(tile + sw_slot(g, L0));
+    for (int i = 0; i < my_runs; ++i) {
+      const float2* src = psi + base + run_off[i];
+      const uint32_t dst = smem_u32(tile + run_slot[i]);
       asm volatile(
           "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
           "[%3];\n" ::"r"(dst),
@@ -547,12 +571,11 @@ tc_sweep_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U0,
     }
   };
   auto issue_store = [&](int64_t t, int buf) {
-    const int64_t base = sw_tile_base(g.smask, n, t);
+    const int64_t base = tile_base(t);
     const float2* tile = tiles + (size_t(buf) << kSwTileBits);
-    for (int q = tid; q < runs; q += kSwThreads) {
-      const uint32_t L0 = uint32_t(q) << r0;
-      float2* dst = psi + base + sw_dep(g, L0);
-      const uint32_t src = smem_u32(tile + sw_slot(g, L0));
+    for (int i = 0; i < my_runs; ++i) {
+      float2* dst = psi + base + run_off[i];
+      const uint32_t src = smem_u32(tile + run_slot[i]);
       asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst),
                    "r"(src), "r"(run_bytes)
                    : "memory");
@@ -560,6 +583,10 @@ tc_sweep_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U0,
     asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
   };
 
+  // this thread's group row slot in each block (constant over the tiles)
+  const uint32_t grp = uint32_t(chunk * 128 + (warp & 3) * 32 + lane);
+  const uint32_t srow0 = sw_slot(g, sw_deposit(grp, g.rpos[0], 8));
+  const uint32_t srow1 = sw_slot(g, sw_deposit(grp, g.rpos[1], 8));
   uint32_t lpar[2] = {0u, 0u}, mpar = 0u;
   bool failed = false, load_pending[2] = {false, false};
   int64_t t = blockIdx.x;
@@ -592,18 +619,15 @@ tc_sweep_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U0,
     }
     float2* tile = tiles + (size_t(buf) << kSwTileBits);
     for (int b = 0; b < 2 && !failed; ++b) {
-      const uint32_t grp = uint32_t(chunk * 128 + (warp & 3) * 32 + lane);
-      const uint32_t Lr = sw_deposit(grp, g.rpos[b], 8);
-      uint32_t Lj[32];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) Lj[j] = Lr | sw_deposit(uint32_t(j), g.tpos[b], 5);
+      const uint32_t sr = b ? srow1 : srow0;
+      const uint32_t* ts = tslot + 32 * b;
       // A operands of this thread's row: amplitudes 16 h .. 16 h + 15
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         uint32_t hi[32], lo[32];
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-          const float2 v = tile[sw_slot(g, Lj[16 * h + i])];
+          const float2 v = tile[sr ^ ts[16 * h + i]];
           const float hx = tf32_hi(v.x), hy = tf32_hi(v.y);
           hi[2 * i] = __float_as_uint(hx);
           hi[2 * i + 1] = __float_as_uint(hy);
@@ -664,7 +688,7 @@ tc_sweep_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U0,
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-          tile[sw_slot(g, Lj[j])] =
+          tile[sr ^ ts[j]] =
               make_float2(__uint_as_float(dv[2 * j]), __uint_as_float(dv[2 * j + 1]));
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
