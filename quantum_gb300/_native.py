@@ -282,8 +282,8 @@ def tc_sweeps(handle, k):
 
 def set_tc_sweep(on):
     """Two consecutive tensor-core blocks share one state sweep where their
-    targets allow it (True, the default) or every block sweeps alone, for
-    calls made from now on; returns the previous setting."""
+    targets allow it (True) or every block sweeps alone (False, the
+    default), for calls made from now on; returns the previous setting."""
     f = lib().tfqg_internal_set_tc_sweep
     f.argtypes = [ctypes.c_int]
     f.restype = ctypes.c_int

@@ -167,11 +167,12 @@ def test_two_block_sweeps_match_single_block_sweeps(tensor_core_wide):
     w = workloads.grid_fsim(rows=4, cols=5, depth=12, seed=8)
     values = np.zeros((1, 0), np.float32)
     b = ops.Batch(w["programs"], [], None)
-    paired = b.state(values)
-    blocks, sweeps = _native.tc_blocks(b._h, 0), _native.tc_sweeps(b._h, 0)
-    assert blocks > 0 and 0 < sweeps < blocks and _native.tc_status(b._h) == 0
-    prev = _native.set_tc_sweep(False)
+    prev = _native.set_tc_sweep(True)
     try:
+        paired = b.state(values)
+        blocks, sweeps = _native.tc_blocks(b._h, 0), _native.tc_sweeps(b._h, 0)
+        assert blocks > 0 and 0 < sweeps < blocks and _native.tc_status(b._h) == 0
+        _native.set_tc_sweep(False)
         single = b.state(values)
         assert _native.tc_sweeps(b._h, 0) == blocks
     finally:
