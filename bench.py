@@ -947,7 +947,12 @@ def main():
     achieved_tflops = adj_flop / (adj_mean_ms / 1e3) / 1e12
     tpc = profiled_traffic_per_circuit()
     traffic = tpc * BATCH if tpc else None
-    launches = 4  # per step: build matrices + simulate, for each of the two ops
+    # per step, for each of the two ops: the matrix build (a second launch
+    # builds the fused gates' products when the plan has any) and the
+    # persistent simulation kernel
+    fused = any(g[5] == 32 for g in _native.forward_plan_gates(
+        batch._h, 0, w["symbol_values"][0]))
+    launches = 2 * (2 + (1 if fused else 0))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
