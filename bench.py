@@ -476,11 +476,15 @@ def run_config(args):
         t0 = time.perf_counter()
         res = autotune.tune(w["programs"], w["pauli_sums"], samples=1000, use_cache=False)
         tuned = {"seconds": time.perf_counter() - t0,
-                 "per_qubit_count": {str(n): {"fusion_width": 2 if r["fuse"] else 1,
-                                              "schedule": ("lockstep" if r["lock"] == 1 else
-                                                           "queue" if r["lock"] == 0 else
-                                                           "default"),
-                                              "ms_sample": r["ms"], "rows_timed": r["rows"]}
+                 "per_qubit_count": {str(n): {"fusion_width": (5 if r["lock"] == 2 else
+                                                               2 if r["fuse"] else 1),
+                                              "schedule": ("lockstep" if r["lock"] in (1, 2)
+                                                           else "queue" if r["lock"] == 0
+                                                           else "default"),
+                                              "gates": ("tensor-core blocks" if r["lock"] == 2
+                                                        else "tile passes"),
+                                              "ms_sample": r["ms"], "rows_timed": r["rows"],
+                                              "candidates_ms": r["candidates"]}
                                      for n, r in res.items()}}
     t0 = time.perf_counter()
     batch = ops.Batch(w["programs"], w["symbol_names"], w["pauli_sums"], kind)
@@ -540,7 +544,9 @@ def run_config(args):
         graph = {"graph_launches_per_step": 2, "ms_per_step": ms,
                  "direct_calls_ms_per_step": direct_ms,
                  "lockstep_rows": __import__("quantum_gb300")._native.batch_lock_rows(
-                     batch._h)[0]}
+                     batch._h)[0],
+                 "lockstep_tensor_core_blocks": __import__(
+                     "quantum_gb300")._native.batch_lock_tc(batch._h)[0]}
         out = out.clone()
         ge.close()
         gs.close()

@@ -302,8 +302,10 @@ def tc_status(handle):
 def tc_inject_status(status):
     """Test hook: calls made from now on treat the tensor-core status word
     as `status` (nonzero: an MMA completion wait timed out), without a
-    timeout on the GPU; 0 restores the real read-back.  Returns the previous
-    setting."""
+    timeout on the GPU; 0 restores the real read-back.  A lockstep call
+    captured in a graph while the hook is set writes status 1 into the
+    device word after its tensor-core launches; `status` 2 does only that
+    (ordinary calls read the real word).  Returns the previous setting."""
     f = lib().tfqg_internal_tc_inject_status
     f.argtypes = [ctypes.c_int]
     f.restype = ctypes.c_int
@@ -423,6 +425,27 @@ def batch_lock_rows(handle):
     g.argtypes = [c_void_p]
     g.restype = ctypes.c_int
     return int(f(handle)), int(g(handle))
+
+
+def set_lock_tc(on):
+    """Lockstep rows of batches created from now on run their gates as
+    5-qubit tensor-core blocks (True, the default) or as tile passes
+    (False), unless a per-qubit-count policy says otherwise.  Returns the
+    previous setting."""
+    f = lib().tfqg_internal_set_lock_tc
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return bool(f(1 if on else 0))
+
+
+def batch_lock_tc(handle):
+    """(tensor-core blocks, kernel units) of a batch's lockstep rows."""
+    f = lib().tfqg_internal_batch_lock_tc
+    f.argtypes = [c_void_p, ctypes.POINTER(ctypes.c_int64)]
+    f.restype = ctypes.c_int64
+    u = ctypes.c_int64()
+    nb = f(handle, ctypes.byref(u))
+    return int(nb), u.value
 
 
 def set_wide_few_rows(rows):

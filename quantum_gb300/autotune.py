@@ -4,11 +4,12 @@ For every qubit count present in a batch it times, on the current GPU, the
 candidate plans of the library's rows and installs the fastest one for rows
 of that qubit count in batches created afterwards:
 
-- fusion width: gates applied one by one (width 1), or the forward fuser's
-  folds of one-qubit chains into two-qubit gates (width 2);
-- tile schedule of streamed rows of 17-21 qubits that do not run wide: one
+- fusion width: gates applied one by one (width 1), the forward fuser's
+  folds of one-qubit chains into two-qubit gates (width 2), or 5-qubit
+  blocks on the tensor cores (width 5, streamed rows in lockstep only);
+- tile schedule of streamed rows of 15-21 qubits that do not run wide: one
   CTA per row through the persistent queue, or lockstep over the whole grid
-  (one launch per pass index across all such rows).
+  (one launch per pass index, or per block index, across all such rows).
 
 (Rows of 24 qubits and more take 5-qubit tensor-core blocks by default; that
 choice is the library's and is not tuned here.)
@@ -30,13 +31,14 @@ import numpy as np
 
 from . import _native, ops
 
-LOCK_QUBITS = range(17, 22)
+LOCK_QUBITS = range(15, 22)
 
 
 def set_row_policy(n, fuse=-1, lock=-1):
-    """Policy for rows of n qubits in batches created from now on: fuse /
-    lock -1 (library default), 0 off, 1 on.  n < 0 resets every qubit
-    count."""
+    """Policy for rows of n qubits in batches created from now on: fuse -1
+    (library default), 0 off, 1 on; lock -1 (library default), 0 off (the
+    queue), 1 lockstep on tile passes, 2 lockstep on tensor-core blocks.
+    n < 0 resets every qubit count."""
     f = _native.lib().tfqg_internal_set_row_policy
     f.argtypes = [ctypes.c_int] * 3
     f.restype = ctypes.c_int
@@ -90,7 +92,8 @@ def qubit_counts(programs):
 def _candidates(n):
     c = [(0, -1), (1, -1)]
     if n in LOCK_QUBITS:
-        c = [(f, lk) for f in (0, 1) for lk in (0, 1)]
+        # (the fusion flag does not change tensor-core rows: one candidate)
+        c = [(f, lk) for f in (0, 1) for lk in (0, 1)] + [(1, 2)]
     return c
 
 

@@ -89,10 +89,22 @@ struct tfqg_batch {
     int32_t begin = 0, count = 0;  // items
     int64_t ntiles = 0;            // tiles (or chunks) the launch covers
   };
+  // a launch of the tensor-core block kernel over lockstep rows: units
+  // [begin, begin + count) of tcl_units, all of one variant
+  struct TcLockLaunch {
+    int32_t begin = 0, count = 0;
+    bool trans = false;
+  };
   struct LockGroup {
     int64_t arena_amps = 0;        // states of the group's rows
     LockLaunch rows;               // one item per row (chunk prefix, offset)
-    std::vector<LockLaunch> fwd, meas;
+    std::vector<LockLaunch> fwd, meas;  // fwd: rows on tile passes only
+    // rows whose gates run as tensor-core blocks: one tcl_items entry per
+    // row (chunk prefix, offset), their blocks [tc_block_begin, +count) of
+    // tcl_blocks, and per block index the direct then transposed launches
+    LockLaunch tc_rows;
+    int32_t tc_block_begin = 0, tc_block_count = 0;
+    std::vector<TcLockLaunch> tc;
   };
   std::vector<int32_t> lock_rows;
   std::vector<int32_t> order_lock;
@@ -100,6 +112,12 @@ struct tfqg_batch {
   std::vector<LockGroup> lock_groups;
   bool any_streamed_lock = false;
   int max_streamed_n_lock = 0;
+  // lockstep rows on tensor-core blocks (their blocks' member gates and
+  // batch rows, and the units of every launch), uploaded to tcl_tab
+  std::vector<tfqg::LockItem> tcl_items;
+  std::vector<tfqg::TcBlock> tcl_blocks;
+  std::vector<int32_t> tcl_members, tcl_block_rows;
+  std::vector<tfqg::TcUnit> tcl_units;
   int max_grads = 0;
   int64_t total_gates = 0, total_grads = 0;
   bool any_fused = false;  // forward plans hold GK_FUSED gates
@@ -141,12 +159,18 @@ struct tfqg_batch {
   std::vector<uint8_t> tc_ran;  // the row's last forward call ran the blocks
   std::vector<int32_t> tc_sweeps;  // state sweeps (launches) of that call
   tfqg::DevBuf tc_tab, tc_mats, tc_status;
+  tfqg::DevBuf tcl_tab, tcl_mats;
+  const tfqg::LockItem* d_tcl_items = nullptr;
+  const tfqg::TcBlock* d_tcl_blocks = nullptr;
+  const int32_t* d_tcl_members = nullptr;
+  const int32_t* d_tcl_block_rows = nullptr;
+  const tfqg::TcUnit* d_tcl_units = nullptr;
   // gives every device buffer back to the pool (the device is synchronized)
   void release_buffers() noexcept {
     tfqg::DevBuf* all[] = {&tables,     &mats,     &dmats,     &work,   &counter,
                            &values,     &out,      &aux,       &aux2,   &wide_state,
                            &wide_acc,   &inner_tmp, &tc_tab,   &tc_mats, &tc_status,
-                           &lock_state, &lock_acc};
+                           &lock_state, &lock_acc,  &tcl_tab,  &tcl_mats};
     for (tfqg::DevBuf* d : all) d->release(true);
   }
   tfqg::BatchDevice bd;

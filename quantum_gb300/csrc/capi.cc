@@ -149,8 +149,9 @@ std::atomic<int> g_gate_fusion{1};
 // Row policy per qubit count, set by an autotuner (quantum_gb300/autotune.py)
 // for batches created from then on: gate fusion of the forward plans
 // (-1: the global setting, 0 off, 1 on) and lockstep rows (-1: the
-// lock_min rule, 0 never, 1 when the row is streamed and not wide).  Each
-// change starts a new epoch, which is part of the compiled-program cache key.
+// lock_min rule, 0 never, 1 when the row is streamed and not wide, on tile
+// passes, 2 the same on tensor-core blocks).  Each change starts a new
+// epoch, which is part of the compiled-program cache key.
 constexpr int kPolicyMaxQubits = 64;
 std::atomic<int> g_fuse_by_n[kPolicyMaxQubits];
 std::atomic<int> g_lock_by_n[kPolicyMaxQubits];
@@ -169,6 +170,11 @@ bool fuse_for(int n, bool dflt) {
   return v < 0 ? dflt : v != 0;
 }
 
+// Lockstep rows run their gates as 5-qubit tensor-core blocks (one launch
+// per block index over all the group's rows) unless their qubit count's
+// policy says tile passes (1); g_lock_tc 0 makes tile passes the default.
+std::atomic<int> g_lock_tc{1};
+
 // Forward passes of wide rows as 5-bit fused blocks on the tensor cores
 // (tc_gates.cu) instead of tile passes on the FP32 pipe: 0 never, 1 always,
 // 2 (default) for rows of at least kTcAutoMinQubits qubits, whose states
@@ -176,9 +182,20 @@ bool fuse_for(int n, bool dflt) {
 // and fewer, fuller sweeps win.
 std::atomic<int> g_tc_gates{2};
 constexpr int kTcAutoMinQubits = 24;
+
+// Whether a lockstep row of n qubits takes tensor-core blocks (decided when
+// its batch is created; tensor cores switched off mean tile passes).
+bool lock_tc_for(int n) {
+  if (g_tc_gates.load() == 0 || n < kTcBits + 7) return false;
+  const int pol = n < kPolicyMaxQubits ? g_lock_by_n[n].load() : -1;
+  return pol < 0 ? g_lock_tc.load() != 0 : pol == 2;
+}
 // Test hook: a status value the host treats as read back from the block
 // kernels of the next calls (0: read the real one).  It lets a test take
-// the timeout branch without a timeout on the GPU.
+// the timeout branch without a timeout on the GPU.  Value 1 also makes a
+// captured lockstep call write status 1 into the device word after its
+// tensor-core launches (where a timed-out kernel would set it); value 2
+// does only the latter, so that an ordinary call still succeeds.
 std::atomic<int> g_tc_status_injected{0};
 // Two consecutive blocks share one state sweep (tc_sweep_kernel) where
 // their targets allow it (1), or every block has its own sweep (0, the
@@ -324,16 +341,63 @@ void program_cache_clear() {
 // TFQG_KIND_INNER: `others` holds batch x num_others paired programs
 // (tfq_inner_product's other_programs); they become rows batch + i *
 // num_others + j, resolved with the qubit map of their reference row i.
+// Runs f(i) for i in [0, n) on the host's cores (serially for small n).  f
+// must not throw: callers keep one exception slot per index and rethrow the
+// first one in index order, so errors surface as a serial loop would raise
+// them.
+template <class F>
+void parallel_for(size_t n, F&& f) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t workers = std::min<size_t>({size_t(hw), size_t(32), n});
+  if (n < 32 || workers <= 1) {
+    for (size_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  auto run = [&]() {
+    for (size_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
+  };
+  std::vector<std::thread> pool;
+  pool.reserve(workers - 1);
+  for (size_t w = 1; w < workers; ++w) pool.emplace_back(run);
+  run();
+  for (std::thread& t : pool) t.join();
+}
+
+void rethrow_first(const std::vector<std::exception_ptr>& errs) {
+  for (const std::exception_ptr& e : errs)
+    if (e) std::rethrow_exception(e);
+}
+
 // Lockstep schedule of the batch's lock rows: groups of rows whose states
 // fit g_lock_arena_amps together; per group one item per row (its chunk
 // prefix and arena offset), then per launch k the items of forward pass k of
-// every row that has one, then per launch m those of measurement pass m.
+// every row on tile passes that has one, then per launch m those of
+// measurement pass m.  Rows on tensor-core blocks get their own item list
+// (tcl_items), their blocks and, per block index, the units of a direct and
+// a transposed launch.
 void build_lock_schedule(tfqg_batch* b) {
   const size_t nr = b->lock_rows.size();
-  size_t i = 0;
   auto prog = [&](int32_t row) -> const DevProgram& {
     return b->programs[b->rows[size_t(row)].program];
   };
+  // block plans of the rows that take the tensor cores (planned on the
+  // host's cores; a row without a plan stays on tile passes)
+  std::vector<std::vector<TcBlock>> tcb(nr);
+  std::vector<std::vector<int32_t>> tcm(nr);
+  std::vector<uint8_t> tc(nr, 0);
+  parallel_for(nr, [&](size_t k) {
+    const DevProgram& p = prog(b->lock_rows[k]);
+    if (!lock_tc_for(p.n)) return;
+    try {
+      tc[k] = plan_tc_blocks(b->gates.data() + p.gate_begin, p.num_gates, p.n, &tcb[k],
+                             &tcm[k]) &&
+              !tcb[k].empty();
+    } catch (...) {
+      tc[k] = 0;
+    }
+  });
+  size_t i = 0;
   while (i < nr) {
     tfqg_batch::LockGroup g;
     size_t j = i;
@@ -361,7 +425,7 @@ void build_lock_schedule(tfqg_batch* b) {
     for (size_t k = i; k < j; ++k) {
       const DevProgram& p = prog(b->lock_rows[k]);
       const DevRow& r = b->rows[size_t(b->lock_rows[k])];
-      max_fwd = std::max(max_fwd, p.fwd_pass_end - p.fwd_pass_begin);
+      if (!tc[k]) max_fwd = std::max(max_fwd, p.fwd_pass_end - p.fwd_pass_begin);
       max_meas = std::max(max_meas, r.meas_end - r.meas_begin);
     }
     for (int meas = 0; meas < 2; ++meas) {
@@ -370,6 +434,7 @@ void build_lock_schedule(tfqg_batch* b) {
         tfqg_batch::LockLaunch L;
         L.begin = int32_t(b->lock_items.size());
         for (size_t k = i; k < j; ++k) {
+          if (!meas && tc[k]) continue;
           const int32_t row = b->lock_rows[k];
           const DevProgram& p = prog(row);
           const DevRow& r = b->rows[size_t(row)];
@@ -384,37 +449,61 @@ void build_lock_schedule(tfqg_batch* b) {
         (meas ? g.meas : g.fwd).push_back(L);
       }
     }
+    // the group's tensor-core rows
+    g.tc_rows.begin = int32_t(b->tcl_items.size());
+    g.tc_block_begin = int32_t(b->tcl_blocks.size());
+    std::vector<int32_t> first_block(j - i, -1);
+    size_t max_blocks = 0;
+    int64_t tchunks = 0;
+    for (size_t k = i; k < j; ++k) {
+      if (!tc[k]) continue;
+      const int32_t row = b->lock_rows[k];
+      const int n = prog(row).n;
+      b->tcl_items.push_back(LockItem{row, 0u, tchunks, off[k - i], n, 0});
+      tchunks += int64_t(1) << (n - kLockChunkBits);
+      first_block[k - i] = int32_t(b->tcl_blocks.size());
+      const uint32_t mbase = uint32_t(b->tcl_members.size());
+      for (TcBlock t : tcb[k]) {
+        t.member_begin += mbase;
+        t.member_end += mbase;
+        b->tcl_blocks.push_back(t);
+        b->tcl_block_rows.push_back(row);
+      }
+      b->tcl_members.insert(b->tcl_members.end(), tcm[k].begin(), tcm[k].end());
+      max_blocks = std::max(max_blocks, tcb[k].size());
+    }
+    g.tc_rows.count = int32_t(b->tcl_items.size()) - g.tc_rows.begin;
+    g.tc_rows.ntiles = tchunks;
+    g.tc_block_count = int32_t(b->tcl_blocks.size()) - g.tc_block_begin;
+    for (size_t q = 0; q < max_blocks; ++q)
+      for (int trans = 0; trans < 2; ++trans) {
+        tfqg_batch::TcLockLaunch L;
+        L.begin = int32_t(b->tcl_units.size());
+        L.trans = trans != 0;
+        for (size_t k = i; k < j; ++k) {
+          if (!tc[k] || q >= tcb[k].size()) continue;
+          const int32_t row = b->lock_rows[k];
+          const int n = prog(row).n;
+          TcUnit u{};
+          const int v = tc_unit_geometry(tcb[k][q], n, &u.tpack, &u.tr);
+          if (v < 0) throw Error(kInternal, "tensor-core block outside its row's qubits");
+          if (v != trans) continue;
+          u.off = off[k - i];
+          u.row = row;
+          u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
+          const int64_t nch = int64_t(1) << (n - kTcBits - 7);
+          for (int64_t c = 0; c < nch; c += kTcUnitChunks) {
+            u.chunk0 = c;
+            u.nchunks = int32_t(std::min<int64_t>(kTcUnitChunks, nch - c));
+            b->tcl_units.push_back(u);
+          }
+        }
+        L.count = int32_t(b->tcl_units.size()) - L.begin;
+        if (L.count) g.tc.push_back(L);
+      }
     b->lock_groups.push_back(std::move(g));
     i = j;
   }
-}
-
-// Runs f(i) for i in [0, n) on the host's cores (serially for small n).  f
-// must not throw: callers keep one exception slot per index and rethrow the
-// first one in index order, so errors surface as a serial loop would raise
-// them.
-template <class F>
-void parallel_for(size_t n, F&& f) {
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const size_t workers = std::min<size_t>({size_t(hw), size_t(32), n});
-  if (n < 32 || workers <= 1) {
-    for (size_t i = 0; i < n; ++i) f(i);
-    return;
-  }
-  std::atomic<size_t> next{0};
-  auto run = [&]() {
-    for (size_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
-  };
-  std::vector<std::thread> pool;
-  pool.reserve(workers - 1);
-  for (size_t w = 1; w < workers; ++w) pool.emplace_back(run);
-  run();
-  for (std::thread& t : pool) t.join();
-}
-
-void rethrow_first(const std::vector<std::exception_ptr>& errs) {
-  for (const std::exception_ptr& e : errs)
-    if (e) std::rethrow_exception(e);
 }
 
 void build_batch(tfqg_batch* b, const char* const* programs,
@@ -992,8 +1081,7 @@ void check_tc_status(tfqg_batch* b, cudaStream_t s) {
   int v = 0;
   TFQG_CUDA(cudaMemcpyAsync(&v, b->tc_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   TFQG_CUDA(cudaStreamSynchronize(s));
-  const int injected = g_tc_status_injected.load();
-  if (injected) v = injected;
+  if (g_tc_status_injected.load() == 1) v = 1;
   if (v != 0)
     throw Error(kInternal,
                 "tensor-core block kernel: an MMA completion wait timed out; the wide "
@@ -1174,9 +1262,38 @@ void run_wide_adjoint(tfqg_batch* b, const BatchDevice& bd, RunArgs* a, cudaStre
   }
 }
 
+// Uploads the tensor-core tables of the lockstep rows (items, blocks,
+// members, block rows, units) once per device and sizes their fused-matrix
+// buffer.
+void tcl_prepare(tfqg_batch* b, cudaStream_t s) {
+  if (b->tcl_tab.p && b->tcl_tab.device == b->device) return;
+  std::vector<unsigned char> blob;
+  const size_t o_items = put(&blob, b->tcl_items);
+  const size_t o_blocks = put(&blob, b->tcl_blocks);
+  const size_t o_members = put(&blob, b->tcl_members);
+  const size_t o_rows = put(&blob, b->tcl_block_rows);
+  const size_t o_units = put(&blob, b->tcl_units);
+  blob.resize(align256(blob.size()));
+  b->tcl_tab.reserve(blob.size(), b->device);
+  unsigned char* base = static_cast<unsigned char*>(b->tcl_tab.p);
+  TFQG_CUDA(cudaMemcpyAsync(base, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+  TFQG_CUDA(cudaStreamSynchronize(s));  // blob is a temporary
+  b->d_tcl_items = reinterpret_cast<const LockItem*>(base + o_items);
+  b->d_tcl_blocks = reinterpret_cast<const TcBlock*>(base + o_blocks);
+  b->d_tcl_members = reinterpret_cast<const int32_t*>(base + o_members);
+  b->d_tcl_block_rows = reinterpret_cast<const int32_t*>(base + o_rows);
+  b->d_tcl_units = reinterpret_cast<const TcUnit*>(base + o_units);
+  b->tcl_mats.reserve(std::max<size_t>(b->tcl_blocks.size(), 1) * 1024 * sizeof(float2),
+                      b->device);
+  b->tc_status.reserve(sizeof(int), b->device);
+}
+
 // Forward-mode work of the lockstep rows, group after group on stream s:
-// one launch per forward pass index over every row of the group, then the
-// group's measurement, state padding or sampling.
+// the group's tensor-core rows (fused block matrices, |0...0>, one launch
+// per block index and variant), one launch per forward pass index over its
+// rows on tile passes, then the group's measurement, state padding or
+// sampling.  A captured call cannot read the tensor-core status word back,
+// so there the rows' results are replaced by markers on a timeout.
 void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaStream_t s) {
   const int dev = b->device;
   const int state_amps = 1 << kStreamTileBits;
@@ -1209,7 +1326,40 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
     acc = static_cast<double*>(b->lock_acc.p);
   }
   const LockItem* items = b->d_lock_items;
+  const bool any_tc = !b->tcl_units.empty();
+  bool capturing = false;
+  int* st = nullptr;
+  float2* U = nullptr;
+  int tgrid = 0;
+  if (any_tc) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    TFQG_CUDA(cudaStreamIsCapturing(s, &cs));
+    capturing = cs != cudaStreamCaptureStatusNone;
+    tcl_prepare(b, s);
+    st = static_cast<int*>(b->tc_status.p);
+    TFQG_CUDA(cudaMemsetAsync(st, 0, sizeof(int), s));
+    U = static_cast<float2*>(b->tcl_mats.p);
+    tgrid = tc_grid(dev);
+  }
+  // tensor-core rows write their states in place: the arena, or the output
+  // rows of a state call
+  float2* tc_state = mode == kModeState ? a->out_state : state;
+  const int row_shift = mode == kModeState ? b->max_n : -1;
   for (const auto& g : b->lock_groups) {
+    if (g.tc_rows.count) {
+      TFQG_CUDA(launch_tc_fuse_rows(bd, a->mats, b->d_tcl_block_rows + g.tc_block_begin,
+                                    b->d_tcl_blocks + g.tc_block_begin, b->d_tcl_members,
+                                    g.tc_block_count, U + int64_t(g.tc_block_begin) * 1024, s));
+      TFQG_CUDA(launch_lock_zero(tc_state, row_shift, b->d_tcl_items + g.tc_rows.begin,
+                                 g.tc_rows.count, g.tc_rows.ntiles, sms * 8, s));
+      for (const auto& L : g.tc)
+        TFQG_CUDA(launch_tc_apply5_units(tc_state, row_shift, U, b->d_tcl_units + L.begin,
+                                         L.count, L.trans, st, tgrid, s));
+      // test hook: a captured call records an injected status on the
+      // device, where a timed-out kernel would have set it
+      if (capturing && g_tc_status_injected.load() != 0)
+        TFQG_CUDA(cudaMemsetAsync(st, 1, 1, s));
+    }
     for (size_t k = 0; k < g.fwd.size(); ++k)
       TFQG_CUDA(sim_launch_lock(bd, *a, items + g.fwd[k].begin, g.fwd[k].count,
                                 g.fwd[k].ntiles, state, k == 0 ? 1 : 0,
@@ -1228,7 +1378,11 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
                                        s));
       TFQG_CUDA(launch_lock_sample(bd, *a, rws, g.rows.count, state, acc, s));
     }
+    if (capturing && g.tc_rows.count)
+      TFQG_CUDA(launch_lock_tc_poison(bd, *a, mode, b->d_tcl_items + g.tc_rows.begin,
+                                      g.tc_rows.count, st, s));
   }
+  if (any_tc && !capturing) check_tc_status(b, s);
 }
 
 int simulate(tfqg_batch* b, int mode, RunArgs* a, cudaStream_t s) {
@@ -1871,7 +2025,7 @@ std::vector<void*> batch_buffers(tfqg_batch* b) {
   return {b->tables.p,     b->mats.p,      b->dmats.p,     b->work.p,     b->counter.p,
           b->values.p,     b->out.p,       b->aux.p,       b->aux2.p,     b->wide_state.p,
           b->wide_acc.p,   b->tc_tab.p,    b->tc_mats.p,   b->tc_status.p, b->lock_state.p,
-          b->lock_acc.p};
+          b->lock_acc.p,   b->tcl_tab.p,   b->tcl_mats.p};
 }
 
 int run_forward(tfqg_batch* b, int what, const float* values, int32_t num_samples,
@@ -2272,7 +2426,8 @@ int tfqg_internal_tc_sweep(void* psi, int n, const void* U0, const void* U1,
 }
 
 // Makes the next calls treat the tensor-core status word as `status`
-// (0 restores the real read-back); returns the previous setting.
+// (0 restores the real read-back; 2: captured calls only, see
+// g_tc_status_injected); returns the previous setting.
 int tfqg_internal_tc_inject_status(int status) { return g_tc_status_injected.exchange(status); }
 
 int tfqg_internal_tc_status(void* batch) {
@@ -2334,8 +2489,9 @@ int tfqg_internal_tc_plan(void* batch, int64_t row, const float* row_values, int
 int tfqg_internal_set_wide_few_rows(int rows) { return g_wide_few_rows.exchange(rows); }
 
 // Row policy for rows of n qubits in batches created from now on (see
-// g_fuse_by_n): fuse / lock -1 default, 0 off, 1 on; n < 0 resets every
-// qubit count.  Returns the new policy epoch.
+// g_fuse_by_n): fuse -1 default, 0 off, 1 on; lock -1 default, 0 off, 1
+// lockstep on tile passes, 2 lockstep on tensor-core blocks; n < 0 resets
+// every qubit count.  Returns the new policy epoch.
 int tfqg_internal_set_row_policy(int n, int fuse, int lock) {
   if (n < 0) {
     for (int i = 0; i < kPolicyMaxQubits; ++i) {
@@ -2344,9 +2500,20 @@ int tfqg_internal_set_row_policy(int n, int fuse, int lock) {
     }
   } else if (n < kPolicyMaxQubits) {
     g_fuse_by_n[n].store(fuse < 0 ? -1 : fuse != 0);
-    g_lock_by_n[n].store(lock < 0 ? -1 : lock != 0);
+    g_lock_by_n[n].store(lock < 0 ? -1 : std::min(lock, 2));
   }
   return g_policy_epoch.fetch_add(1) + 1;
+}
+
+// Lockstep rows of batches created from now on default to tensor-core
+// blocks (1) or tile passes (0); returns the previous value.
+int tfqg_internal_set_lock_tc(int on) { return g_lock_tc.exchange(on ? 1 : 0); }
+
+// Tensor-core blocks and units of a batch's lockstep rows (for tests).
+int64_t tfqg_internal_batch_lock_tc(const tfqg_batch* b, int64_t* units) {
+  if (!b) return -1;
+  if (units) *units = int64_t(b->tcl_units.size());
+  return int64_t(b->tcl_blocks.size());
 }
 
 // Qubit count from which streamed rows of batches created from now on run in

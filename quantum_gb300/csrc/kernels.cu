@@ -508,6 +508,52 @@ __global__ void lock_pad_kernel(BatchDevice b, RunArgs a, const LockItem* rows) 
     out[k] = make_float2(-2.f, 0.f);
 }
 
+// |0...0> in every row of `rows`, one warp per chunk of 2^kLockChunkBits
+// amplitudes (16-byte stores)
+__global__ void __launch_bounds__(256)
+lock_zero_kernel(float2* state, int row_shift, const LockItem* rows, int nrows,
+                 int64_t nchunks) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t C = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); C < nchunks;
+       C += warps) {
+    const LockItem it = rows[lock_find(rows, nrows, C)];
+    float2* psi = state + (row_shift >= 0 ? (int64_t(it.row) << row_shift) : it.off);
+    const int64_t c = C - it.prefix;
+    float4* p = reinterpret_cast<float4*>(psi + (c << kLockChunkBits));
+#pragma unroll
+    for (int k = 0; k < (1 << (kLockChunkBits - 1)) / 32; ++k) {
+      const int q = lane + 32 * k;
+      __stcg(p + q, make_float4(c == 0 && q == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f));
+    }
+  }
+}
+
+// One CTA per row: the row's outputs become markers when *status is set.
+__global__ void lock_tc_poison_kernel(BatchDevice b, RunArgs a, int mode, const LockItem* rows,
+                                      const int* status) {
+  if (*status == 0) return;
+  const LockItem it = rows[blockIdx.x];
+  const float nan = __int_as_float(0x7fc00000);
+  if (mode == kModeExpect) {
+    for (int j = threadIdx.x; j < b.num_ops; j += blockDim.x)
+      a.out_f[int64_t(it.row) * b.num_ops + j] = nan;
+    if (a.term_vals) {
+      const DevRow r = b.rows[it.row];
+      for (uint32_t t = threadIdx.x; t < r.term_end - r.term_begin; t += blockDim.x)
+        a.term_vals[int64_t(it.row) * a.term_stride + t] = nan;
+    }
+  } else if (mode == kModeState) {
+    float2* out = a.out_state + (int64_t(it.row) << b.max_n);
+    for (int64_t k = threadIdx.x; k < (int64_t(1) << it.n); k += blockDim.x)
+      out[k] = make_float2(nan, nan);
+  } else {
+    int8_t* out = a.out_samples + int64_t(it.row) * a.num_samples * b.max_n;
+    for (int64_t k = threadIdx.x; k < int64_t(a.num_samples) * b.max_n; k += blockDim.x)
+      out[k] = -1;
+  }
+}
+
 __global__ void fill_kernel(float2* p, int64_t count, float2 first, float2 rest) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
        i += int64_t(gridDim.x) * blockDim.x)
@@ -710,6 +756,21 @@ cudaError_t launch_lock_pad(const BatchDevice& b, const RunArgs& a, const LockIt
                             int nrows, cudaStream_t s) {
   if (nrows <= 0) return cudaSuccess;
   lock_pad_kernel<<<dim3(8, unsigned(nrows)), 256, 0, s>>>(b, a, rows);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lock_zero(float2* state, int row_shift, const LockItem* rows, int nrows,
+                             int64_t nchunks, int grid, cudaStream_t s) {
+  if (nrows <= 0 || nchunks <= 0) return cudaSuccess;
+  lock_zero_kernel<<<grid, 256, 0, s>>>(state, row_shift, rows, nrows, nchunks);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lock_tc_poison(const BatchDevice& b, const RunArgs& a, int mode,
+                                  const LockItem* rows, int nrows, const int* status,
+                                  cudaStream_t s) {
+  if (nrows <= 0) return cudaSuccess;
+  lock_tc_poison_kernel<<<nrows, 256, 0, s>>>(b, a, mode, rows, status);
   return cudaGetLastError();
 }
 

@@ -262,6 +262,53 @@ const void* tc_sweep_kernel_ptr();
 cudaError_t launch_tc_sweep2(float2* psi, int n, const float2* U0, const float2* U1,
                              const TcBlock& b0, const TcBlock& b1, int* status, int grid,
                              cudaStream_t s);
+// Lockstep rows on the tensor cores: block k of every row of a lockstep
+// group in one launch.  A unit is a run of consecutive chunks (128 groups of
+// 32 amplitudes each) of one row's state under one block: the state (arena
+// offset `off`, or batch row `row` of the output states), the block's
+// fused matrix (index `mat` into the matrices buffer), its packed targets
+// and, for the transposed variant, its chunk geometry.  Units of one launch
+// all take the same variant.
+struct TcUnit {
+  int64_t off;
+  int64_t chunk0;
+  int32_t nchunks;
+  int32_t row;
+  uint32_t tpack;
+  uint32_t mat;
+  TcTrans tr;
+};
+static_assert(sizeof(TcUnit) == 56, "TcUnit layout");
+// Chunks per unit (the block's B operands are built once per unit).
+constexpr int kTcUnitChunks = 16;
+// Targets of `blk` packed 5 bits each and the variant (1 transposed, 0
+// direct, with its geometry in *tr), or -1 when the block does not fit a
+// 2^n state.
+int tc_unit_geometry(const TcBlock& blk, int n, uint32_t* tpack, TcTrans* tr);
+// Fused matrices of blocks whose rows differ: block i belongs to batch row
+// block_rows[i].
+cudaError_t launch_tc_fuse_rows(const BatchDevice& b, const float2* mats,
+                                const int32_t* block_rows, const TcBlock* blocks,
+                                const int32_t* members, int nblocks, float2* U,
+                                cudaStream_t s);
+// Applies each unit's block (matrix U + 1024 * mat) to its chunks; the
+// state of a unit is state + off, or state + (row << row_shift) when
+// row_shift >= 0.  *status set to 1 on a timed-out MMA wait.
+cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float2* U,
+                                   const TcUnit* units, int nunits, bool trans, int* status,
+                                   int grid, cudaStream_t s);
+// |0...0> in every row of `rows` (chunks of 2^kLockChunkBits amplitudes
+// counted by the items' prefixes); states at arena + off, or at
+// state + (row << row_shift) when row_shift >= 0.
+cudaError_t launch_lock_zero(float2* state, int row_shift, const LockItem* rows, int nrows,
+                             int64_t nchunks, int grid, cudaStream_t s);
+// After a captured call whose tensor-core launches set *status: the rows'
+// results are replaced by markers (expectations and amplitudes NaN, every
+// sample -1), since a replay has no host check.  Does nothing while
+// *status is 0.
+cudaError_t launch_lock_tc_poison(const BatchDevice& b, const RunArgs& a, int mode,
+                                  const LockItem* rows, int nrows, const int* status,
+                                  cudaStream_t s);
 // p[i] = (i == 0 ? first : rest) for i in [0, count).
 cudaError_t launch_fill(float2* p, int64_t count, float2 first, float2 rest, int grid,
                         cudaStream_t s);

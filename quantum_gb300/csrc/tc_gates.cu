@@ -123,12 +123,14 @@ __device__ __forceinline__ int64_t group_base(int64_t g, const int* t) {
   return g;
 }
 
+// Block blk belongs to batch row block_rows[blk] (or `row` when block_rows
+// is null).
 __global__ void tc_fuse_kernel(BatchDevice b, const float2* mats, int row,
-                               const TcBlock* blocks, const int32_t* members, int nblocks,
-                               float2* U) {
+                               const int32_t* block_rows, const TcBlock* blocks,
+                               const int32_t* members, int nblocks, float2* U) {
   const int blk = blockIdx.x, j = threadIdx.x;
   if (blk >= nblocks || j >= 32) return;
-  const DevRow r = b.rows[row];
+  const DevRow r = b.rows[block_rows ? block_rows[blk] : row];
   const DevProgram p = b.programs[r.program];
   const GateTemplate* gates = b.gates + p.gate_begin;
   const float2* m0 = mats + int64_t(r.mat_offset) * 16;
@@ -169,18 +171,81 @@ __device__ __forceinline__ uint32_t tr_deposit(uint32_t v, uint32_t pos, int bit
   return L;
 }
 
+// Shared memory of the block kernels: the A operands (hi, lo), the B
+// operands (hi, lo), the MMA mbarrier, the TMEM base address and the
+// timeout flag, at fixed offsets from the dynamic shared-memory base.
+struct TcSmem {
+  unsigned char* s;
+  __device__ __forceinline__ float* a_hi() const { return reinterpret_cast<float*>(s); }
+  __device__ __forceinline__ float* a_lo() const {
+    return reinterpret_cast<float*>(s + kTcAbytes);
+  }
+  __device__ __forceinline__ float* b_hi() const {
+    return reinterpret_cast<float*>(s + 2 * kTcAbytes);
+  }
+  __device__ __forceinline__ float* b_lo() const {
+    return reinterpret_cast<float*>(s + 2 * kTcAbytes + kTcBbytes);
+  }
+  __device__ __forceinline__ uint64_t* bar() const {
+    return reinterpret_cast<uint64_t*>(s + 2 * kTcAbytes + 2 * kTcBbytes);
+  }
+  __device__ __forceinline__ uint32_t* tmem_slot() const {
+    return reinterpret_cast<uint32_t*>(bar() + 1);
+  }
+  __device__ __forceinline__ int* timed_out() const { return reinterpret_cast<int*>(bar() + 2); }
+};
+
+// mbarrier and timeout flag initialised, TMEM allocated; returns its base.
+__device__ __forceinline__ uint32_t tc_begin(const TcSmem& m) {
+  if (threadIdx.x == 0) {
+    *m.timed_out() = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(m.bar())) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if ((threadIdx.x >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(m.tmem_slot())),
+                 "r"(kTcTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  return *m.tmem_slot();
+}
+
+// After a timed-out wait the MMAs may still be running: wait for them
+// (bounded) and record status 1; then free the TMEM.
+__device__ __forceinline__ void tc_end(const TcSmem& m, uint32_t tmem, bool failed,
+                                       uint32_t parity, int* status) {
+  if (failed) {
+    bool done = false;
+    for (uint32_t it = 0; it < kTcSpin && !done; ++it)
+      done = mbar_try_wait(smem_u32(m.bar()), parity ^ 1u);
+    if (threadIdx.x == 0) atomicExch(status, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                 "r"(kTcTmemCols)
+                 : "memory");
+}
+
+// Applies one block (matrix U, targets tpack, transposed geometry tr) to
+// chunks chunk, chunk + step, ... below nchunk of the state psi.  `parity`
+// is the MMA mbarrier's phase, carried from call to call.  Returns false
+// when an MMA completion wait timed out (the same value in every thread of
+// the CTA).
 template <bool kTrans>
-__global__ void __launch_bounds__(kTcRows, 2)
-tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
-                 uint32_t tpack, TcTrans tr, int* status) {
-  extern __shared__ __align__(1024) unsigned char tc_smem[];
-  float* a_hi = reinterpret_cast<float*>(tc_smem);
-  float* a_lo = reinterpret_cast<float*>(tc_smem + kTcAbytes);
-  float* b_hi = reinterpret_cast<float*>(tc_smem + 2 * kTcAbytes);
-  float* b_lo = reinterpret_cast<float*>(tc_smem + 2 * kTcAbytes + kTcBbytes);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tc_smem + 2 * kTcAbytes + 2 * kTcBbytes);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
-  int* timed_out = reinterpret_cast<int*>(bar + 2);
+__device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
+                                                 const float2* __restrict__ U, uint32_t tpack,
+                                                 const TcTrans& tr, int64_t chunk,
+                                                 int64_t nchunk, int64_t step, const TcSmem& m,
+                                                 uint32_t tmem, uint32_t& parity) {
+  float* a_hi = m.a_hi();
+  float* a_lo = m.a_lo();
   // staging buffers of the transposed variant: the A operands' space, free
   // whenever no MMA is in flight (loads stage in a_hi, results in a_lo)
   float2* stage_in = reinterpret_cast<float2*>(a_hi);
@@ -216,35 +281,18 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
     h_t = tr_h(uint32_t(2 * tid), tr.c);
   }
 
-  // B operands: R in real form, split into tf32 hi and lo
+  // B operands: R in real form, split into tf32 hi and lo (no MMA is in
+  // flight: the previous call's last completion was waited for)
   for (int idx = tid; idx < kTcNdim * kTcKdim; idx += blockDim.x) {
     const int nr = idx / kTcKdim, k = idx % kTcKdim;
     const float2 u = U[(nr >> 1) * 32 + (k >> 1)];
     const float v = (nr & 1) ? ((k & 1) ? u.x : u.y) : ((k & 1) ? -u.y : u.x);
     const float hi = tf32_hi(v);
     const uint32_t o = kmaj(nr, k) >> 2;
-    b_hi[o] = hi;
-    b_lo[o] = v - hi;
+    m.b_hi()[o] = hi;
+    m.b_lo()[o] = v - hi;
   }
-  if (tid == 0) {
-    *timed_out = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
-                     smem_u32(tmem_slot)),
-                 "r"(kTcTmemCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
 
-  const int64_t nchunk = int64_t(1) << (n - kTcBits - 7);
-  int64_t chunk = blockIdx.x;
   float2 v[32];
   float4 raw[16];
   // chunk c starts at the index of its group 128 c (row and target bits 0)
@@ -277,7 +325,6 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
       for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
     }
   }
-  uint32_t parity = 0;
   bool failed = false;
   while (chunk < nchunk) {
     if (kTrans) {
@@ -307,7 +354,7 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
     if (tid == 0) {
       const uint32_t idesc = idesc_tf32(kTcRows, kTcNdim);
       const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
-      const uint32_t bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+      const uint32_t bh = smem_u32(m.b_hi()), bl = smem_u32(m.b_lo());
       const uint32_t as[3] = {al, ah, ah}, bs[3] = {bh, bl, bh};
       uint32_t acc = 0;
       for (int pr = 0; pr < 3; ++pr)
@@ -323,10 +370,10 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
         }
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-              smem_u32(bar))
+              smem_u32(m.bar()))
           : "memory");
     }
-    const int64_t next = chunk + gridDim.x;
+    const int64_t next = chunk + step;
     if (next < nchunk) {  // the next chunk's loads overlap the MMAs
       if (kTrans) {
         load_raw(next);
@@ -337,12 +384,12 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
       }
     }
     bool done = false;
-    for (uint32_t it = 0; it < kTcSpin && !done; ++it) done = mbar_try_wait(smem_u32(bar), parity);
-    if (!done) atomicExch(timed_out, 1);
+    for (uint32_t it = 0; it < kTcSpin && !done; ++it) done = mbar_try_wait(smem_u32(m.bar()), parity);
+    if (!done) atomicExch(m.timed_out(), 1);
     parity ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     __syncthreads();
-    if (*timed_out) {
+    if (*m.timed_out()) {
       failed = true;
       break;
     }
@@ -384,19 +431,41 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     chunk = next;
   }
-  if (failed) {
-    // the MMAs may still be running: wait for them (bounded) before freeing
-    bool done = false;
-    for (uint32_t it = 0; it < kTcSpin && !done; ++it)
-      done = mbar_try_wait(smem_u32(bar), parity ^ 1u);
-    if (tid == 0) atomicExch(status, 1);
+  return !failed;
+}
+
+template <bool kTrans>
+__global__ void __launch_bounds__(kTcRows, 2)
+tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
+                 uint32_t tpack, TcTrans tr, int* status) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  const TcSmem m{tc_smem};
+  const uint32_t tmem = tc_begin(m);
+  uint32_t parity = 0;
+  const int64_t nchunk = int64_t(1) << (n - kTcBits - 7);
+  const bool ok = tc_apply5_chunks<kTrans>(psi, U, tpack, tr, blockIdx.x, nchunk, gridDim.x,
+                                           m, tmem, parity);
+  tc_end(m, tmem, !ok, parity, status);
+}
+
+// Units of many rows' states (lockstep rows), taken grid-strided; each
+// unit's chunks run in order, the next chunk's loads overlapping the MMAs.
+template <bool kTrans>
+__global__ void __launch_bounds__(kTcRows, 2)
+tc_apply5_units_kernel(float2* __restrict__ state, int row_shift, const float2* __restrict__ U,
+                       const TcUnit* __restrict__ units, int nunits, int* status) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  const TcSmem m{tc_smem};
+  const uint32_t tmem = tc_begin(m);
+  uint32_t parity = 0;
+  bool ok = true;
+  for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+    const TcUnit un = units[u];
+    float2* psi = state + (row_shift >= 0 ? (int64_t(un.row) << row_shift) : un.off);
+    ok = tc_apply5_chunks<kTrans>(psi, U + int64_t(un.mat) * 1024, un.tpack, un.tr, un.chunk0,
+                                  un.chunk0 + un.nchunks, 1, m, tmem, parity);
   }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
-                 "r"(kTcTmemCols)
-                 : "memory");
+  tc_end(m, tmem, !ok, parity, status);
 }
 
 // ---- two blocks per sweep ------------------------------------------------------
@@ -735,7 +804,16 @@ cudaError_t launch_tc_fuse(const BatchDevice& b, const float2* mats, int row,
                            const TcBlock* blocks, const int32_t* members, int nblocks,
                            float2* U, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  tc_fuse_kernel<<<nblocks, 32, 0, s>>>(b, mats, row, blocks, members, nblocks, U);
+  tc_fuse_kernel<<<nblocks, 32, 0, s>>>(b, mats, row, nullptr, blocks, members, nblocks, U);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_fuse_rows(const BatchDevice& b, const float2* mats,
+                                const int32_t* block_rows, const TcBlock* blocks,
+                                const int32_t* members, int nblocks, float2* U,
+                                cudaStream_t s) {
+  if (nblocks <= 0) return cudaSuccess;
+  tc_fuse_kernel<<<nblocks, 32, 0, s>>>(b, mats, 0, block_rows, blocks, members, nblocks, U);
   return cudaGetLastError();
 }
 
@@ -813,6 +891,38 @@ cudaError_t launch_tc_apply5(float2* psi, int n, const float2* U, const TcBlock&
     tc_apply5_kernel<true><<<grid, kTcRows, kTcSmem, s>>>(psi, n, U, tpack, tr, status);
   else
     tc_apply5_kernel<false><<<grid, kTcRows, kTcSmem, s>>>(psi, n, U, tpack, tr, status);
+  return cudaGetLastError();
+}
+
+int tc_unit_geometry(const TcBlock& blk, int n, uint32_t* tpack, TcTrans* tr) {
+  if (n < kTcBits + 7 || n > 31) return -1;
+  uint32_t tp = 0;
+  for (int i = 0; i < kTcBits; ++i) {
+    if (blk.tgt[i] >= n || (i > 0 && blk.tgt[i] <= blk.tgt[i - 1])) return -1;
+    tp |= uint32_t(blk.tgt[i]) << (5 * i);
+  }
+  *tpack = tp;
+  *tr = TcTrans{};
+  return tc_transposed_geometry(blk, n, tr) ? 1 : 0;
+}
+
+cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float2* U,
+                                   const TcUnit* units, int nunits, bool trans, int* status,
+                                   int grid, cudaStream_t s) {
+  if (nunits <= 0) return cudaSuccess;
+  if (grid > nunits) grid = nunits;
+  if (grid < 1) grid = 1;
+  const void* k = trans ? reinterpret_cast<const void*>(&tc_apply5_units_kernel<true>)
+                        : reinterpret_cast<const void*>(&tc_apply5_units_kernel<false>);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(kTcSmem));
+  if (e != cudaSuccess) return e;
+  if (trans)
+    tc_apply5_units_kernel<true><<<grid, kTcRows, kTcSmem, s>>>(state, row_shift, U, units,
+                                                                nunits, status);
+  else
+    tc_apply5_units_kernel<false><<<grid, kTcRows, kTcSmem, s>>>(state, row_shift, U, units,
+                                                                 nunits, status);
   return cudaGetLastError();
 }
 

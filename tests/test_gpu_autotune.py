@@ -1,7 +1,8 @@
 """The autotuner on the GPU: for every qubit count of an uneven batch it
-times the candidate plans (fusion width 1 or 2; for 17-21 qubits also the
-queue or lockstep schedule), installs the fastest, and batches created
-afterwards still give the oracle's expectations."""
+times the candidate plans (fusion width 1 or 2; for 15-21 qubits also the
+queue or lockstep schedule, and lockstep on 5-qubit tensor-core blocks),
+installs the fastest, and batches created afterwards still give the
+oracle's expectations."""
 
 import numpy as np
 import pytest
@@ -29,7 +30,7 @@ def test_tune_installs_the_fastest_candidate(tmp_path, monkeypatch):
         assert sorted(res) == sorted(set(nqs))
         for n, r in res.items():
             assert r["ms"] == min(r["candidates"].values())
-            assert len(r["candidates"]) == (4 if n == 17 else 2)
+            assert len(r["candidates"]) == (5 if n in autotune.LOCK_QUBITS else 2)
         # a second call installs the cached choices without timing
         again = autotune.tune(progs, psums, samples=100, use_cache=True)
         assert all(r["cached"] for r in again.values())

@@ -1,9 +1,10 @@
 """Lockstep rows (forward modes): streamed rows of 17-21 qubits that are not
-wide run side by side over the whole grid, one launch per pass index, instead
-of one CTA each.  Expectation (and the per-term values of the sampled
-expectation), state with padding, and samples against the oracle, with the
-rows split over several lockstep groups, and against the same batch run
-through the queue (lockstep off)."""
+wide run side by side over the whole grid, one launch per pass index (tile
+passes) or per block index (5-qubit tensor-core blocks), instead of one CTA
+each.  Expectation (and the per-term values of the sampled expectation),
+state with padding, and samples against the oracle, with the rows split
+over several lockstep groups, under both gate paths, and against the same
+batch run through the queue (lockstep off)."""
 
 import numpy as np
 import pytest
@@ -19,16 +20,26 @@ pytestmark = pytest.mark.gpu
 NQS = [17, 6, 18, 17, 14, 19, 17, 10]
 
 
-@pytest.fixture
-def lockstep():
+@pytest.fixture(params=[False, True], ids=["tile_passes", "tensor_cores"])
+def lockstep(request):
     """Lockstep from 17 qubits, no few-rows wide rule, small groups (three
-    groups over the batch's five lock rows)."""
+    groups over the batch's five lock rows); the rows' gates on tile passes
+    or on tensor-core blocks."""
     old = (_native.set_lock_min_qubits(17), _native.set_wide_few_rows(0),
-           _native.set_lock_arena_amps(1 << 19))
-    yield
+           _native.set_lock_arena_amps(1 << 19), _native.set_lock_tc(request.param))
+    yield request.param
     _native.set_lock_min_qubits(old[0])
     _native.set_wide_few_rows(old[1])
     _native.set_lock_arena_amps(old[2])
+    _native.set_lock_tc(old[3])
+
+
+def _check_path(b, tc):
+    blocks, units = _native.batch_lock_tc(b._h)
+    if tc:
+        assert blocks > 0 and units >= blocks, (blocks, units)
+    else:
+        assert blocks == 0 and units == 0, (blocks, units)
 
 
 def _inputs(seed):
@@ -48,10 +59,12 @@ def test_expectation_and_state(lockstep):
     b = ops.Batch(programs, names, psums)
     rows, groups = _native.batch_lock_rows(b._h)
     assert rows == 5 and groups >= 3, (rows, groups)
+    _check_path(b, lockstep)
     got = b.expectation(values)
     want = O.simulate_expectation(programs, names, values, psums)
     np.testing.assert_allclose(got, want, atol=expectation_atol(psums), rtol=0)
     sb = ops.Batch(programs, names, None)
+    _check_path(sb, lockstep)
     st = sb.state(values)
     np.testing.assert_allclose(st, O.simulate_state(programs, names, values), atol=1e-5, rtol=0)
     # the same batch through the queue, one CTA per row
@@ -65,6 +78,7 @@ def test_sampled_expectation_term_values(lockstep):
     programs, names, values, psums = _inputs(2)
     b = ops.Batch(programs, names, psums)
     assert _native.batch_lock_rows(b._h)[0] == 5
+    _check_path(b, lockstep)
     R = 40000
     got = b.sampled_expectation(values, np.full((len(NQS), 2), R, np.int32), seed=5)
     want = O.simulate_expectation(programs, names, values, psums)
@@ -76,6 +90,7 @@ def test_samples(lockstep):
     programs, names, values, _ = _inputs(3)
     b = ops.Batch(programs, names, None)
     assert _native.batch_lock_rows(b._h)[0] == 5
+    _check_path(b, lockstep)
     shots = 4000
     s = b.samples(values, shots, seed=9)
     maxn = max(NQS)

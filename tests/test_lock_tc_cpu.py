@@ -1,0 +1,91 @@
+"""The schedule of lockstep rows on tensor-core blocks, built on the host when
+a batch is created (no GPU): every lockstep row with a 5-qubit plan
+contributes its plan's blocks, and every block one unit per 16 chunks of
+128 groups of its row's state; the default, the per-qubit-count policy (2:
+tensor-core blocks, 1: tile passes) and the tensor-core switch decide which
+rows take them; a row whose gate spans six bits keeps its tile passes."""
+
+import numpy as np
+
+from quantum_gb300 import _native, autotune, ops
+from quantum_gb300 import serialize as S
+from tests.circuits import make_gate, random_circuit
+
+
+def _programs(nqs, seed=0, six_bit_row=None):
+    rng = np.random.default_rng(seed)
+    out = []
+    for r, n in enumerate(nqs):
+        qs = S.GridQubit.rect(1, n)
+        c = random_circuit(qs, 6, rng, [])
+        if r == six_bit_row:
+            op = make_gate(rng, "CZP", [qs[1], qs[n - 2]], [], 0.0)
+            c.moments.insert(0, [op.controlled_by(qs[0], qs[3], qs[6], qs[n - 1])])
+        out.append(S.serialize_circuit(c))
+    return out
+
+
+class _Settings:
+    def __enter__(self):
+        self.old = (_native.set_lock_min_qubits(14), _native.set_wide_few_rows(0),
+                    _native.set_lock_tc(True), _native.set_tensor_core_gates(2))
+        autotune.reset()
+        return self
+
+    def __exit__(self, *exc):
+        _native.set_lock_min_qubits(self.old[0])
+        _native.set_wide_few_rows(self.old[1])
+        _native.set_lock_tc(self.old[2])
+        _native.set_tensor_core_gates(self.old[3])
+        autotune.reset()
+
+
+def _expected(b, nqs, rows):
+    blocks = units = 0
+    for r in rows:
+        plan = _native.tc_plan(b._h, r, np.zeros(0, np.float32))
+        assert plan is not None
+        chunks = 2 ** (nqs[r] - 12)
+        blocks += len(plan)
+        units += len(plan) * -(-chunks // 16)
+    return blocks, units
+
+
+def test_units_follow_the_plans():
+    nqs = [15, 18, 6, 17, 21, 15]
+    progs = _programs(nqs)
+    with _Settings():
+        b = ops.Batch(progs, [], None)
+        assert _native.batch_lock_rows(b._h)[0] == 5
+        assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [0, 1, 3, 4, 5])
+
+
+def test_default_and_policy_choose_the_rows():
+    nqs = [16, 18, 18, 16]
+    progs = _programs(nqs, seed=1)
+    with _Settings():
+        _native.set_lock_tc(False)
+        b = ops.Batch(progs, [], None)
+        assert _native.batch_lock_rows(b._h)[0] == 4
+        assert _native.batch_lock_tc(b._h) == (0, 0)
+        autotune.set_row_policy(18, lock=2)
+        b = ops.Batch(progs, [], None)
+        assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [1, 2])
+        _native.set_lock_tc(True)
+        autotune.set_row_policy(18, lock=1)
+        b = ops.Batch(progs, [], None)
+        assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [0, 3])
+        _native.set_tensor_core_gates(0)
+        b = ops.Batch(progs, [], None)
+        assert _native.batch_lock_rows(b._h)[0] == 4
+        assert _native.batch_lock_tc(b._h) == (0, 0)
+
+
+def test_row_without_plan_keeps_tile_passes():
+    nqs = [16, 17, 16]
+    progs = _programs(nqs, seed=2, six_bit_row=1)
+    with _Settings():
+        b = ops.Batch(progs, [], None)
+        assert _native.batch_lock_rows(b._h)[0] == 3
+        assert _native.tc_plan(b._h, 1, np.zeros(0, np.float32)) is None
+        assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [0, 2])
