@@ -480,6 +480,8 @@ void build_lock_schedule(tfqg_batch* b) {
         tfqg_batch::TcLockLaunch L;
         L.begin = int32_t(b->tcl_units.size());
         L.trans = trans != 0;
+        std::vector<std::pair<TcUnit, int64_t>> rows_in;  // unit template, chunks
+        int64_t total = 0;
         for (size_t k = i; k < j; ++k) {
           if (!tc[k] || q >= tcb[k].size()) continue;
           const int32_t row = b->lock_rows[k];
@@ -492,12 +494,19 @@ void build_lock_schedule(tfqg_batch* b) {
           u.row = row;
           u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
           const int64_t nch = int64_t(1) << (n - kTcBits - 7);
-          for (int64_t c = 0; c < nch; c += kTcUnitChunks) {
-            u.chunk0 = c;
-            u.nchunks = int32_t(std::min<int64_t>(kTcUnitChunks, nch - c));
-            b->tcl_units.push_back(u);
-          }
+          rows_in.emplace_back(u, nch);
+          total += nch;
         }
+        // units of up to kTcUnitChunks chunks, fewer when the launch would
+        // otherwise have too few units to spread over the GPU
+        int64_t per = kTcUnitChunks;
+        while (per > 1 && total / per < kTcUnitTarget) per >>= 1;
+        for (auto& ru : rows_in)
+          for (int64_t c = 0; c < ru.second; c += per) {
+            ru.first.chunk0 = c;
+            ru.first.nchunks = int32_t(std::min<int64_t>(per, ru.second - c));
+            b->tcl_units.push_back(ru.first);
+          }
         L.count = int32_t(b->tcl_units.size()) - L.begin;
         if (L.count) g.tc.push_back(L);
       }
@@ -1283,7 +1292,7 @@ void tcl_prepare(tfqg_batch* b, cudaStream_t s) {
   b->d_tcl_members = reinterpret_cast<const int32_t*>(base + o_members);
   b->d_tcl_block_rows = reinterpret_cast<const int32_t*>(base + o_rows);
   b->d_tcl_units = reinterpret_cast<const TcUnit*>(base + o_units);
-  b->tcl_mats.reserve(std::max<size_t>(b->tcl_blocks.size(), 1) * 1024 * sizeof(float2),
+  b->tcl_mats.reserve(std::max<size_t>(b->tcl_blocks.size(), 1) * tc_b_floats() * sizeof(float),
                       b->device);
   b->tc_status.reserve(sizeof(int), b->device);
 }
@@ -1329,7 +1338,7 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
   const bool any_tc = !b->tcl_units.empty();
   bool capturing = false;
   int* st = nullptr;
-  float2* U = nullptr;
+  float* Bops = nullptr;
   int tgrid = 0;
   if (any_tc) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1338,7 +1347,7 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
     tcl_prepare(b, s);
     st = static_cast<int*>(b->tc_status.p);
     TFQG_CUDA(cudaMemsetAsync(st, 0, sizeof(int), s));
-    U = static_cast<float2*>(b->tcl_mats.p);
+    Bops = static_cast<float*>(b->tcl_mats.p);
     tgrid = tc_grid(dev);
   }
   // tensor-core rows write their states in place: the arena, or the output
@@ -1347,13 +1356,14 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
   const int row_shift = mode == kModeState ? b->max_n : -1;
   for (const auto& g : b->lock_groups) {
     if (g.tc_rows.count) {
-      TFQG_CUDA(launch_tc_fuse_rows(bd, a->mats, b->d_tcl_block_rows + g.tc_block_begin,
-                                    b->d_tcl_blocks + g.tc_block_begin, b->d_tcl_members,
-                                    g.tc_block_count, U + int64_t(g.tc_block_begin) * 1024, s));
+      TFQG_CUDA(launch_tc_fuse_b(bd, a->mats, b->d_tcl_block_rows + g.tc_block_begin,
+                                 b->d_tcl_blocks + g.tc_block_begin, b->d_tcl_members,
+                                 g.tc_block_count,
+                                 Bops + int64_t(g.tc_block_begin) * int64_t(tc_b_floats()), s));
       TFQG_CUDA(launch_lock_zero(tc_state, row_shift, b->d_tcl_items + g.tc_rows.begin,
                                  g.tc_rows.count, g.tc_rows.ntiles, sms * 8, s));
       for (const auto& L : g.tc)
-        TFQG_CUDA(launch_tc_apply5_units(tc_state, row_shift, U, b->d_tcl_units + L.begin,
+        TFQG_CUDA(launch_tc_apply5_units(tc_state, row_shift, Bops, b->d_tcl_units + L.begin,
                                          L.count, L.trans, st, tgrid, s));
       // test hook: a captured call records an injected status on the
       // device, where a timed-out kernel would have set it

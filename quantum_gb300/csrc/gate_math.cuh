@@ -318,15 +318,16 @@ TFQG_HD void fused_product(const GateTemplate* gates, const GateTemplate& f,
 
 // Column j of the 32 x 32 matrix of a tensor-core block (TcBlock): the
 // basis state |j> of the block's 5 bits, with every member gate applied in
-// time order, in complex128.  A member's targets and controls map to block
+// time order, in Cx<R> (complex128 or complex64).  A member's targets and
+// controls map to block
 // positions (index bit i of the column is bit blk.tgt[i]); a 2-qubit
 // member's matrix has b0 as its most significant index bit, and the gate
 // acts where the control bits hold their required values.  `load(k, m)`
 // gives member k's matrix (4 or 16 entries).
-template <class Load>
+template <class R, class Load>
 TFQG_HD void tc_block_column(const GateTemplate* gates, const int32_t* members,
-                             const TcBlock& blk, int j, Load load, Cx<double>* col) {
-  for (int i = 0; i < 32; ++i) col[i] = Cx<double>(i == j ? 1.0 : 0.0, 0.0);
+                             const TcBlock& blk, int j, Load load, Cx<R>* col) {
+  for (int i = 0; i < 32; ++i) col[i] = Cx<R>(R(i == j ? 1 : 0), R(0));
   for (uint32_t mi = blk.member_begin; mi < blk.member_end; ++mi) {
     const GateTemplate& g = gates[members[mi]];
     int pos[32];
@@ -338,13 +339,13 @@ TFQG_HD void tc_block_column(const GateTemplate* gates, const int32_t* members,
         cm |= 1u << pos[b];
         if ((g.cval >> b) & 1u) cv |= 1u << pos[b];
       }
-    Cx<double> m[16];
+    Cx<R> m[16];
     load(members[mi], m);
     if (g.nq == 1) {
       const uint32_t s = 1u << pos[g.b0];
       for (uint32_t i = 0; i < 32; ++i) {
         if ((i & s) || (i & cm) != cv) continue;
-        const Cx<double> a = col[i], c = col[i | s];
+        const Cx<R> a = col[i], c = col[i | s];
         col[i] = m[0] * a + m[1] * c;
         col[i | s] = m[2] * a + m[3] * c;
       }
@@ -353,10 +354,10 @@ TFQG_HD void tc_block_column(const GateTemplate* gates, const int32_t* members,
       for (uint32_t i = 0; i < 32; ++i) {
         if ((i & (s0 | s1)) || (i & cm) != cv) continue;
         const uint32_t idx[4] = {i, i | s1, i | s0, i | s0 | s1};
-        Cx<double> v[4], w[4];
+        Cx<R> v[4], w[4];
         for (int k = 0; k < 4; ++k) v[k] = col[idx[k]];
         for (int r = 0; r < 4; ++r) {
-          w[r] = Cx<double>(0.0, 0.0);
+          w[r] = Cx<R>(R(0), R(0));
           for (int k = 0; k < 4; ++k) w[r] = w[r] + m[r * 4 + k] * v[k];
         }
         for (int k = 0; k < 4; ++k) col[idx[k]] = w[k];

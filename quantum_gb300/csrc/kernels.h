@@ -279,22 +279,29 @@ struct TcUnit {
   TcTrans tr;
 };
 static_assert(sizeof(TcUnit) == 56, "TcUnit layout");
-// Chunks per unit (the block's B operands are built once per unit).
+// Chunks per unit: at most kTcUnitChunks (one bulk copy of the block's B
+// operands per unit), fewer where a launch would have fewer than
+// kTcUnitTarget units.
 constexpr int kTcUnitChunks = 16;
+constexpr int64_t kTcUnitTarget = 2048;
 // Targets of `blk` packed 5 bits each and the variant (1 transposed, 0
 // direct, with its geometry in *tr), or -1 when the block does not fit a
 // 2^n state.
 int tc_unit_geometry(const TcBlock& blk, int n, uint32_t* tpack, TcTrans* tr);
-// Fused matrices of blocks whose rows differ: block i belongs to batch row
-// block_rows[i].
-cudaError_t launch_tc_fuse_rows(const BatchDevice& b, const float2* mats,
-                                const int32_t* block_rows, const TcBlock* blocks,
-                                const int32_t* members, int nblocks, float2* U,
-                                cudaStream_t s);
-// Applies each unit's block (matrix U + 1024 * mat) to its chunks; the
-// state of a unit is state + off, or state + (row << row_shift) when
-// row_shift >= 0.  *status set to 1 on a timed-out MMA wait.
-cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float2* U,
+// Floats of one block's B operands (R in real form, tf32 hi then lo, in
+// the block kernel's shared-memory layout).
+size_t tc_b_floats();
+// B operands of blocks whose rows differ (block i belongs to batch row
+// block_rows[i]), from the member gates' bound matrices in complex64:
+// B + i * tc_b_floats().
+cudaError_t launch_tc_fuse_b(const BatchDevice& b, const float2* mats,
+                             const int32_t* block_rows, const TcBlock* blocks,
+                             const int32_t* members, int nblocks, float* B, cudaStream_t s);
+// Applies each unit's block (B operands B + mat * tc_b_floats(), 16-byte
+// aligned) to its chunks; the state of a unit is state + off, or
+// state + (row << row_shift) when row_shift >= 0.  *status set to 1 on a
+// timed-out wait.
+cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float* B,
                                    const TcUnit* units, int nunits, bool trans, int* status,
                                    int grid, cudaStream_t s);
 // |0...0> in every row of `rows` (chunks of 2^kLockChunkBits amplitudes

@@ -57,6 +57,7 @@ constexpr uint32_t kTcSbo = (kTcKdim / 4) * 128u;  // bytes between 8-row groups
 constexpr size_t kTcAbytes = size_t(kTcRows) * kTcKdim * 4;  // 32 KiB
 constexpr size_t kTcBbytes = size_t(kTcNdim) * kTcKdim * 4;  // 16 KiB
 constexpr size_t kTcSmem = 2 * kTcAbytes + 2 * kTcBbytes + 64;
+constexpr int kTcBfloats = int(2 * kTcBbytes / 4);  // B hi and lo of one block
 
 // byte offset of element (row, k) in the K-major no-swizzle layout with 64
 // columns: 8-row groups kTcSbo apart, 16-byte core-matrix rows, 128-byte core
@@ -123,14 +124,12 @@ __device__ __forceinline__ int64_t group_base(int64_t g, const int* t) {
   return g;
 }
 
-// Block blk belongs to batch row block_rows[blk] (or `row` when block_rows
-// is null).
 __global__ void tc_fuse_kernel(BatchDevice b, const float2* mats, int row,
-                               const int32_t* block_rows, const TcBlock* blocks,
-                               const int32_t* members, int nblocks, float2* U) {
+                               const TcBlock* blocks, const int32_t* members, int nblocks,
+                               float2* U) {
   const int blk = blockIdx.x, j = threadIdx.x;
   if (blk >= nblocks || j >= 32) return;
-  const DevRow r = b.rows[block_rows ? block_rows[blk] : row];
+  const DevRow r = b.rows[row];
   const DevProgram p = b.programs[r.program];
   const GateTemplate* gates = b.gates + p.gate_begin;
   const float2* m0 = mats + int64_t(r.mat_offset) * 16;
@@ -143,6 +142,42 @@ __global__ void tc_fuse_kernel(BatchDevice b, const float2* mats, int row,
                   col);
   float2* dst = U + int64_t(blk) * 1024;
   for (int i = 0; i < 32; ++i) dst[i * 32 + j] = make_float2(float(col[i].re), float(col[i].im));
+}
+
+// Lockstep rows: each block's matrix in complex64 (one thread per column;
+// block blk belongs to batch row block_rows[blk]), written straight into
+// the block kernel's B operands: R in real form split into tf32 hi and lo,
+// K-major, kTcBbytes each, hi then lo (kTcBfloats floats per block).
+__global__ void tc_fuse_b_kernel(BatchDevice b, const float2* mats, const int32_t* block_rows,
+                                 const TcBlock* blocks, const int32_t* members, int nblocks,
+                                 float* B) {
+  const int blk = blockIdx.x, j = threadIdx.x;
+  if (blk >= nblocks || j >= 32) return;
+  const DevRow r = b.rows[block_rows[blk]];
+  const DevProgram p = b.programs[r.program];
+  const GateTemplate* gates = b.gates + p.gate_begin;
+  const float2* m0 = mats + int64_t(r.mat_offset) * 16;
+  Cx<float> col[32];
+  tc_block_column(gates, members, blocks[blk], j,
+                  [&](int k, Cx<float>* m) {
+                    const float2* src = m0 + int64_t(k) * 16;
+                    for (int i = 0; i < 16; ++i) m[i] = Cx<float>(src[i].x, src[i].y);
+                  },
+                  col);
+  // thread j holds U[:, j]: the B entries of K columns 2j (re) and 2j + 1 (im)
+  float* bh = B + int64_t(blk) * kTcBfloats;
+  float* bl = bh + kTcBfloats / 2;
+  for (int nr = 0; nr < kTcNdim; ++nr) {
+    const Cx<float> u = col[nr >> 1];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const float v = (nr & 1) ? (c ? u.re : u.im) : (c ? -u.im : u.re);
+      const float hi = tf32_hi(v);
+      const uint32_t o = kmaj(nr, 2 * j + c) >> 2;
+      bh[o] = hi;
+      bl[o] = v - hi;
+    }
+  }
 }
 
 // physical offset of the chunk positions set in L
@@ -193,6 +228,8 @@ struct TcSmem {
     return reinterpret_cast<uint32_t*>(bar() + 1);
   }
   __device__ __forceinline__ int* timed_out() const { return reinterpret_cast<int*>(bar() + 2); }
+  // completion of the bulk copy of the B operands (units kernel)
+  __device__ __forceinline__ uint64_t* bbar() const { return bar() + 3; }
 };
 
 // mbarrier and timeout flag initialised, TMEM allocated; returns its base.
@@ -200,6 +237,7 @@ __device__ __forceinline__ uint32_t tc_begin(const TcSmem& m) {
   if (threadIdx.x == 0) {
     *m.timed_out() = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(m.bar())) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(m.bbar())) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if ((threadIdx.x >> 5) == 0) {
@@ -235,15 +273,18 @@ __device__ __forceinline__ void tc_end(const TcSmem& m, uint32_t tmem, bool fail
 
 // Applies one block (matrix U, targets tpack, transposed geometry tr) to
 // chunks chunk, chunk + step, ... below nchunk of the state psi.  `parity`
-// is the MMA mbarrier's phase, carried from call to call.  Returns false
-// when an MMA completion wait timed out (the same value in every thread of
-// the CTA).
-template <bool kTrans>
+// is the MMA mbarrier's phase, carried from call to call.  kBulkB: the B
+// operands arrive by a bulk copy that completes on m.bbar() in phase
+// parity `bpar` (U unused); the MMA-issuing thread waits for it before its
+// first MMAs.  Returns false when a wait timed out (the same value in every
+// thread of the CTA).
+template <bool kTrans, bool kBulkB>
 __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
                                                  const float2* __restrict__ U, uint32_t tpack,
                                                  const TcTrans& tr, int64_t chunk,
                                                  int64_t nchunk, int64_t step, const TcSmem& m,
-                                                 uint32_t tmem, uint32_t& parity) {
+                                                 uint32_t tmem, uint32_t& parity,
+                                                 uint32_t bpar = 0) {
   float* a_hi = m.a_hi();
   float* a_lo = m.a_lo();
   // staging buffers of the transposed variant: the A operands' space, free
@@ -283,7 +324,7 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
 
   // B operands: R in real form, split into tf32 hi and lo (no MMA is in
   // flight: the previous call's last completion was waited for)
-  for (int idx = tid; idx < kTcNdim * kTcKdim; idx += blockDim.x) {
+  for (int idx = tid; !kBulkB && idx < kTcNdim * kTcKdim; idx += blockDim.x) {
     const int nr = idx / kTcKdim, k = idx % kTcKdim;
     const float2 u = U[(nr >> 1) * 32 + (k >> 1)];
     const float v = (nr & 1) ? ((k & 1) ? u.x : u.y) : ((k & 1) ? -u.y : u.x);
@@ -325,7 +366,7 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
       for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
     }
   }
-  bool failed = false;
+  bool failed = false, b_waited = !kBulkB;
   while (chunk < nchunk) {
     if (kTrans) {
       // staged chunk -> this thread's group (the staging space is the A
@@ -351,7 +392,21 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (tid == 0) {
+    bool issue = tid == 0;
+    if (!b_waited) {
+      // the B operands' bulk copy (bounded wait; on a timeout no MMA is
+      // issued, so the completion wait below times out as well)
+      if (issue) {
+        bool ok = false;
+        for (uint32_t it = 0; it < kTcSpin && !ok; ++it) ok = mbar_try_wait(smem_u32(m.bbar()), bpar);
+        if (!ok) {
+          atomicExch(m.timed_out(), 1);
+          issue = false;
+        }
+      }
+      b_waited = true;
+    }
+    if (issue) {
       const uint32_t idesc = idesc_tf32(kTcRows, kTcNdim);
       const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
       const uint32_t bh = smem_u32(m.b_hi()), bl = smem_u32(m.b_lo());
@@ -443,27 +498,48 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
   const uint32_t tmem = tc_begin(m);
   uint32_t parity = 0;
   const int64_t nchunk = int64_t(1) << (n - kTcBits - 7);
-  const bool ok = tc_apply5_chunks<kTrans>(psi, U, tpack, tr, blockIdx.x, nchunk, gridDim.x,
-                                           m, tmem, parity);
+  const bool ok = tc_apply5_chunks<kTrans, false>(psi, U, tpack, tr, blockIdx.x, nchunk,
+                                                  gridDim.x, m, tmem, parity);
   tc_end(m, tmem, !ok, parity, status);
 }
 
 // Units of many rows' states (lockstep rows), taken grid-strided; each
 // unit's chunks run in order, the next chunk's loads overlapping the MMAs.
+// A unit's B operands (block `mat` of B, kTcBfloats floats) come in one
+// bulk copy (cp.async.bulk, the TMA engine) issued when the unit starts;
+// the previous unit's MMAs, which read the old ones, have completed then.
 template <bool kTrans>
 __global__ void __launch_bounds__(kTcRows, 2)
-tc_apply5_units_kernel(float2* __restrict__ state, int row_shift, const float2* __restrict__ U,
+tc_apply5_units_kernel(float2* __restrict__ state, int row_shift, const float* __restrict__ B,
                        const TcUnit* __restrict__ units, int nunits, int* status) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   const TcSmem m{tc_smem};
   const uint32_t tmem = tc_begin(m);
-  uint32_t parity = 0;
+  uint32_t parity = 0, copies = 0;
   bool ok = true;
-  for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x) {
+  for (int u = blockIdx.x; u < nunits && ok; u += gridDim.x, ++copies) {
     const TcUnit un = units[u];
+    if (threadIdx.x == 0) {
+      const uint32_t bar = smem_u32(m.bbar());
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                   "r"(uint32_t(kTcBfloats * 4))
+                   : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+          "[%3];\n" ::"r"(smem_u32(m.b_hi())),
+          "l"(B + int64_t(un.mat) * kTcBfloats), "r"(uint32_t(kTcBfloats * 4)), "r"(bar)
+          : "memory");
+    }
     float2* psi = state + (row_shift >= 0 ? (int64_t(un.row) << row_shift) : un.off);
-    ok = tc_apply5_chunks<kTrans>(psi, U + int64_t(un.mat) * 1024, un.tpack, un.tr, un.chunk0,
-                                  un.chunk0 + un.nchunks, 1, m, tmem, parity);
+    ok = tc_apply5_chunks<kTrans, true>(psi, nullptr, un.tpack, un.tr, un.chunk0,
+                                        un.chunk0 + un.nchunks, 1, m, tmem, parity,
+                                        copies & 1u);
+  }
+  if (!ok) {
+    // the failed unit's B copy may still be in flight (bounded wait)
+    bool done = false;
+    for (uint32_t it = 0; it < kTcSpin && !done; ++it)
+      done = mbar_try_wait(smem_u32(m.bbar()), (copies - 1u) & 1u);
   }
   tc_end(m, tmem, !ok, parity, status);
 }
@@ -804,16 +880,17 @@ cudaError_t launch_tc_fuse(const BatchDevice& b, const float2* mats, int row,
                            const TcBlock* blocks, const int32_t* members, int nblocks,
                            float2* U, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  tc_fuse_kernel<<<nblocks, 32, 0, s>>>(b, mats, row, nullptr, blocks, members, nblocks, U);
+  tc_fuse_kernel<<<nblocks, 32, 0, s>>>(b, mats, row, blocks, members, nblocks, U);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc_fuse_rows(const BatchDevice& b, const float2* mats,
-                                const int32_t* block_rows, const TcBlock* blocks,
-                                const int32_t* members, int nblocks, float2* U,
-                                cudaStream_t s) {
+size_t tc_b_floats() { return size_t(kTcBfloats); }
+
+cudaError_t launch_tc_fuse_b(const BatchDevice& b, const float2* mats,
+                             const int32_t* block_rows, const TcBlock* blocks,
+                             const int32_t* members, int nblocks, float* B, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  tc_fuse_kernel<<<nblocks, 32, 0, s>>>(b, mats, 0, block_rows, blocks, members, nblocks, U);
+  tc_fuse_b_kernel<<<nblocks, 32, 0, s>>>(b, mats, block_rows, blocks, members, nblocks, B);
   return cudaGetLastError();
 }
 
@@ -906,9 +983,10 @@ int tc_unit_geometry(const TcBlock& blk, int n, uint32_t* tpack, TcTrans* tr) {
   return tc_transposed_geometry(blk, n, tr) ? 1 : 0;
 }
 
-cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float2* U,
+cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float* B,
                                    const TcUnit* units, int nunits, bool trans, int* status,
                                    int grid, cudaStream_t s) {
+  if (reinterpret_cast<uintptr_t>(B) % 16 != 0) return cudaErrorInvalidValue;
   if (nunits <= 0) return cudaSuccess;
   if (grid > nunits) grid = nunits;
   if (grid < 1) grid = 1;
@@ -918,10 +996,10 @@ cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float2* U
                                        int(kTcSmem));
   if (e != cudaSuccess) return e;
   if (trans)
-    tc_apply5_units_kernel<true><<<grid, kTcRows, kTcSmem, s>>>(state, row_shift, U, units,
+    tc_apply5_units_kernel<true><<<grid, kTcRows, kTcSmem, s>>>(state, row_shift, B, units,
                                                                 nunits, status);
   else
-    tc_apply5_units_kernel<false><<<grid, kTcRows, kTcSmem, s>>>(state, row_shift, U, units,
+    tc_apply5_units_kernel<false><<<grid, kTcRows, kTcSmem, s>>>(state, row_shift, B, units,
                                                                  nunits, status);
   return cudaGetLastError();
 }
