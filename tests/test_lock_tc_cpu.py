@@ -1,9 +1,11 @@
 """The schedule of lockstep rows on tensor-core blocks, built on the host when
 a batch is created (no GPU): every lockstep row with a 5-qubit plan
-contributes its plan's blocks, and every block one unit per 16 chunks of
-128 groups of its row's state; the default, the per-qubit-count policy (2:
-tensor-core blocks, 1: tile passes) and the tensor-core switch decide which
-rows take them; a row whose gate spans six bits keeps its tile passes."""
+contributes its plan's blocks; launch q of a variant (direct, or transposed
+for blocks with a target below bit 5) covers block q of every such row, in
+units of up to 16 chunks of 128 groups, fewer when the launch would have
+under 2048 units; the default, the per-qubit-count policy (2: tensor-core
+blocks, 1: tile passes) and the tensor-core switch decide which rows take
+them; a row whose gate spans six bits keeps its tile passes."""
 
 import numpy as np
 
@@ -41,13 +43,18 @@ class _Settings:
 
 
 def _expected(b, nqs, rows):
-    blocks = units = 0
-    for r in rows:
-        plan = _native.tc_plan(b._h, r, np.zeros(0, np.float32))
-        assert plan is not None
-        chunks = 2 ** (nqs[r] - 12)
-        blocks += len(plan)
-        units += len(plan) * -(-chunks // 16)
+    plans = {r: _native.tc_plan(b._h, r, np.zeros(0, np.float32)) for r in rows}
+    assert all(p is not None for p in plans.values())
+    blocks = sum(len(p) for p in plans.values())
+    units = 0
+    for q in range(max(len(p) for p in plans.values())):
+        for trans in (False, True):
+            chunks = [2 ** (nqs[r] - 12) for r, p in plans.items()
+                      if q < len(p) and (p[q][0][0] < 5) == trans]
+            per = 16
+            while per > 1 and sum(chunks) // per < 2048:
+                per //= 2
+            units += sum(-(-c // per) for c in chunks)
     return blocks, units
 
 
