@@ -427,15 +427,15 @@ def batch_lock_rows(handle):
     return int(f(handle)), int(g(handle))
 
 
-def set_lock_tc(on):
+def set_lock_tc(mode):
     """Lockstep rows of batches created from now on run their gates as
-    5-qubit tensor-core blocks (True, the default) or as tile passes
-    (False), unless a per-qubit-count policy says otherwise.  Returns the
-    previous setting."""
+    5-qubit tensor-core blocks (1 or True), as tile passes (0 or False), or
+    as blocks from 18 qubits (2, the default), unless a per-qubit-count
+    policy says otherwise.  Returns the previous setting."""
     f = lib().tfqg_internal_set_lock_tc
     f.argtypes = [ctypes.c_int]
     f.restype = ctypes.c_int
-    return bool(f(1 if on else 0))
+    return int(f(int(mode)))
 
 
 def batch_lock_tc(handle):

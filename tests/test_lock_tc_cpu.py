@@ -3,9 +3,9 @@ a batch is created (no GPU): every lockstep row with a 5-qubit plan
 contributes its plan's blocks; launch q of a variant (direct, or transposed
 for blocks with a target below bit 5) covers block q of every such row, in
 units of up to 16 chunks of 128 groups, fewer when the launch would have
-under 2048 units; the default, the per-qubit-count policy (2: tensor-core
-blocks, 1: tile passes) and the tensor-core switch decide which rows take
-them; a row whose gate spans six bits keeps its tile passes."""
+under 2048 units; the default (blocks from 18 qubits), the
+per-qubit-count policy (2: tensor-core blocks, 1: tile passes) and the
+tensor-core switch decide which rows take them; a row whose gate spans six bits keeps its tile passes."""
 
 import numpy as np
 
@@ -82,6 +82,10 @@ def test_default_and_policy_choose_the_rows():
         autotune.set_row_policy(18, lock=1)
         b = ops.Batch(progs, [], None)
         assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [0, 3])
+        autotune.reset()
+        _native.set_lock_tc(2)  # the default: blocks from 18 qubits
+        b = ops.Batch(progs, [], None)
+        assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [1, 2])
         _native.set_tensor_core_gates(0)
         b = ops.Batch(progs, [], None)
         assert _native.batch_lock_rows(b._h)[0] == 4
