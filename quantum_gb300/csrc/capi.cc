@@ -178,6 +178,10 @@ bool fuse_for(int n, bool dflt) {
 // on blocks against 8.7 ms on tile passes; at 17 qubits 5.1 against 4.7.
 std::atomic<int> g_lock_tc{2};
 constexpr int kLockTcMinQubits = 18;
+// Units of the lockstep tensor-core launches (kernels.h kTcUnitChunks,
+// kTcUnitTarget), settable for measurements.
+std::atomic<int64_t> g_tc_unit_chunks{kTcUnitChunks};
+std::atomic<int64_t> g_tc_unit_target{kTcUnitTarget};
 
 // Forward passes of wide rows as 5-bit fused blocks on the tensor cores
 // (tc_gates.cu) instead of tile passes on the FP32 pipe: 0 never, 1 always,
@@ -505,8 +509,8 @@ void build_lock_schedule(tfqg_batch* b) {
         }
         // units of up to kTcUnitChunks chunks, fewer when the launch would
         // otherwise have too few units to spread over the GPU
-        int64_t per = kTcUnitChunks;
-        while (per > 1 && total / per < kTcUnitTarget) per >>= 1;
+        int64_t per = g_tc_unit_chunks.load();
+        while (per > 1 && total / per < g_tc_unit_target.load()) per >>= 1;
         for (auto& ru : rows_in)
           for (int64_t c = 0; c < ru.second; c += per) {
             ru.first.chunk0 = c;
@@ -2526,6 +2530,13 @@ int tfqg_internal_set_row_policy(int n, int fuse, int lock) {
 // value.
 int tfqg_internal_set_lock_tc(int mode) {
   return g_lock_tc.exchange(mode < 0 || mode > 2 ? 2 : mode);
+}
+
+// Largest unit (chunks) and the units a lockstep tensor-core launch aims
+// for, for batches created from now on (<= 0 keeps the value).
+void tfqg_internal_set_tc_units(int64_t max_chunks, int64_t target) {
+  if (max_chunks > 0) g_tc_unit_chunks.store(max_chunks);
+  if (target > 0) g_tc_unit_target.store(target);
 }
 
 // Tensor-core blocks and units of a batch's lockstep rows (for tests).

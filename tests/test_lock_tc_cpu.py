@@ -3,7 +3,7 @@ a batch is created (no GPU): every lockstep row with a 5-qubit plan
 contributes its plan's blocks; launch q of a variant (direct, or transposed
 for blocks with a target below bit 5) covers block q of every such row, in
 units of up to 16 chunks of 128 groups, fewer when the launch would have
-under 2048 units; the default (blocks from 18 qubits), the
+under 512 units; the default (blocks from 18 qubits), the
 per-qubit-count policy (2: tensor-core blocks, 1: tile passes) and the
 tensor-core switch decide which rows take them; a row whose gate spans six bits keeps its tile passes."""
 
@@ -52,7 +52,7 @@ def _expected(b, nqs, rows):
             chunks = [2 ** (nqs[r] - 12) for r, p in plans.items()
                       if q < len(p) and (p[q][0][0] < 5) == trans]
             per = 16
-            while per > 1 and sum(chunks) // per < 2048:
+            while per > 1 and sum(chunks) // per < 512:
                 per //= 2
             units += sum(-(-c // per) for c in chunks)
     return blocks, units
