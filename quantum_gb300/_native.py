@@ -438,6 +438,30 @@ def set_lock_tc(mode):
     return int(f(int(mode)))
 
 
+def set_tc_lock_persistent(on):
+    """Lockstep tensor-core rows of later calls run as one persistent launch
+    per lockstep group (True, the default: CTAs take units from a queue,
+    each waiting for its row's earlier blocks) or as one launch per block
+    index and variant (False).  Returns the previous setting."""
+    f = lib().tfqg_internal_set_tc_lock_persistent
+    f.argtypes = [ctypes.c_int]
+    f.restype = ctypes.c_int
+    return bool(f(1 if on else 0))
+
+
+def batch_lock_punits(handle):
+    """The persistent form's units of a batch in queue order: an int64
+    array of rows (group, row slot, batch row, need, first chunk, chunks)."""
+    import numpy as np
+    f = lib().tfqg_internal_batch_lock_punits
+    f.argtypes = [c_void_p, c_void_p, ctypes.c_int64]
+    f.restype = ctypes.c_int64
+    n = f(handle, None, 0)
+    out = np.zeros((max(n, 1), 6), np.int64)
+    f(handle, out.ctypes.data, n)
+    return out[:n]
+
+
 def batch_lock_tc(handle):
     """(tensor-core blocks, kernel units) of a batch's lockstep rows."""
     f = lib().tfqg_internal_batch_lock_tc

@@ -105,6 +105,9 @@ struct tfqg_batch {
     LockLaunch tc_rows;
     int32_t tc_block_begin = 0, tc_block_count = 0;
     std::vector<TcLockLaunch> tc;
+    // the same units for the persistent form: [tcp_begin, +tcp_count) of
+    // tcl_punits, in queue order
+    int32_t tcp_begin = 0, tcp_count = 0;
   };
   std::vector<int32_t> lock_rows;
   std::vector<int32_t> order_lock;
@@ -117,7 +120,7 @@ struct tfqg_batch {
   std::vector<tfqg::LockItem> tcl_items;
   std::vector<tfqg::TcBlock> tcl_blocks;
   std::vector<int32_t> tcl_members, tcl_block_rows;
-  std::vector<tfqg::TcUnit> tcl_units;
+  std::vector<tfqg::TcUnit> tcl_units, tcl_punits;
   int max_grads = 0;
   int64_t total_gates = 0, total_grads = 0;
   bool any_fused = false;  // forward plans hold GK_FUSED gates
@@ -159,18 +162,19 @@ struct tfqg_batch {
   std::vector<uint8_t> tc_ran;  // the row's last forward call ran the blocks
   std::vector<int32_t> tc_sweeps;  // state sweeps (launches) of that call
   tfqg::DevBuf tc_tab, tc_mats, tc_status;
-  tfqg::DevBuf tcl_tab, tcl_mats;
+  tfqg::DevBuf tcl_tab, tcl_mats, tcl_sync;
   const tfqg::LockItem* d_tcl_items = nullptr;
   const tfqg::TcBlock* d_tcl_blocks = nullptr;
   const int32_t* d_tcl_members = nullptr;
   const int32_t* d_tcl_block_rows = nullptr;
   const tfqg::TcUnit* d_tcl_units = nullptr;
+  const tfqg::TcUnit* d_tcl_punits = nullptr;
   // gives every device buffer back to the pool (the device is synchronized)
   void release_buffers() noexcept {
     tfqg::DevBuf* all[] = {&tables,     &mats,     &dmats,     &work,   &counter,
                            &values,     &out,      &aux,       &aux2,   &wide_state,
                            &wide_acc,   &inner_tmp, &tc_tab,   &tc_mats, &tc_status,
-                           &lock_state, &lock_acc,  &tcl_tab,  &tcl_mats};
+                           &lock_state, &lock_acc,  &tcl_tab,  &tcl_mats, &tcl_sync};
     for (tfqg::DevBuf* d : all) d->release(true);
   }
   tfqg::BatchDevice bd;

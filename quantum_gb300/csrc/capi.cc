@@ -182,6 +182,9 @@ constexpr int kLockTcMinQubits = 18;
 // kTcUnitTarget), settable for measurements.
 std::atomic<int64_t> g_tc_unit_chunks{kTcUnitChunks};
 std::atomic<int64_t> g_tc_unit_target{kTcUnitTarget};
+// Lockstep tensor-core rows run as one persistent launch per group (1) or
+// one launch per block index and variant (0).
+std::atomic<int> g_tc_lock_persistent{1};
 
 // Forward passes of wide rows as 5-bit fused blocks on the tensor cores
 // (tc_gates.cu) instead of tile passes on the FP32 pipe: 0 never, 1 always,
@@ -520,6 +523,38 @@ void build_lock_schedule(tfqg_batch* b) {
         L.count = int32_t(b->tcl_units.size()) - L.begin;
         if (L.count) g.tc.push_back(L);
       }
+    // the persistent form's queue: block index, then row, then chunk; each
+    // unit waits for its row's units of the earlier blocks
+    g.tcp_begin = int32_t(b->tcl_punits.size());
+    {
+      std::vector<int32_t> row_units(j - i, 0), slot(j - i, 0);
+      for (size_t k = i, sl = size_t(g.tc_rows.begin); k < j; ++k)
+        if (tc[k]) slot[k - i] = int32_t(sl++);
+      const int64_t per = kTcUnitChunks;
+      for (size_t q = 0; q < max_blocks; ++q)
+        for (size_t k = i; k < j; ++k) {
+          if (!tc[k] || q >= tcb[k].size()) continue;
+          const int32_t row = b->lock_rows[k];
+          const int n = prog(row).n;
+          TcUnit u{};
+          const int v = tc_unit_geometry(tcb[k][q], n, &u.tpack, &u.tr);
+          if (v < 0) throw Error(kInternal, "tensor-core block outside its row's qubits");
+          if (v) u.tpack |= kTcUnitTrans;
+          u.off = off[k - i];
+          u.row = row;
+          u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
+          u.slot = slot[k - i];
+          u.need = row_units[k - i];
+          const int64_t nch = int64_t(1) << (n - kTcBits - 7);
+          for (int64_t c = 0; c < nch; c += per) {
+            u.chunk0 = c;
+            u.nchunks = int32_t(std::min<int64_t>(per, nch - c));
+            b->tcl_punits.push_back(u);
+          }
+          row_units[k - i] += int32_t((nch + per - 1) / per);
+        }
+    }
+    g.tcp_count = int32_t(b->tcl_punits.size()) - g.tcp_begin;
     b->lock_groups.push_back(std::move(g));
     i = j;
   }
@@ -1292,6 +1327,7 @@ void tcl_prepare(tfqg_batch* b, cudaStream_t s) {
   const size_t o_members = put(&blob, b->tcl_members);
   const size_t o_rows = put(&blob, b->tcl_block_rows);
   const size_t o_units = put(&blob, b->tcl_units);
+  const size_t o_punits = put(&blob, b->tcl_punits);
   blob.resize(align256(blob.size()));
   b->tcl_tab.reserve(blob.size(), b->device);
   unsigned char* base = static_cast<unsigned char*>(b->tcl_tab.p);
@@ -1302,6 +1338,9 @@ void tcl_prepare(tfqg_batch* b, cudaStream_t s) {
   b->d_tcl_members = reinterpret_cast<const int32_t*>(base + o_members);
   b->d_tcl_block_rows = reinterpret_cast<const int32_t*>(base + o_rows);
   b->d_tcl_units = reinterpret_cast<const TcUnit*>(base + o_units);
+  b->d_tcl_punits = reinterpret_cast<const TcUnit*>(base + o_punits);
+  // persistent form: a queue counter per group, then a count per row
+  b->tcl_sync.reserve((b->lock_groups.size() + b->tcl_items.size()) * sizeof(int), b->device);
   b->tcl_mats.reserve(std::max<size_t>(b->tcl_blocks.size(), 1) * tc_b_floats() * sizeof(float),
                       b->device);
   b->tc_status.reserve(sizeof(int), b->device);
@@ -1360,6 +1399,13 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
     Bops = static_cast<float*>(b->tcl_mats.p);
     tgrid = tc_grid(dev);
   }
+  const bool persistent = any_tc && g_tc_lock_persistent.load() != 0;
+  int* queues = persistent ? static_cast<int*>(b->tcl_sync.p) : nullptr;
+  int* done = persistent ? queues + b->lock_groups.size() : nullptr;
+  if (persistent)
+    TFQG_CUDA(cudaMemsetAsync(queues, 0,
+                              (b->lock_groups.size() + b->tcl_items.size()) * sizeof(int), s));
+  size_t gi = 0;
   // tensor-core rows write their states in place: the arena, or the output
   // rows of a state call
   float2* tc_state = mode == kModeState ? a->out_state : state;
@@ -1372,9 +1418,14 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
                                  Bops + int64_t(g.tc_block_begin) * int64_t(tc_b_floats()), s));
       TFQG_CUDA(launch_lock_zero(tc_state, row_shift, b->d_tcl_items + g.tc_rows.begin,
                                  g.tc_rows.count, g.tc_rows.ntiles, sms * 8, s));
-      for (const auto& L : g.tc)
-        TFQG_CUDA(launch_tc_apply5_units(tc_state, row_shift, Bops, b->d_tcl_units + L.begin,
-                                         L.count, L.trans, st, tgrid, s));
+      if (persistent)
+        TFQG_CUDA(launch_tc_lock_persistent(tc_state, row_shift, Bops,
+                                            b->d_tcl_punits + g.tcp_begin, g.tcp_count,
+                                            queues + gi, done, st, tgrid, s));
+      else
+        for (const auto& L : g.tc)
+          TFQG_CUDA(launch_tc_apply5_units(tc_state, row_shift, Bops, b->d_tcl_units + L.begin,
+                                           L.count, L.trans, st, tgrid, s));
       // test hook: a captured call records an injected status on the
       // device, where a timed-out kernel would have set it
       if (capturing && g_tc_status_injected.load() != 0)
@@ -1401,6 +1452,7 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
     if (capturing && g.tc_rows.count)
       TFQG_CUDA(launch_lock_tc_poison(bd, *a, mode, b->d_tcl_items + g.tc_rows.begin,
                                       g.tc_rows.count, st, s));
+    ++gi;
   }
   if (any_tc && !capturing) check_tc_status(b, s);
 }
@@ -2045,7 +2097,7 @@ std::vector<void*> batch_buffers(tfqg_batch* b) {
   return {b->tables.p,     b->mats.p,      b->dmats.p,     b->work.p,     b->counter.p,
           b->values.p,     b->out.p,       b->aux.p,       b->aux2.p,     b->wide_state.p,
           b->wide_acc.p,   b->tc_tab.p,    b->tc_mats.p,   b->tc_status.p, b->lock_state.p,
-          b->lock_acc.p,   b->tcl_tab.p,   b->tcl_mats.p};
+          b->lock_acc.p,   b->tcl_tab.p,   b->tcl_mats.p,  b->tcl_sync.p};
 }
 
 int run_forward(tfqg_batch* b, int what, const float* values, int32_t num_samples,
@@ -2532,6 +2584,13 @@ int tfqg_internal_set_lock_tc(int mode) {
   return g_lock_tc.exchange(mode < 0 || mode > 2 ? 2 : mode);
 }
 
+// Lockstep tensor-core rows of later calls run as one persistent launch per
+// group (1) or one launch per block index and variant (0); returns the
+// previous setting.
+int tfqg_internal_set_tc_lock_persistent(int on) {
+  return g_tc_lock_persistent.exchange(on ? 1 : 0);
+}
+
 // Largest unit (chunks) and the units a lockstep tensor-core launch aims
 // for, for batches created from now on (<= 0 keeps the value).
 void tfqg_internal_set_tc_units(int64_t max_chunks, int64_t target) {
@@ -2544,6 +2603,24 @@ int64_t tfqg_internal_batch_lock_tc(const tfqg_batch* b, int64_t* units) {
   if (!b) return -1;
   if (units) *units = int64_t(b->tcl_units.size());
   return int64_t(b->tcl_blocks.size());
+}
+
+// The persistent form's units in queue order, 6 values each (group, row
+// slot, batch row, need, first chunk, chunks), at most `max` of them;
+// returns their number.
+int64_t tfqg_internal_batch_lock_punits(const tfqg_batch* b, int64_t* out, int64_t max) {
+  if (!b) return -1;
+  int64_t k = 0;
+  for (size_t gi = 0; gi < b->lock_groups.size(); ++gi) {
+    const auto& g = b->lock_groups[gi];
+    for (int32_t u = g.tcp_begin; u < g.tcp_begin + g.tcp_count; ++u, ++k) {
+      if (k >= max || !out) continue;
+      const TcUnit& t = b->tcl_punits[size_t(u)];
+      const int64_t v[6] = {int64_t(gi), t.slot, t.row, t.need, t.chunk0, t.nchunks};
+      for (int i = 0; i < 6; ++i) out[6 * k + i] = v[i];
+    }
+  }
+  return k;
 }
 
 // Qubit count from which streamed rows of batches created from now on run in

@@ -269,6 +269,11 @@ cudaError_t launch_tc_sweep2(float2* psi, int n, const float2* U0, const float2*
 // fused matrix (index `mat` into the matrices buffer), its packed targets
 // and, for the transposed variant, its chunk geometry.  Units of one launch
 // all take the same variant.
+// In the persistent form (one launch per group, see
+// launch_tc_lock_persistent) a unit also carries the transposed-variant flag
+// (tpack bit 31), its row's slot among the batch's tensor-core rows and the
+// number of that row's units that must be done before it starts (those of
+// the row's earlier blocks).
 struct TcUnit {
   int64_t off;
   int64_t chunk0;
@@ -277,8 +282,11 @@ struct TcUnit {
   uint32_t tpack;
   uint32_t mat;
   TcTrans tr;
+  int32_t slot;
+  int32_t need;
 };
-static_assert(sizeof(TcUnit) == 56, "TcUnit layout");
+static_assert(sizeof(TcUnit) == 64, "TcUnit layout");
+constexpr uint32_t kTcUnitTrans = 1u << 31;
 // Chunks per unit: at most kTcUnitChunks (one bulk copy of the block's B
 // operands per unit), fewer where a launch would have fewer than
 // kTcUnitTarget units.  (On GB300, 128 random 18-qubit rows: 6.8 ms per
@@ -306,6 +314,14 @@ cudaError_t launch_tc_fuse_b(const BatchDevice& b, const float2* mats,
 cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float* B,
                                    const TcUnit* units, int nunits, bool trans, int* status,
                                    int grid, cudaStream_t s);
+// All units of a lockstep group in one launch: CTAs take units in queue
+// order from *queue (zeroed before the launch); a unit waits (bounded) until
+// done[slot] >= need, runs, then counts itself in done[slot] (zeroed before
+// the launch).  A timed-out wait sets *status and every CTA stops taking
+// units.
+cudaError_t launch_tc_lock_persistent(float2* state, int row_shift, const float* B,
+                                      const TcUnit* units, int nunits, int* queue, int* done,
+                                      int* status, int grid, cudaStream_t s);
 // |0...0> in every row of `rows` (chunks of 2^kLockChunkBits amplitudes
 // counted by the items' prefixes); states at arena + off, or at
 // state + (row << row_shift) when row_shift >= 0.

@@ -228,8 +228,10 @@ struct TcSmem {
     return reinterpret_cast<uint32_t*>(bar() + 1);
   }
   __device__ __forceinline__ int* timed_out() const { return reinterpret_cast<int*>(bar() + 2); }
-  // completion of the bulk copy of the B operands (units kernel)
+  // completion of the bulk copy of the B operands (units kernels)
   __device__ __forceinline__ uint64_t* bbar() const { return bar() + 3; }
+  // the unit a CTA of the persistent kernel takes next
+  __device__ __forceinline__ int* next_unit() const { return reinterpret_cast<int*>(bar() + 4); }
 };
 
 // mbarrier and timeout flag initialised, TMEM allocated; returns its base.
@@ -276,9 +278,10 @@ __device__ __forceinline__ void tc_end(const TcSmem& m, uint32_t tmem, bool fail
 // is the MMA mbarrier's phase, carried from call to call.  kBulkB: the B
 // operands arrive by a bulk copy that completes on m.bbar() in phase
 // parity `bpar` (U unused); the MMA-issuing thread waits for it before its
-// first MMAs.  Returns false when a wait timed out (the same value in every
-// thread of the CTA).
-template <bool kTrans, bool kBulkB>
+// first MMAs.  kCg: state loads bypass L1 (other CTAs of the same launch
+// wrote the state).  Returns false when a wait timed out (the same value in
+// every thread of the CTA).
+template <bool kTrans, bool kBulkB, bool kCg = false>
 __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
                                                  const float2* __restrict__ U, uint32_t tpack,
                                                  const TcTrans& tr, int64_t chunk,
@@ -343,7 +346,8 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
     const float2* src = psi + chunk_base(c) + dep_t;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
-      raw[i] = __ldcs(reinterpret_cast<const float4*>(src + tr_dep(uint32_t(256 * i), tr.cb)));
+      raw[i] = kCg ? __ldcg(reinterpret_cast<const float4*>(src + tr_dep(uint32_t(256 * i), tr.cb)))
+                   : __ldcs(reinterpret_cast<const float4*>(src + tr_dep(uint32_t(256 * i), tr.cb)));
   };
   // registers -> swizzled staging slots (transposed variant)
   auto stage_raw = [&]() {
@@ -363,7 +367,7 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
     } else {
       const float2* src = psi + group_base(chunk * kTcRows + tid, t);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
+      for (int j = 0; j < 32; ++j) v[j] = kCg ? __ldcg(src + off[j]) : src[off[j]];
     }
   }
   bool failed = false, b_waited = !kBulkB;
@@ -435,7 +439,7 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
       } else {
         const float2* src = psi + group_base(next * kTcRows + tid, t);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = src[off[j]];
+        for (int j = 0; j < 32; ++j) v[j] = kCg ? __ldcg(src + off[j]) : src[off[j]];
       }
     }
     bool done = false;
@@ -540,6 +544,93 @@ tc_apply5_units_kernel(float2* __restrict__ state, int row_shift, const float* _
     bool done = false;
     for (uint32_t it = 0; it < kTcSpin && !done; ++it)
       done = mbar_try_wait(smem_u32(m.bbar()), (copies - 1u) & 1u);
+  }
+  tc_end(m, tmem, !ok, parity, status);
+}
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Persistent form: every unit of a lockstep group in one launch.  CTAs take
+// units from a queue counter in order (block index, row, chunk), so the
+// units a unit depends on (its row's earlier blocks) were taken before it
+// by running CTAs and always finish: a unit waits (bounded) until its row's
+// count of finished units reaches `need`, then runs, then publishes (every
+// thread fences its state stores, the CTA synchronizes, one thread adds 1
+// to the count).  State loads bypass L1, since other CTAs of the launch
+// wrote the state.  A timed-out wait sets *status; a CTA that sees *status
+// set takes no further units.
+__global__ void __launch_bounds__(kTcRows, 2)
+tc_lock_persistent_kernel(float2* __restrict__ state, int row_shift,
+                          const float* __restrict__ B, const TcUnit* __restrict__ units,
+                          int nunits, int* queue, int* done, int* status) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  const TcSmem m{tc_smem};
+  const uint32_t tmem = tc_begin(m);
+  uint32_t parity = 0, copies = 0;
+  bool ok = true;
+  for (;;) {
+    if (threadIdx.x == 0)
+      *m.next_unit() =
+          *reinterpret_cast<volatile int*>(status) != 0 ? nunits : atomicAdd(queue, 1);
+    __syncthreads();
+    const int u = *m.next_unit();
+    if (u >= nunits) break;
+    const TcUnit un = units[u];
+    if (threadIdx.x == 0 && un.need > 0) {
+      bool ready = false;
+      for (uint32_t it = 0; it < kTcSpin && !ready; ++it) {
+        ready = ld_acquire_gpu(done + un.slot) >= un.need;
+        if (!ready) {
+          if (*reinterpret_cast<volatile int*>(status) != 0) break;
+          __nanosleep(64);
+        }
+      }
+      if (!ready) atomicExch(m.timed_out(), 1);
+    }
+    __syncthreads();
+    if (*m.timed_out()) {
+      ok = false;
+      break;
+    }
+    if (threadIdx.x == 0) {
+      const uint32_t bar = smem_u32(m.bbar());
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                   "r"(uint32_t(kTcBfloats * 4))
+                   : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+          "[%3];\n" ::"r"(smem_u32(m.b_hi())),
+          "l"(B + int64_t(un.mat) * kTcBfloats), "r"(uint32_t(kTcBfloats * 4)), "r"(bar)
+          : "memory");
+    }
+    float2* psi = state + (row_shift >= 0 ? (int64_t(un.row) << row_shift) : un.off);
+    const uint32_t tpack = un.tpack & ~kTcUnitTrans;
+    if (un.tpack & kTcUnitTrans)
+      ok = tc_apply5_chunks<true, true, true>(psi, nullptr, tpack, un.tr, un.chunk0,
+                                              un.chunk0 + un.nchunks, 1, m, tmem, parity,
+                                              copies & 1u);
+    else
+      ok = tc_apply5_chunks<false, true, true>(psi, nullptr, tpack, un.tr, un.chunk0,
+                                               un.chunk0 + un.nchunks, 1, m, tmem, parity,
+                                               copies & 1u);
+    ++copies;
+    if (!ok) break;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(done + un.slot, 1);
+    }
+  }
+  if (!ok && copies > 0) {
+    // the failed unit's B copy may still be in flight (bounded wait)
+    bool fin = false;
+    for (uint32_t it = 0; it < kTcSpin && !fin; ++it)
+      fin = mbar_try_wait(smem_u32(m.bbar()), (copies - 1u) & 1u);
   }
   tc_end(m, tmem, !ok, parity, status);
 }
@@ -1001,6 +1092,22 @@ cudaError_t launch_tc_apply5_units(float2* state, int row_shift, const float* B,
   else
     tc_apply5_units_kernel<false><<<grid, kTcRows, kTcSmem, s>>>(state, row_shift, B, units,
                                                                  nunits, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_lock_persistent(float2* state, int row_shift, const float* B,
+                                      const TcUnit* units, int nunits, int* queue, int* done,
+                                      int* status, int grid, cudaStream_t s) {
+  if (nunits <= 0) return cudaSuccess;
+  if (reinterpret_cast<uintptr_t>(B) % 16 != 0) return cudaErrorInvalidValue;
+  if (grid > nunits) grid = nunits;
+  if (grid < 1) grid = 1;
+  cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(&tc_lock_persistent_kernel),
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(kTcSmem));
+  if (e != cudaSuccess) return e;
+  tc_lock_persistent_kernel<<<grid, kTcRows, kTcSmem, s>>>(state, row_shift, B, units, nunits,
+                                                           queue, done, status);
   return cudaGetLastError();
 }
 

@@ -1,6 +1,7 @@
 """Lockstep rows on tensor-core blocks: block k of every lockstep row in one
 launch (units of up to 16 chunks of one row each, direct and transposed
-variants in separate launches).  Rows of 15-19 qubits (streamed rows) against the complex128
+variants in separate launches), or all blocks of a lockstep group in one
+persistent launch whose units wait for their row's earlier blocks.  Rows of 15-19 qubits (streamed rows) against the complex128
 oracle and against the same rows on tile passes; a row whose gate spans six
 bits (no 5-qubit plan) keeps its tile passes inside a tensor-core group;
 deep circuits (many blocks per row, ragged block counts); a timed-out wait
@@ -21,17 +22,20 @@ pytestmark = pytest.mark.gpu
 NAMES = ["a", "b", "c"]
 
 
-@pytest.fixture
-def lock_tc():
-    """Lockstep from 14 qubits (streamed rows start at 15), no few-rows wide rule, groups of at most
-    2^20 amplitudes, tensor-core blocks on."""
+@pytest.fixture(params=[True, False], ids=["persistent", "per_block_launches"])
+def lock_tc(request):
+    """Lockstep from 14 qubits (streamed rows start at 15), no few-rows wide
+    rule, groups of at most 2^20 amplitudes, tensor-core blocks on; one
+    persistent launch per group or one launch per block index."""
     old = (_native.set_lock_min_qubits(14), _native.set_wide_few_rows(0),
-           _native.set_lock_arena_amps(1 << 20), _native.set_lock_tc(True))
+           _native.set_lock_arena_amps(1 << 20), _native.set_lock_tc(True),
+           _native.set_tc_lock_persistent(request.param))
     yield
     _native.set_lock_min_qubits(old[0])
     _native.set_wide_few_rows(old[1])
     _native.set_lock_arena_amps(old[2])
     _native.set_lock_tc(old[3])
+    _native.set_tc_lock_persistent(old[4])
 
 
 def _batch(nqs, depths, seed, six_bit_row=None):

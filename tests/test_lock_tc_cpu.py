@@ -100,3 +100,40 @@ def test_row_without_plan_keeps_tile_passes():
         assert _native.batch_lock_rows(b._h)[0] == 3
         assert _native.tc_plan(b._h, 1, np.zeros(0, np.float32)) is None
         assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [0, 2])
+
+
+def test_persistent_queue_order():
+    """The persistent form's queue: per row, units of one block after
+    another (16 chunks each, every chunk once per block); a unit needs
+    exactly its row's units of earlier blocks, and all of them come before
+    it in the queue (so a waiting unit never waits on one not yet taken)."""
+    nqs = [15, 18, 6, 17, 20, 16]
+    progs = _programs(nqs, seed=3)
+    with _Settings():
+        old = _native.set_lock_arena_amps(1 << 19)  # several groups
+        try:
+            b = ops.Batch(progs, [], None)
+        finally:
+            _native.set_lock_arena_amps(old)
+        pu = _native.batch_lock_punits(b._h)
+        lock = [r for r, n in enumerate(nqs) if n >= 15]
+        blocks = {r: len(_native.tc_plan(b._h, r, np.zeros(0, np.float32))) for r in lock}
+        assert len(np.unique(pu[:, 0])) > 1
+        seen, row_of = {}, {}
+        for g, slot, row, need, c0, nch in pu:
+            assert row_of.setdefault(slot, row) == row
+            prev = seen.setdefault(slot, [])
+            # the units this one needs: its row's units of earlier blocks,
+            # all already in the queue
+            assert need == sum(1 for (nd, _, _) in prev if nd < need) <= len(prev)
+            prev.append((need, c0, nch))
+        # every row: its blocks x its chunks, 16 chunks per unit
+        assert sorted(row_of.values()) == lock
+        for slot, r in row_of.items():
+            chunks = 2 ** (nqs[r] - 12)
+            per_block = -(-chunks // 16)
+            assert len(seen[slot]) == blocks[r] * per_block
+            cover = {}
+            for need, c0, nch in seen[slot]:
+                cover.setdefault(need, []).extend(range(c0, c0 + nch))
+            assert all(sorted(v) == list(range(chunks)) for v in cover.values())
