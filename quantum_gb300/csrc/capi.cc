@@ -530,8 +530,14 @@ void build_lock_schedule(tfqg_batch* b) {
       std::vector<int32_t> row_units(j - i, 0), slot(j - i, 0);
       for (size_t k = i, sl = size_t(g.tc_rows.begin); k < j; ++k)
         if (tc[k]) slot[k - i] = int32_t(sl++);
-      const int64_t per = kTcUnitChunks;
-      for (size_t q = 0; q < max_blocks; ++q)
+      for (size_t q = 0; q < max_blocks; ++q) {
+        // units of up to kTcUnitChunks chunks, fewer where the block index
+        // has too few chunks over all rows to keep the GPU busy
+        int64_t level = 0;
+        for (size_t k = i; k < j; ++k)
+          if (tc[k] && q < tcb[k].size()) level += int64_t(1) << (prog(b->lock_rows[k]).n - kTcBits - 7);
+        int64_t per = g_tc_unit_chunks.load();
+        while (per > 1 && level / per < g_tc_unit_target.load()) per >>= 1;
         for (size_t k = i; k < j; ++k) {
           if (!tc[k] || q >= tcb[k].size()) continue;
           const int32_t row = b->lock_rows[k];
@@ -553,6 +559,7 @@ void build_lock_schedule(tfqg_batch* b) {
           }
           row_units[k - i] += int32_t((nch + per - 1) / per);
         }
+      }
     }
     g.tcp_count = int32_t(b->tcl_punits.size()) - g.tcp_begin;
     b->lock_groups.push_back(std::move(g));

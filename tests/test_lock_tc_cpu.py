@@ -104,9 +104,9 @@ def test_row_without_plan_keeps_tile_passes():
 
 def test_persistent_queue_order():
     """The persistent form's queue: per row, units of one block after
-    another (16 chunks each, every chunk once per block); a unit needs
-    exactly its row's units of earlier blocks, and all of them come before
-    it in the queue (so a waiting unit never waits on one not yet taken)."""
+    another (every chunk once per block); a unit needs exactly its row's
+    units of earlier blocks, and all of them come before it in the queue (so
+    a waiting unit never waits on one not yet taken)."""
     nqs = [15, 18, 6, 17, 20, 16]
     progs = _programs(nqs, seed=3)
     with _Settings():
@@ -127,12 +127,11 @@ def test_persistent_queue_order():
             # all already in the queue
             assert need == sum(1 for (nd, _, _) in prev if nd < need) <= len(prev)
             prev.append((need, c0, nch))
-        # every row: its blocks x its chunks, 16 chunks per unit
+        # every row: each of its blocks covers each of its chunks once
         assert sorted(row_of.values()) == lock
         for slot, r in row_of.items():
             chunks = 2 ** (nqs[r] - 12)
-            per_block = -(-chunks // 16)
-            assert len(seen[slot]) == blocks[r] * per_block
+            assert len({need for need, _, _ in seen[slot]}) == blocks[r]
             cover = {}
             for need, c0, nch in seen[slot]:
                 cover.setdefault(need, []).extend(range(c0, c0 + nch))
