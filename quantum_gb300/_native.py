@@ -430,7 +430,7 @@ def batch_lock_rows(handle):
 def set_lock_tc(mode):
     """Lockstep rows of batches created from now on run their gates as
     5-qubit tensor-core blocks (1 or True), as tile passes (0 or False), or
-    as blocks from 18 qubits (2, the default), unless a per-qubit-count
+    as blocks from 15 qubits (2, the default), unless a per-qubit-count
     policy says otherwise.  Returns the previous setting."""
     f = lib().tfqg_internal_set_lock_tc
     f.argtypes = [ctypes.c_int]

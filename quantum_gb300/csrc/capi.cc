@@ -174,10 +174,11 @@ bool fuse_for(int n, bool dflt) {
 // per block index over all the group's rows) or as tile passes, as their
 // qubit count's policy says; without one, g_lock_tc decides: 0 tile
 // passes, 1 blocks, 2 (default) blocks from kLockTcMinQubits qubits.  On
-// GB300, 128 random 18-qubit rows (depth 5-40, random pairs) take 8.0 ms
-// on blocks against 8.7 ms on tile passes; at 17 qubits 5.1 against 4.7.
+// GB300 an expectation call over 128 random rows (depth 5-40, random
+// pairs) takes 1.20 / 3.35 / 26.1 ms on blocks (one persistent launch)
+// against 1.40 / 4.7 / 43.5 ms on tile passes at 15 / 17 / 20 qubits.
 std::atomic<int> g_lock_tc{2};
-constexpr int kLockTcMinQubits = 18;
+constexpr int kLockTcMinQubits = 15;
 // Units of the lockstep tensor-core launches (kernels.h kTcUnitChunks,
 // kTcUnitTarget), settable for measurements.
 std::atomic<int64_t> g_tc_unit_chunks{kTcUnitChunks};
@@ -2585,8 +2586,8 @@ int tfqg_internal_set_row_policy(int n, int fuse, int lock) {
 }
 
 // Lockstep rows of batches created from now on default to tile passes (0),
-// tensor-core blocks (1) or blocks from 18 qubits (2); returns the previous
-// value.
+// tensor-core blocks (1) or blocks from kLockTcMinQubits qubits (2);
+// returns the previous value.
 int tfqg_internal_set_lock_tc(int mode) {
   return g_lock_tc.exchange(mode < 0 || mode > 2 ? 2 : mode);
 }

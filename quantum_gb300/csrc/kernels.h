@@ -289,11 +289,11 @@ static_assert(sizeof(TcUnit) == 64, "TcUnit layout");
 constexpr uint32_t kTcUnitTrans = 1u << 31;
 // Chunks per unit: at most kTcUnitChunks (one bulk copy of the block's B
 // operands per unit), fewer where a launch would have fewer than
-// kTcUnitTarget units.  (On GB300, 128 random 18-qubit rows: 6.8 ms per
-// call with these values, 7.5 ms with a target of 2048 units, 8.3 ms with
-// one-chunk units.)
+// kTcUnitTarget units.  (On GB300, 128 random 17-qubit rows in one
+// persistent launch: 3.35 ms per call with these values, 3.57 ms with a
+// target of 512 units, 5.05 ms with 2048.)
 constexpr int kTcUnitChunks = 16;
-constexpr int64_t kTcUnitTarget = 512;
+constexpr int64_t kTcUnitTarget = 256;
 // Targets of `blk` packed 5 bits each and the variant (1 transposed, 0
 // direct, with its geometry in *tr), or -1 when the block does not fit a
 // 2^n state.

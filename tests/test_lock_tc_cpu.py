@@ -3,7 +3,7 @@ a batch is created (no GPU): every lockstep row with a 5-qubit plan
 contributes its plan's blocks; launch q of a variant (direct, or transposed
 for blocks with a target below bit 5) covers block q of every such row, in
 units of up to 16 chunks of 128 groups, fewer when the launch would have
-under 512 units; the default (blocks from 18 qubits), the
+under 256 units; the default (blocks from 15 qubits), the
 per-qubit-count policy (2: tensor-core blocks, 1: tile passes) and the
 tensor-core switch decide which rows take them; a row whose gate spans six bits keeps its tile passes."""
 
@@ -52,7 +52,7 @@ def _expected(b, nqs, rows):
             chunks = [2 ** (nqs[r] - 12) for r, p in plans.items()
                       if q < len(p) and (p[q][0][0] < 5) == trans]
             per = 16
-            while per > 1 and sum(chunks) // per < 512:
+            while per > 1 and sum(chunks) // per < 256:
                 per //= 2
             units += sum(-(-c // per) for c in chunks)
     return blocks, units
@@ -83,9 +83,9 @@ def test_default_and_policy_choose_the_rows():
         b = ops.Batch(progs, [], None)
         assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [0, 3])
         autotune.reset()
-        _native.set_lock_tc(2)  # the default: blocks from 18 qubits
+        _native.set_lock_tc(2)  # the default: blocks from 15 qubits
         b = ops.Batch(progs, [], None)
-        assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [1, 2])
+        assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [0, 1, 2, 3])
         _native.set_tensor_core_gates(0)
         b = ops.Batch(progs, [], None)
         assert _native.batch_lock_rows(b._h)[0] == 4
