@@ -97,6 +97,7 @@ struct tfqg_batch {
   };
   struct LockGroup {
     int64_t arena_amps = 0;        // states of the group's rows
+    int64_t acc_terms = 0;         // measurement terms of its rows (each row its own)
     LockLaunch rows;               // one item per row (chunk prefix, offset)
     std::vector<LockLaunch> fwd, meas;  // fwd: rows on tile passes only
     // rows whose gates run as tensor-core blocks: one tcl_items entry per

@@ -423,16 +423,22 @@ void build_lock_schedule(tfqg_batch* b) {
       ++j;
     }
     std::vector<int64_t> off(j - i);
+    std::vector<int32_t> accb(j - i);
     g.rows.begin = int32_t(b->lock_items.size());
     int64_t o = 0, chunks = 0;
     for (size_t k = i; k < j; ++k) {
       const int32_t row = b->lock_rows[k];
+      const DevRow& r = b->rows[size_t(row)];
       const int n = prog(row).n;
       off[k - i] = o;
-      b->lock_items.push_back(LockItem{row, 0u, chunks, o, n, 0});
+      accb[k - i] = int32_t(g.acc_terms);
+      if (r.meas_begin < r.meas_end)
+        g.acc_terms += b->meas[r.meas_end - 1].end - b->meas[r.meas_begin].begin;
+      b->lock_items.push_back(LockItem{row, 0u, chunks, o, n, accb[k - i]});
       o += int64_t(1) << n;
       chunks += int64_t(1) << (n - kLockChunkBits);
     }
+    if (g.acc_terms > INT32_MAX) throw Error(kResourceExhausted, "too many measurement terms");
     g.rows.count = int32_t(j - i);
     g.rows.ntiles = chunks;
     uint32_t max_fwd = 0, max_meas = 0;
@@ -456,7 +462,8 @@ void build_lock_schedule(tfqg_batch* b) {
           const uint32_t count = meas ? r.meas_end - r.meas_begin
                                       : p.fwd_pass_end - p.fwd_pass_begin;
           if (q >= count) continue;
-          b->lock_items.push_back(LockItem{row, first + q, L.ntiles, off[k - i], p.n, 0});
+          b->lock_items.push_back(
+              LockItem{row, first + q, L.ntiles, off[k - i], p.n, accb[k - i]});
           L.ntiles += int64_t(1) << (p.n - kStreamTileBits);
         }
         L.count = int32_t(b->lock_items.size()) - L.begin;
@@ -1381,7 +1388,8 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
     state = static_cast<float2*>(b->lock_state.p);
   }
   double* acc = nullptr;
-  const size_t nwacc = 2 * b->meas_terms.size();
+  size_t nwacc = 0;  // term accumulators of the largest group (2 per term and row)
+  for (const auto& g : b->lock_groups) nwacc = std::max(nwacc, 2 * size_t(g.acc_terms));
   if (mode == kModeExpect) {
     b->lock_acc.reserve((nwacc + size_t(rows) * size_t(std::max<int64_t>(b->n_ops, 1))) *
                             sizeof(double),
@@ -1445,7 +1453,8 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
                                 mode == kModeState ? 1 : 0, grid, smem, state_amps, s));
     const LockItem* rws = items + g.rows.begin;
     if (mode == kModeExpect) {
-      if (nwacc) TFQG_CUDA(cudaMemsetAsync(acc, 0, nwacc * sizeof(double), s));
+      if (g.acc_terms)
+        TFQG_CUDA(cudaMemsetAsync(acc, 0, 2 * size_t(g.acc_terms) * sizeof(double), s));
       for (const auto& L : g.meas)
         TFQG_CUDA(launch_lock_measure(bd, *a, items + L.begin, L.count, L.ntiles, state, acc,
                                       mgrid, smem, state_amps, s));

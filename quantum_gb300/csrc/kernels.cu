@@ -421,8 +421,15 @@ __device__ __forceinline__ int lock_find(const LockItem* items, int nitems, int6
   return lo;
 }
 
+// First batch-wide measurement-term index of a row (0 for a row without
+// measurement passes).
+__device__ __forceinline__ int row_first_term(const BatchDevice& b, const DevRow& r) {
+  return r.meas_begin < r.meas_end ? int(b.meas[r.meas_begin].begin) : 0;
+}
+
 // Measurement pass items[i].pass of every row: each tile's term sums go to
-// wacc[2 * term + {0, 1}] (term: the batch-wide measurement-term index).
+// wacc[2 * (acc + t) + {0, 1}], t the term's index within its row's
+// measurement terms and acc the row's first accumulator.
 __global__ void __launch_bounds__(kWideThreads, 2)
 lock_measure_kernel(BatchDevice b, RunArgs a, const LockItem* items, int nitems,
                     int64_t ntiles, const float2* arena, double* wacc, int state_amps) {
@@ -448,7 +455,7 @@ lock_measure_kernel(BatchDevice b, RunArgs a, const LockItem* items, int nitems,
     __syncthreads();
     measure_tile(sm, nt, 1u << kTile, base, false);
     __syncthreads();
-    double* dst = wacc + 2 * int64_t(M.begin);
+    double* dst = wacc + 2 * (int64_t(it.acc) + (int64_t(M.begin) - row_first_term(b, rc.r)));
     for (int i = threadIdx.x; i < 2 * nt; i += blockDim.x)
       if (sm.macc[i] != 0.0) atomicAdd(dst + i, sm.macc[i]);
     __syncthreads();
@@ -459,7 +466,8 @@ lock_measure_kernel(BatchDevice b, RunArgs a, const LockItem* items, int nitems,
 __global__ void lock_expect_finalize_kernel(BatchDevice b, RunArgs a, const LockItem* rows,
                                             const double* wacc, double* acc) {
   const LockItem it = rows[blockIdx.x];
-  expect_finalize_body(b, a, it.row, wacc, 0, acc + int64_t(blockIdx.x) * b.num_ops);
+  expect_finalize_body(b, a, it.row, wacc + 2 * int64_t(it.acc),
+                       row_first_term(b, b.rows[it.row]), acc + int64_t(blockIdx.x) * b.num_ops);
 }
 
 // Sampling of lockstep rows uses chunks of 2^kLockChunkBits (kernels.h)

@@ -174,14 +174,17 @@ cudaError_t launch_wide_sample(const BatchDevice& b, const RunArgs& a, int row,
 // passes, the expectation finalize or the sampling, all over the group's
 // rows at once.  An item is one row of a launch: its pass (forward or
 // measurement), the global index of its first tile or chunk (prefix,
-// ascending over the items), its state offset in the arena and its qubits.
+// ascending over the items), its state offset in the arena, its qubits and
+// the first of its row's term accumulators in the group (acc: rows that
+// share a program and observables share their measurement passes, so the
+// sums are kept per row, not per measurement term).
 struct LockItem {
   int32_t row;
   uint32_t pass;
   int64_t prefix;
   int64_t off;
   int32_t n;
-  int32_t pad_;
+  int32_t acc;
 };
 static_assert(sizeof(LockItem) == 32, "LockItem layout");
 // Lockstep sampling sums |psi|^2 over chunks of 2^kLockChunkBits amplitudes

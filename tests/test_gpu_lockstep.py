@@ -101,3 +101,28 @@ def test_samples(lockstep):
             counts = np.bincount(bits_to_index(s[r], n), minlength=2 ** n)
             p, chi2, bins = chi2_pvalue(counts, probs[r][1], shots)
             assert p > 1e-3, (r, n, chi2, bins, p)
+
+
+def test_repeated_program_rows(lockstep):
+    """Rows with one program and one observable list (a batch of symbol
+    values for the same circuit) share their measurement passes; every row
+    still keeps its own term sums, in every lockstep group."""
+    rng = np.random.default_rng(4)
+    names = ["a", "b", "c"]
+    qs = S.GridQubit.rect(1, 17)
+    prog = S.serialize_circuit(random_circuit(qs, 4, rng, names, p_control=0.2))
+    ps = [random_paulisum(qs, rng) for _ in range(2)]
+    programs, psums = [prog] * 6, [ps] * 6
+    values = rng.uniform(-2, 2, size=(6, 3)).astype(np.float32)
+    b = ops.Batch(programs, names, psums)
+    rows, groups = _native.batch_lock_rows(b._h)
+    assert rows == 6 and groups >= 2, (rows, groups)
+    _check_path(b, lockstep)
+    got = b.expectation(values)
+    want = O.simulate_expectation(programs, names, values, psums)
+    assert np.ptp(want[:, 0]) > 1e-3  # the rows differ
+    np.testing.assert_allclose(got, want, atol=expectation_atol(psums), rtol=0)
+    R = 40000
+    got = b.sampled_expectation(values, np.full((6, 2), R, np.int32), seed=3)
+    bound = 5 * expectation_atol(psums, 1.0) / np.sqrt(R)
+    np.testing.assert_allclose(got, want, atol=bound, rtol=0)
