@@ -53,6 +53,10 @@ def parse():
                     help="c4: forward passes as 5-qubit fused blocks on the tensor cores "
                          "(split 3xTF32), one HBM sweep per block; auto (the library "
                          "default) for rows of 24 qubits and more, off: tile passes")
+    ap.add_argument("--c3-qubits", default=None,
+                    help="LO-HI: only the C3 rows of LO..HI qubits (a bucket of C3)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="C3 without the autotuner (the library's default plans)")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default): the headline expectation + adjoint line; "
                          "c1, c3, c4, c5: the other benchmark configurations, "
@@ -456,7 +460,14 @@ def run_config(args):
         units, unit = 32, "circuits/s"
     elif wl == "c3":
         w = workloads.uneven_batch(4096, 4, 20, 5, 40, seed=1)
-        units, unit = 4096, "circuits/s"
+        if args.c3_qubits:
+            lo, hi = (int(x) for x in args.c3_qubits.split("-"))
+            keep = [i for i, n in enumerate(w["n_per_row"]) if lo <= n <= hi]
+            w = dict(w, programs=[w["programs"][i] for i in keep],
+                     pauli_sums=[w["pauli_sums"][i] for i in keep],
+                     symbol_values=w["symbol_values"][keep],
+                     n_per_row=[w["n_per_row"][i] for i in keep])
+        units, unit = len(w["programs"]), "circuits/s"
     elif wl == "c4":
         gr, gc = (int(x) for x in args.c4_grid.split("x"))
         w = workloads.grid_fsim(gr, gc, 24, seed=1)
@@ -469,7 +480,7 @@ def run_config(args):
         __import__("quantum_gb300")._native.set_tensor_core_gates(
             {"auto": 2, "on": 1, "off": 0}[args.tensor_cores])
     tuned = None
-    if wl == "c3":
+    if wl == "c3" and not args.no_autotune:
         # the autotuner picks fusion width and tile schedule per qubit count
         # on this GPU (untimed, before the batch is built)
         from quantum_gb300 import autotune
@@ -554,7 +565,10 @@ def run_config(args):
             "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "dtype": "c64 (f32 state, f64 reductions)",
             "data": "synthetic (seeded)", "config": {"workload": wl, "what": CONFIGS[wl],
-                       **({"grid": args.c4_grid} if wl == "c4" else {})},
+                       **({"grid": args.c4_grid} if wl == "c4" else {}),
+                       **({"c3_qubits": args.c3_qubits} if wl == "c3" and args.c3_qubits
+                          else {}),
+                       **({"autotune": False} if wl == "c3" and args.no_autotune else {})},
             "host_parse_plan_s": parse_s, "clocks": clk,
             "specialized": sorted(__import__("quantum_gb300")._native.batch_specialization(
                 batch._h)[1])}
