@@ -653,6 +653,8 @@ def config_accuracy(wl, w, batch, vals, out):
         chi = []
         for lo, hi in ((4, 8), (9, 12), (13, 16), (17, 20)):
             idx = np.nonzero((ns >= lo) & (ns <= hi))[0]
+            if len(idx) == 0:
+                continue
             r = int(min(idx, key=lambda i: len(w["programs"][i])))
             n = int(ns[r])
             _, _, psi = F.simulate_state_row(w["programs"][r], [], z)

@@ -284,8 +284,8 @@ __device__ __forceinline__ void tc_end(const TcSmem& m, uint32_t tmem, bool fail
 template <bool kTrans, bool kBulkB, bool kCg = false>
 __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
                                                  const float2* __restrict__ U, uint32_t tpack,
-                                                 const TcTrans& tr, int64_t chunk,
-                                                 int64_t nchunk, int64_t step, const TcSmem& m,
+                                                 const TcTrans& tr, int chunk, int nchunk,
+                                                 int step, const TcSmem& m,
                                                  uint32_t tmem, uint32_t& parity,
                                                  uint32_t bpar = 0) {
   float* a_hi = m.a_hi();
@@ -340,9 +340,9 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
   float2 v[32];
   float4 raw[16];
   // chunk c starts at the index of its group 128 c (row and target bits 0)
-  auto chunk_base = [&](int64_t c) { return group_base(c * kTcRows, t); };
+  auto chunk_base = [&](int c) { return group_base(int64_t(c) * kTcRows, t); };
   // linear 16-byte loads of a chunk into registers (transposed variant)
-  auto load_raw = [&](int64_t c) {
+  auto load_raw = [&](int c) {
     const float2* src = psi + chunk_base(c) + dep_t;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
@@ -365,7 +365,7 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
     if (kTrans) {
       load_raw(chunk);
     } else {
-      const float2* src = psi + group_base(chunk * kTcRows + tid, t);
+      const float2* src = psi + group_base(int64_t(chunk) * kTcRows + tid, t);
 #pragma unroll
       for (int j = 0; j < 32; ++j) v[j] = kCg ? __ldcg(src + off[j]) : src[off[j]];
     }
@@ -432,12 +432,12 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
               smem_u32(m.bar()))
           : "memory");
     }
-    const int64_t next = chunk + step;
+    const int next = chunk + step;
     if (next < nchunk) {  // the next chunk's loads overlap the MMAs
       if (kTrans) {
         load_raw(next);
       } else {
-        const float2* src = psi + group_base(next * kTcRows + tid, t);
+        const float2* src = psi + group_base(int64_t(next) * kTcRows + tid, t);
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = kCg ? __ldcg(src + off[j]) : src[off[j]];
       }
@@ -478,7 +478,7 @@ __device__ __forceinline__ bool tc_apply5_chunks(float2* __restrict__ psi,
           __stcs(reinterpret_cast<float4*>(dst + tr_dep(uint32_t(256 * i), tr.cb)), x);
         }
       } else {
-        float2* dst = psi + group_base(chunk * kTcRows + tid, t);
+        float2* dst = psi + group_base(int64_t(chunk) * kTcRows + tid, t);
 #pragma unroll
         for (int i = 0; i < 32; ++i)
           dst[off[i]] = make_float2(__uint_as_float(d[2 * i]), __uint_as_float(d[2 * i + 1]));
@@ -501,9 +501,9 @@ tc_apply5_kernel(float2* __restrict__ psi, int n, const float2* __restrict__ U,
   const TcSmem m{tc_smem};
   const uint32_t tmem = tc_begin(m);
   uint32_t parity = 0;
-  const int64_t nchunk = int64_t(1) << (n - kTcBits - 7);
-  const bool ok = tc_apply5_chunks<kTrans, false>(psi, U, tpack, tr, blockIdx.x, nchunk,
-                                                  gridDim.x, m, tmem, parity);
+  const int nchunk = 1 << (n - kTcBits - 7);  // n <= 31: at most 2^19 chunks
+  const bool ok = tc_apply5_chunks<kTrans, false>(psi, U, tpack, tr, int(blockIdx.x), nchunk,
+                                                  int(gridDim.x), m, tmem, parity);
   tc_end(m, tmem, !ok, parity, status);
 }
 
@@ -535,8 +535,8 @@ tc_apply5_units_kernel(float2* __restrict__ state, int row_shift, const float* _
           : "memory");
     }
     float2* psi = state + (row_shift >= 0 ? (int64_t(un.row) << row_shift) : un.off);
-    ok = tc_apply5_chunks<kTrans, true>(psi, nullptr, un.tpack, un.tr, un.chunk0,
-                                        un.chunk0 + un.nchunks, 1, m, tmem, parity,
+    ok = tc_apply5_chunks<kTrans, true>(psi, nullptr, un.tpack, un.tr, int(un.chunk0),
+                                        int(un.chunk0) + un.nchunks, 1, m, tmem, parity,
                                         copies & 1u);
   }
   if (!ok) {
@@ -610,12 +610,12 @@ tc_lock_persistent_kernel(float2* __restrict__ state, int row_shift,
     float2* psi = state + (row_shift >= 0 ? (int64_t(un.row) << row_shift) : un.off);
     const uint32_t tpack = un.tpack & ~kTcUnitTrans;
     if (un.tpack & kTcUnitTrans)
-      ok = tc_apply5_chunks<true, true, true>(psi, nullptr, tpack, un.tr, un.chunk0,
-                                              un.chunk0 + un.nchunks, 1, m, tmem, parity,
+      ok = tc_apply5_chunks<true, true, true>(psi, nullptr, tpack, un.tr, int(un.chunk0),
+                                              int(un.chunk0) + un.nchunks, 1, m, tmem, parity,
                                               copies & 1u);
     else
-      ok = tc_apply5_chunks<false, true, true>(psi, nullptr, tpack, un.tr, un.chunk0,
-                                               un.chunk0 + un.nchunks, 1, m, tmem, parity,
+      ok = tc_apply5_chunks<false, true, true>(psi, nullptr, tpack, un.tr, int(un.chunk0),
+                                               int(un.chunk0) + un.nchunks, 1, m, tmem, parity,
                                                copies & 1u);
     ++copies;
     if (!ok) break;
