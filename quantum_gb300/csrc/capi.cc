@@ -186,9 +186,6 @@ std::atomic<int64_t> g_tc_unit_target{kTcUnitTarget};
 // Lockstep tensor-core rows run as one persistent launch per group (1) or
 // one launch per block index and variant (0).
 std::atomic<int> g_tc_lock_persistent{1};
-// The persistent queue takes rows in batches of at most this many
-// amplitudes through all their blocks (0: all the group's rows at once).
-std::atomic<int64_t> g_tc_lock_l2_amps{0};
 
 // Forward passes of wide rows as 5-bit fused blocks on the tensor cores
 // (tc_gates.cu) instead of tile passes on the FP32 pipe: 0 never, 1 always,
@@ -534,60 +531,42 @@ void build_lock_schedule(tfqg_batch* b) {
         L.count = int32_t(b->tcl_units.size()) - L.begin;
         if (L.count) g.tc.push_back(L);
       }
-    // the persistent form's queue: rows in batches whose states together
-    // stay under g_tc_lock_l2_amps (all rows in one batch when it is 0);
-    // per batch block index, then row, then chunk; each unit waits for its
-    // row's units of the earlier blocks, which come earlier in the queue
+    // the persistent form's queue: block index, then row, then chunk; each
+    // unit waits for its row's units of the earlier blocks
     g.tcp_begin = int32_t(b->tcl_punits.size());
     {
       std::vector<int32_t> row_units(j - i, 0), slot(j - i, 0);
       for (size_t k = i, sl = size_t(g.tc_rows.begin); k < j; ++k)
         if (tc[k]) slot[k - i] = int32_t(sl++);
-      const int64_t l2 = g_tc_lock_l2_amps.load();
-      size_t k0 = i;
-      while (k0 < j) {
-        size_t k1 = k0;
-        int64_t amps = 0;
-        size_t rb_blocks = 0;
-        while (k1 < j) {
-          const int64_t a = tc[k1] ? int64_t(1) << prog(b->lock_rows[k1]).n : 0;
-          if (l2 > 0 && k1 > k0 && amps + a > l2) break;
-          amps += a;
-          if (tc[k1]) rb_blocks = std::max(rb_blocks, tcb[k1].size());
-          ++k1;
-        }
-        for (size_t q = 0; q < rb_blocks; ++q) {
-          // units of up to kTcUnitChunks chunks, fewer where the block
-          // index has too few chunks over the rows to keep the GPU busy
-          int64_t level = 0;
-          for (size_t k = k0; k < k1; ++k)
-            if (tc[k] && q < tcb[k].size())
-              level += int64_t(1) << (prog(b->lock_rows[k]).n - kTcBits - 7);
-          int64_t per = g_tc_unit_chunks.load();
-          while (per > 1 && level / per < g_tc_unit_target.load()) per >>= 1;
-          for (size_t k = k0; k < k1; ++k) {
-            if (!tc[k] || q >= tcb[k].size()) continue;
-            const int32_t row = b->lock_rows[k];
-            const int n = prog(row).n;
-            TcUnit u{};
-            const int v = tc_unit_geometry(tcb[k][q], n, &u.tpack, &u.tr);
-            if (v < 0) throw Error(kInternal, "tensor-core block outside its row's qubits");
-            if (v) u.tpack |= kTcUnitTrans;
-            u.off = off[k - i];
-            u.row = row;
-            u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
-            u.slot = slot[k - i];
-            u.need = row_units[k - i];
-            const int64_t nch = int64_t(1) << (n - kTcBits - 7);
-            for (int64_t c = 0; c < nch; c += per) {
-              u.chunk0 = c;
-              u.nchunks = int32_t(std::min<int64_t>(per, nch - c));
-              b->tcl_punits.push_back(u);
-            }
-            row_units[k - i] += int32_t((nch + per - 1) / per);
+      for (size_t q = 0; q < max_blocks; ++q) {
+        // units of up to kTcUnitChunks chunks, fewer where the block index
+        // has too few chunks over all rows to keep the GPU busy
+        int64_t level = 0;
+        for (size_t k = i; k < j; ++k)
+          if (tc[k] && q < tcb[k].size()) level += int64_t(1) << (prog(b->lock_rows[k]).n - kTcBits - 7);
+        int64_t per = g_tc_unit_chunks.load();
+        while (per > 1 && level / per < g_tc_unit_target.load()) per >>= 1;
+        for (size_t k = i; k < j; ++k) {
+          if (!tc[k] || q >= tcb[k].size()) continue;
+          const int32_t row = b->lock_rows[k];
+          const int n = prog(row).n;
+          TcUnit u{};
+          const int v = tc_unit_geometry(tcb[k][q], n, &u.tpack, &u.tr);
+          if (v < 0) throw Error(kInternal, "tensor-core block outside its row's qubits");
+          if (v) u.tpack |= kTcUnitTrans;
+          u.off = off[k - i];
+          u.row = row;
+          u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
+          u.slot = slot[k - i];
+          u.need = row_units[k - i];
+          const int64_t nch = int64_t(1) << (n - kTcBits - 7);
+          for (int64_t c = 0; c < nch; c += per) {
+            u.chunk0 = c;
+            u.nchunks = int32_t(std::min<int64_t>(per, nch - c));
+            b->tcl_punits.push_back(u);
           }
+          row_units[k - i] += int32_t((nch + per - 1) / per);
         }
-        k0 = k1;
       }
     }
     g.tcp_count = int32_t(b->tcl_punits.size()) - g.tcp_begin;
@@ -2627,12 +2606,6 @@ int tfqg_internal_set_lock_tc(int mode) {
 // previous setting.
 int tfqg_internal_set_tc_lock_persistent(int on) {
   return g_tc_lock_persistent.exchange(on ? 1 : 0);
-}
-
-// Row batches of the persistent queue (amplitudes; 0: one batch), for
-// batches created from now on; returns the previous value.
-int64_t tfqg_internal_set_tc_lock_l2_amps(int64_t amps) {
-  return g_tc_lock_l2_amps.exchange(amps < 0 ? 0 : amps);
 }
 
 // Largest unit (chunks) and the units a lockstep tensor-core launch aims

@@ -7,10 +7,7 @@ under 256 units; the default (blocks from 15 qubits), the
 per-qubit-count policy (2: tensor-core blocks, 1: tile passes) and the
 tensor-core switch decide which rows take them; a row whose gate spans six bits keeps its tile passes."""
 
-import ctypes
-
 import numpy as np
-import pytest
 
 from quantum_gb300 import _native, autotune, ops
 from quantum_gb300 import serialize as S
@@ -105,26 +102,19 @@ def test_row_without_plan_keeps_tile_passes():
         assert _native.batch_lock_tc(b._h) == _expected(b, nqs, [0, 2])
 
 
-@pytest.mark.parametrize("l2_amps", [0, 1 << 18])
-def test_persistent_queue_order(l2_amps):
-    """The persistent form's queue (all of a group's rows at once, or rows
-    in batches of at most 2^18 amplitudes): per row, units of one block
-    after another (every chunk once per block); a unit needs exactly its
-    row's units of earlier blocks, and all of them come before it in the
-    queue (so a waiting unit never waits on one not yet taken)."""
-    nqs = [15, 18, 6, 17, 20, 16, 15, 15]
+def test_persistent_queue_order():
+    """The persistent form's queue: per row, units of one block after
+    another (every chunk once per block); a unit needs exactly its row's
+    units of earlier blocks, and all of them come before it in the queue (so
+    a waiting unit never waits on one not yet taken)."""
+    nqs = [15, 18, 6, 17, 20, 16]
     progs = _programs(nqs, seed=3)
-    f = _native.lib().tfqg_internal_set_tc_lock_l2_amps
-    f.argtypes = [ctypes.c_int64]
-    f.restype = ctypes.c_int64
     with _Settings():
         old = _native.set_lock_arena_amps(1 << 19)  # several groups
-        old_l2 = f(l2_amps)
         try:
             b = ops.Batch(progs, [], None)
         finally:
             _native.set_lock_arena_amps(old)
-            f(old_l2)
         pu = _native.batch_lock_punits(b._h)
         lock = [r for r, n in enumerate(nqs) if n >= 15]
         blocks = {r: len(_native.tc_plan(b._h, r, np.zeros(0, np.float32))) for r in lock}
