@@ -39,6 +39,14 @@
 // bits 4-11, chosen on the host so that the 32 groups of a warp fall on 16
 // distinct bank pairs (2 per pair, the minimum for 8-byte accesses) while
 // 16-byte accesses by consecutive lanes stay on distinct banks.
+//
+// Lockstep rows (many streamed states of 15-21 qubits) use the same chunk
+// loop (tc_apply5_chunks) on units, runs of up to 16 chunks of one row's
+// state under one block: tc_fuse_b_kernel writes every block's B operands
+// to global memory once per call, and a unit brings them into shared memory
+// with one bulk copy.  tc_lock_persistent_kernel runs all of a group's
+// units in one launch (a unit waits for its row's earlier blocks);
+// tc_apply5_units_kernel runs the units of one block index and variant.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
