@@ -168,8 +168,8 @@ struct tfqg_batch {
   const tfqg::TcBlock* d_tcl_blocks = nullptr;
   const int32_t* d_tcl_members = nullptr;
   const int32_t* d_tcl_block_rows = nullptr;
-  const tfqg::TcUnit* d_tcl_units = nullptr;
-  const tfqg::TcUnit* d_tcl_punits = nullptr;
+  const tfqg::TcUnit* d_tcl_units = nullptr;  // units of the uploaded form
+  bool tcl_persistent = false;                 // the uploaded form
   // gives every device buffer back to the pool (the device is synchronized)
   void release_buffers() noexcept {
     tfqg::DevBuf* all[] = {&tables,     &mats,     &dmats,     &work,   &counter,

@@ -1331,29 +1331,40 @@ void run_wide_adjoint(tfqg_batch* b, const BatchDevice& bd, RunArgs* a, cudaStre
   }
 }
 
-// Uploads the tensor-core tables of the lockstep rows (items, blocks,
-// members, block rows, units) once per device and sizes their fused-matrix
-// buffer.
-void tcl_prepare(tfqg_batch* b, cudaStream_t s) {
-  if (b->tcl_tab.p && b->tcl_tab.device == b->device) return;
+// The tensor-core tables of the lockstep rows as one blob (items, blocks,
+// members, block rows, then the units of the persistent form or of the
+// per-block-index launches) and the sections' offsets.
+struct TclOffsets {
+  size_t items, blocks, members, rows, units;
+};
+TclOffsets tcl_blob(const tfqg_batch* b, bool persistent, std::vector<unsigned char>* blob) {
+  TclOffsets o;
+  o.items = put(blob, b->tcl_items);
+  o.blocks = put(blob, b->tcl_blocks);
+  o.members = put(blob, b->tcl_members);
+  o.rows = put(blob, b->tcl_block_rows);
+  o.units = put(blob, persistent ? b->tcl_punits : b->tcl_units);
+  blob->resize(align256(blob->size()));
+  return o;
+}
+
+// Uploads the tensor-core tables of the lockstep rows for the form in use,
+// once per device and form, and sizes their fused-matrix buffer.
+void tcl_prepare(tfqg_batch* b, bool persistent, cudaStream_t s) {
+  if (b->tcl_tab.p && b->tcl_tab.device == b->device && b->tcl_persistent == persistent)
+    return;
   std::vector<unsigned char> blob;
-  const size_t o_items = put(&blob, b->tcl_items);
-  const size_t o_blocks = put(&blob, b->tcl_blocks);
-  const size_t o_members = put(&blob, b->tcl_members);
-  const size_t o_rows = put(&blob, b->tcl_block_rows);
-  const size_t o_units = put(&blob, b->tcl_units);
-  const size_t o_punits = put(&blob, b->tcl_punits);
-  blob.resize(align256(blob.size()));
+  const TclOffsets o = tcl_blob(b, persistent, &blob);
   b->tcl_tab.reserve(blob.size(), b->device);
   unsigned char* base = static_cast<unsigned char*>(b->tcl_tab.p);
   TFQG_CUDA(cudaMemcpyAsync(base, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
   TFQG_CUDA(cudaStreamSynchronize(s));  // blob is a temporary
-  b->d_tcl_items = reinterpret_cast<const LockItem*>(base + o_items);
-  b->d_tcl_blocks = reinterpret_cast<const TcBlock*>(base + o_blocks);
-  b->d_tcl_members = reinterpret_cast<const int32_t*>(base + o_members);
-  b->d_tcl_block_rows = reinterpret_cast<const int32_t*>(base + o_rows);
-  b->d_tcl_units = reinterpret_cast<const TcUnit*>(base + o_units);
-  b->d_tcl_punits = reinterpret_cast<const TcUnit*>(base + o_punits);
+  b->tcl_persistent = persistent;
+  b->d_tcl_items = reinterpret_cast<const LockItem*>(base + o.items);
+  b->d_tcl_blocks = reinterpret_cast<const TcBlock*>(base + o.blocks);
+  b->d_tcl_members = reinterpret_cast<const int32_t*>(base + o.members);
+  b->d_tcl_block_rows = reinterpret_cast<const int32_t*>(base + o.rows);
+  b->d_tcl_units = reinterpret_cast<const TcUnit*>(base + o.units);
   // persistent form: a queue counter per group, then a count per row
   b->tcl_sync.reserve((b->lock_groups.size() + b->tcl_items.size()) * sizeof(int), b->device);
   b->tcl_mats.reserve(std::max<size_t>(b->tcl_blocks.size(), 1) * tc_b_floats() * sizeof(float),
@@ -1405,17 +1416,17 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
   int* st = nullptr;
   float* Bops = nullptr;
   int tgrid = 0;
+  const bool persistent = any_tc && g_tc_lock_persistent.load() != 0;
   if (any_tc) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     TFQG_CUDA(cudaStreamIsCapturing(s, &cs));
     capturing = cs != cudaStreamCaptureStatusNone;
-    tcl_prepare(b, s);
+    tcl_prepare(b, persistent, s);
     st = static_cast<int*>(b->tc_status.p);
     TFQG_CUDA(cudaMemsetAsync(st, 0, sizeof(int), s));
     Bops = static_cast<float*>(b->tcl_mats.p);
     tgrid = tc_grid(dev);
   }
-  const bool persistent = any_tc && g_tc_lock_persistent.load() != 0;
   int* queues = persistent ? static_cast<int*>(b->tcl_sync.p) : nullptr;
   int* done = persistent ? queues + b->lock_groups.size() : nullptr;
   if (persistent)
@@ -1436,7 +1447,7 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
                                  g.tc_rows.count, g.tc_rows.ntiles, sms * 8, s));
       if (persistent)
         TFQG_CUDA(launch_tc_lock_persistent(tc_state, row_shift, Bops,
-                                            b->d_tcl_punits + g.tcp_begin, g.tcp_count,
+                                            b->d_tcl_units + g.tcp_begin, g.tcp_count,
                                             queues + gi, done, st, tgrid, s));
       else
         for (const auto& L : g.tc)
@@ -2749,12 +2760,19 @@ int tfqg_internal_forward_plan_gates(void* batch, int64_t row,
 
 int64_t tfqg_internal_batch_table_bytes(void* batch) {
   tfqg_batch* b = static_cast<tfqg_batch*>(batch);
-  size_t bytes = 0;
-  bytes += b->programs.size() * sizeof(DevProgram) + b->rows.size() * sizeof(DevRow);
-  bytes += b->gates.size() * sizeof(GateTemplate) + b->passes.size() * sizeof(DevPass);
-  bytes += b->ops.size() * sizeof(DevOp) + b->terms.size() * sizeof(DevTerm);
-  bytes += b->channels.size() * sizeof(DevChannel) + b->kraus.size() * sizeof(float2);
-  bytes += b->grad_cols.size() * sizeof(int32_t) + b->order.size() * sizeof(int32_t);
+  // every table a forward call uploads: the packed batch tables, the
+  // lockstep rows' tensor-core tables (the form in use) and the wide rows'
+  // tensor-core plans
+  std::vector<unsigned char> blob;
+  pack_tables(b, &blob);
+  size_t bytes = blob.size();
+  if (!b->tcl_units.empty()) {
+    blob.clear();
+    tcl_blob(b, g_tc_lock_persistent.load() != 0, &blob);
+    bytes += blob.size();
+  }
+  if (b->tc_planned)
+    bytes += align256(b->tc_blocks.size() * sizeof(TcBlock)) + b->tc_members.size() * 4;
   return int64_t(bytes);
 }
 
