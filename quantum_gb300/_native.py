@@ -377,6 +377,26 @@ def program_cache(on=None):
     return bool(prev), h.value, m.value
 
 
+def program_cache_capacity(nbytes=0):
+    """Capacity of the compiled-program cache in bytes (0 leaves it; the
+    default is TFQG_PROGRAM_CACHE_BYTES, else 1 GiB); returns the previous
+    capacity."""
+    f = lib().tfqg_internal_program_cache_bytes
+    f.argtypes = [ctypes.c_int64]
+    f.restype = ctypes.c_int64
+    return int(f(int(nbytes)))
+
+
+def program_cache_size():
+    """(entries, bytes) held by the compiled-program cache."""
+    f = lib().tfqg_internal_program_cache_size
+    f.argtypes = [ctypes.POINTER(ctypes.c_int64)]
+    f.restype = ctypes.c_int64
+    nb = ctypes.c_int64()
+    n = f(ctypes.byref(nb))
+    return int(n), nb.value
+
+
 def batch_fingerprint(handle):
     """FNV-1a hash of a batch's packed host tables."""
     f = lib().tfqg_internal_batch_fingerprint

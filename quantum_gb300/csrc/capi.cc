@@ -282,10 +282,29 @@ struct ProgramCacheEntry {
   std::unordered_map<std::string, int> index;
   size_t cost = 0;
   uint64_t stamp = 0;
+  // the 5-qubit tensor-core block plan of the program's gates, made when a
+  // batch first runs the program as a lockstep row on blocks
+  mutable std::once_flag tc_once;
+  mutable bool tc_ok = false;
+  mutable std::vector<TcBlock> tc_blocks;
+  mutable std::vector<int32_t> tc_members;
 };
 
-constexpr size_t kProgramCacheBytes = size_t(256) << 20;
-constexpr size_t kProgramCacheEntries = 2048;
+// Capacity: TFQG_PROGRAM_CACHE_BYTES (default 1 GiB; a batch of 4096 random
+// 20-qubit circuits of depth up to 40 takes about 500 MB) and 65536
+// entries.  A batch larger than the cache would miss on every call (its
+// programs evict one another in order).
+std::atomic<size_t> g_pc_cap{0};  // 0: not read from the environment yet
+size_t program_cache_bytes() {
+  size_t v = g_pc_cap.load();
+  if (v == 0) {
+    const char* e = getenv("TFQG_PROGRAM_CACHE_BYTES");
+    v = e && strtoull(e, nullptr, 10) > 0 ? size_t(strtoull(e, nullptr, 10)) : size_t(1) << 30;
+    g_pc_cap.store(v);
+  }
+  return v;
+}
+constexpr size_t kProgramCacheEntries = 65536;
 std::mutex g_pc_mu;
 std::unordered_multimap<uint64_t, std::shared_ptr<const ProgramCacheEntry>> g_pc;
 uint64_t g_pc_clock = 0;
@@ -328,17 +347,28 @@ void program_cache_insert(std::shared_ptr<ProgramCacheEntry> e) {
             (cp.fwd_ops.size() + cp.bwd_ops.size()) * sizeof(DevOp) +
             (cp.fwd_passes.size() + cp.bwd_passes.size()) * sizeof(DevPass) +
             e->index.size() * 48 + 256;
-  if (e->cost > kProgramCacheBytes / 4) return;
+  const size_t cap = program_cache_bytes();
+  if (e->cost > cap / 4) return;
   const uint64_t h = program_cache_hash(e->bytes.data(), e->bytes.size(), e->names, e->job,
                                         e->plan_key);
   std::lock_guard<std::mutex> lk(g_pc_mu);
-  while (!g_pc.empty() &&
-         (g_pc_bytes + e->cost > kProgramCacheBytes || g_pc.size() >= kProgramCacheEntries)) {
-    auto oldest = g_pc.begin();
-    for (auto it = g_pc.begin(); it != g_pc.end(); ++it)
-      if (it->second->stamp < oldest->second->stamp) oldest = it;
-    g_pc_bytes -= oldest->second->cost;
-    g_pc.erase(oldest);
+  if (!g_pc.empty() &&
+      (g_pc_bytes + e->cost > cap || g_pc.size() >= kProgramCacheEntries)) {
+    // evict the least recently used eighth of the entries (at least enough
+    // for the new one) in one pass
+    std::vector<std::pair<uint64_t, decltype(g_pc)::iterator>> by_age;
+    by_age.reserve(g_pc.size());
+    for (auto it = g_pc.begin(); it != g_pc.end(); ++it) by_age.emplace_back(it->second->stamp, it);
+    std::sort(by_age.begin(), by_age.end(),
+              [](const auto& a, const auto& b) { return a.first < b.first; });
+    const size_t quota = std::max<size_t>(1, by_age.size() / 8);
+    size_t k = 0;
+    for (; k < by_age.size() &&
+           (k < quota || g_pc_bytes + e->cost > cap || g_pc.size() >= kProgramCacheEntries);
+         ++k) {
+      g_pc_bytes -= by_age[k].second->second->cost;
+      g_pc.erase(by_age[k].second);
+    }
   }
   e->stamp = ++g_pc_clock;
   g_pc_bytes += e->cost;
@@ -390,25 +420,44 @@ void rethrow_first(const std::vector<std::exception_ptr>& errs) {
 // measurement pass m.  Rows on tensor-core blocks get their own item list
 // (tcl_items), their blocks and, per block index, the units of a direct and
 // a transposed launch.
-void build_lock_schedule(tfqg_batch* b) {
+void build_lock_schedule(
+    tfqg_batch* b, const std::vector<std::shared_ptr<const ProgramCacheEntry>>& entries) {
   const size_t nr = b->lock_rows.size();
   auto prog = [&](int32_t row) -> const DevProgram& {
     return b->programs[b->rows[size_t(row)].program];
   };
   // block plans of the rows that take the tensor cores (planned on the
-  // host's cores; a row without a plan stays on tile passes)
+  // host's cores, once per cached program; a row without a plan stays on
+  // tile passes)
   std::vector<std::vector<TcBlock>> tcb(nr);
   std::vector<std::vector<int32_t>> tcm(nr);
   std::vector<uint8_t> tc(nr, 0);
   parallel_for(nr, [&](size_t k) {
-    const DevProgram& p = prog(b->lock_rows[k]);
+    const int32_t pid = b->rows[size_t(b->lock_rows[k])].program;
+    const DevProgram& p = b->programs[size_t(pid)];
     if (!lock_tc_for(p.n)) return;
     try {
-      tc[k] = plan_tc_blocks(b->gates.data() + p.gate_begin, p.num_gates, p.n, &tcb[k],
-                             &tcm[k]) &&
-              !tcb[k].empty();
+      const ProgramCacheEntry* e = size_t(pid) < entries.size() ? entries[pid].get() : nullptr;
+      if (e) {
+        std::call_once(e->tc_once, [e]() {
+          e->tc_ok = plan_tc_blocks(e->cp.gates.data(), int(e->cp.gates.size()), e->cp.n,
+                                    &e->tc_blocks, &e->tc_members) &&
+                     !e->tc_blocks.empty();
+        });
+        if (e->tc_ok) {
+          tcb[k] = e->tc_blocks;
+          tcm[k] = e->tc_members;
+          tc[k] = 1;
+        }
+      } else {
+        tc[k] = plan_tc_blocks(b->gates.data() + p.gate_begin, p.num_gates, p.n, &tcb[k],
+                               &tcm[k]) &&
+                !tcb[k].empty();
+      }
     } catch (...) {
       tc[k] = 0;
+      tcb[k].clear();
+      tcm[k].clear();
     }
   });
   size_t i = 0;
@@ -766,6 +815,9 @@ void build_batch(tfqg_batch* b, const char* const* programs,
     });
     rethrow_first(compile_errs);
   }
+  // every program's cache entry (found, or made now), which also keeps the
+  // program's tensor-core block plan once made
+  std::vector<std::shared_ptr<const ProgramCacheEntry>> entries(cached);
   for (size_t pid = 0; pid < parsed.size(); ++pid) {
     if (inner && pair_of[pid] >= 0) continue;
     if (cached[pid]) continue;
@@ -782,6 +834,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       e->empty = parsed[pid].moments.empty();
       e->cp = compiled[pid];
       e->index = index[pid];
+      entries[pid] = e;
       program_cache_insert(std::move(e));
     }
   }
@@ -970,7 +1023,7 @@ void build_batch(tfqg_batch* b, const char* const* programs,
       b->max_streamed_n_lock = std::max(b->max_streamed_n_lock, int(p.n));
     }
   }
-  build_lock_schedule(b);
+  build_lock_schedule(b, entries);
   jit_assign_signatures(b);
   if (b->max_grads > 6144)
     throw Error(kResourceExhausted,
@@ -2391,6 +2444,21 @@ int tfqg_internal_program_cache(int on, int64_t* hits, int64_t* misses) {
   const int prev = g_pc_on.exchange(on ? 1 : 0);
   if (!on) program_cache_clear();
   return prev;
+}
+
+// Capacity of the compiled-program cache in bytes (0 keeps it); returns
+// the previous capacity.  Entries beyond it are evicted on the next insert.
+int64_t tfqg_internal_program_cache_bytes(int64_t bytes) {
+  const size_t prev = program_cache_bytes();
+  if (bytes > 0) g_pc_cap.store(size_t(bytes));
+  return int64_t(prev);
+}
+
+// Entries and bytes held by the compiled-program cache.
+int64_t tfqg_internal_program_cache_size(int64_t* bytes) {
+  std::lock_guard<std::mutex> lk(g_pc_mu);
+  if (bytes) *bytes = int64_t(g_pc_bytes);
+  return int64_t(g_pc.size());
 }
 
 // Gate fusion of forward plans on (1) or off (0) for batches created after

@@ -3,7 +3,10 @@
 A batch built from cached programs must have the same packed tables as one
 built from scratch; the key must cover the symbol-name order, the job kind
 and the fusion setting; invalid programs are never cached, so their errors
-repeat."""
+repeat; the cache stays within its capacity, evicting the least recently
+used entries, and a batch that fits hits on every program the second time;
+the tensor-core block plan kept in an entry gives the lockstep schedule
+that planning from scratch gives."""
 
 import numpy as np
 import pytest
@@ -88,3 +91,45 @@ def test_empty_program_cached_keeps_its_semantics(fresh_cache):
     ps = S.serialize_paulisum([(1.0, [(q[0], "Z")])])
     fps = {_fp([empty], [], [[ps]], ops.KIND_FORWARD) for _ in range(2)}
     assert len(fps) == 1
+
+
+def test_capacity_and_eviction(fresh_cache):
+    programs, names, psums = _inputs(seed=5, nqs=tuple(range(3, 15)) * 3)
+    old = _native.program_cache_capacity(1 << 16)
+    try:
+        b = ops.Batch(programs, names, psums)
+        b.close()
+        n, nbytes = _native.program_cache_size()
+        assert 0 < n < len(programs) and nbytes <= 1 << 16, (n, nbytes)
+        _native.program_cache_capacity(1 << 30)
+        b = ops.Batch(programs, names, psums)
+        b.close()
+        _, h0, m0 = _native.program_cache()
+        b = ops.Batch(programs, names, psums)
+        b.close()
+        _, h1, m1 = _native.program_cache()
+        assert (h1 - h0, m1 - m0) == (len(programs), 0)
+    finally:
+        _native.program_cache_capacity(old)
+
+
+def test_cached_tensor_core_plans_give_the_same_schedule(fresh_cache):
+    programs, names, psums = _inputs(seed=7, nqs=(15, 16, 17, 15))
+    old = (_native.set_lock_min_qubits(15), _native.set_wide_few_rows(0), _native.set_lock_tc(1))
+    try:
+        first = ops.Batch(programs, names, psums)   # plans, keeps them in the cache
+        again = ops.Batch(programs, names, psums)   # takes them from the cache
+        _native.program_cache(False)
+        fresh = ops.Batch(programs, names, psums)   # plans without a cache
+        want = _native.batch_lock_tc(fresh._h)
+        assert want[0] > 0
+        for b in (first, again):
+            assert _native.batch_lock_tc(b._h) == want
+            np.testing.assert_array_equal(_native.batch_lock_punits(b._h),
+                                          _native.batch_lock_punits(fresh._h))
+        for b in (first, again, fresh):
+            b.close()
+    finally:
+        _native.set_lock_min_qubits(old[0])
+        _native.set_wide_few_rows(old[1])
+        _native.set_lock_tc(old[2])
