@@ -850,47 +850,83 @@ void build_batch(tfqg_batch* b, const char* const* programs,
   }
 
   // 5. pack programs
-  // (a cached program is packed straight from its cache entry)
+  // (a cached program is packed straight from its cache entry): every
+  // program's table offsets first, then the copies on the host's cores
   b->programs.resize(compiled.size());
+  auto cp_of = [&](size_t pid) -> const CompiledProgram& {
+    return cached[pid] ? cached[pid]->cp : compiled[pid];
+  };
+  struct PackAt {
+    size_t grads, gates, channels, kraus, passes, ops;
+  };
+  std::vector<PackAt> at(compiled.size() + 1);
+  at[0] = PackAt{b->grad_cols.size(), b->gates.size(), b->channels.size(), b->kraus.size(),
+                 b->passes.size(), b->ops.size()};
   for (size_t pid = 0; pid < compiled.size(); ++pid) {
-    const CompiledProgram& cp = cached[pid] ? cached[pid]->cp : compiled[pid];
+    const CompiledProgram& cp = cp_of(pid);
+    size_t kr = 0;
+    for (const ChannelHost& ch : cp.channels) kr += ch.kraus.size() / 2;
+    at[pid + 1] = PackAt{at[pid].grads + cp.grad_col.size(), at[pid].gates + cp.gates.size(),
+                         at[pid].channels + cp.channels.size(), at[pid].kraus + kr,
+                         at[pid].passes + cp.fwd_passes.size() + cp.bwd_passes.size(),
+                         at[pid].ops + cp.fwd_ops.size() + cp.bwd_ops.size()};
+  }
+  const PackAt& total = at[compiled.size()];
+  if (total.gates > UINT32_MAX || total.ops > UINT32_MAX || total.passes > UINT32_MAX)
+    throw Error(kResourceExhausted, "the batch's gate tables exceed 2^32 entries");
+  b->grad_cols.resize(total.grads);
+  b->gates.resize(total.gates);
+  b->channels.resize(total.channels);
+  b->kraus.resize(total.kraus);
+  b->passes.resize(total.passes);
+  b->ops.resize(total.ops);
+  parallel_for(compiled.size(), [&](size_t pid) {
+    const CompiledProgram& cp = cp_of(pid);
+    const PackAt& o = at[pid];
     DevProgram& dp = b->programs[pid];
     memset(&dp, 0, sizeof(dp));
     dp.n = cp.empty() ? 0 : cp.n;
     dp.num_gates = int32_t(cp.gates.size());
     dp.num_grads = int32_t(cp.grad_col.size());
-    dp.grad_col_begin = uint32_t(b->grad_cols.size());
-    b->grad_cols.insert(b->grad_cols.end(), cp.grad_col.begin(), cp.grad_col.end());
-    dp.gate_begin = uint32_t(b->gates.size());
-    b->gates.insert(b->gates.end(), cp.gates.begin(), cp.gates.end());
-    dp.channel_begin = uint32_t(b->channels.size());
+    dp.grad_col_begin = uint32_t(o.grads);
+    std::copy(cp.grad_col.begin(), cp.grad_col.end(), b->grad_cols.begin() + o.grads);
+    dp.gate_begin = uint32_t(o.gates);
+    std::copy(cp.gates.begin(), cp.gates.end(), b->gates.begin() + o.gates);
+    dp.channel_begin = uint32_t(o.channels);
     dp.num_channels = int32_t(cp.channels.size());
-    for (const ChannelHost& ch : cp.channels) {
+    size_t kr = o.kraus;
+    for (size_t c = 0; c < cp.channels.size(); ++c) {
+      const ChannelHost& ch = cp.channels[c];
       DevChannel d = ch.dev;
-      d.kraus = uint32_t(b->kraus.size() / 4);
+      d.kraus = uint32_t(kr / 4);
       for (size_t k = 0; k < ch.kraus.size(); k += 2)
-        b->kraus.push_back(make_float2(float(ch.kraus[k]), float(ch.kraus[k + 1])));
-      b->channels.push_back(d);
+        b->kraus[kr++] = make_float2(float(ch.kraus[k]), float(ch.kraus[k + 1]));
+      b->channels[o.channels + c] = d;
     }
     dp.resident = cp.resident ? 1 : 0;
-    const uint32_t op_base = uint32_t(b->ops.size());
-    dp.fwd_pass_begin = uint32_t(b->passes.size());
+    size_t pass = o.passes;
+    const uint32_t op_base = uint32_t(o.ops);
+    dp.fwd_pass_begin = uint32_t(pass);
     for (DevPass ps : cp.fwd_passes) {
       ps.op_begin += op_base;
       ps.op_end += op_base;
-      b->passes.push_back(ps);
+      b->passes[pass++] = ps;
     }
-    dp.fwd_pass_end = uint32_t(b->passes.size());
-    b->ops.insert(b->ops.end(), cp.fwd_ops.begin(), cp.fwd_ops.end());
-    const uint32_t bop_base = uint32_t(b->ops.size());
-    dp.bwd_pass_begin = uint32_t(b->passes.size());
+    dp.fwd_pass_end = uint32_t(pass);
+    std::copy(cp.fwd_ops.begin(), cp.fwd_ops.end(), b->ops.begin() + o.ops);
+    const uint32_t bop_base = uint32_t(o.ops + cp.fwd_ops.size());
+    dp.bwd_pass_begin = uint32_t(pass);
     for (DevPass ps : cp.bwd_passes) {
       ps.op_begin += bop_base;
       ps.op_end += bop_base;
-      b->passes.push_back(ps);
+      b->passes[pass++] = ps;
     }
-    dp.bwd_pass_end = uint32_t(b->passes.size());
-    b->ops.insert(b->ops.end(), cp.bwd_ops.begin(), cp.bwd_ops.end());
+    dp.bwd_pass_end = uint32_t(pass);
+    std::copy(cp.bwd_ops.begin(), cp.bwd_ops.end(), b->ops.begin() + bop_base);
+  });
+  for (size_t pid = 0; pid < compiled.size(); ++pid) {
+    const CompiledProgram& cp = cp_of(pid);
+    const DevProgram& dp = b->programs[pid];
     if (dp.n > 0) {
       b->max_n = std::max(b->max_n, dp.n);
       if (cp.resident) b->max_resident_n = std::max(b->max_resident_n, dp.n);
