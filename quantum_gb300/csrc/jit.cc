@@ -21,6 +21,7 @@
 #include <unistd.h>
 
 #include <map>
+#include <unordered_map>
 #include <memory>
 #include <mutex>
 #include <sstream>
@@ -387,8 +388,16 @@ std::vector<char> nvrtc_compile(const std::string& src, std::string* info = null
 
 }  // namespace
 
+struct SignatureHash {
+  size_t operator()(const std::vector<uint32_t>& v) const {
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (const uint32_t x : v) h = (h ^ x) * 0x100000001b3ull;
+    return size_t(h ^ (h >> 29));
+  }
+};
+
 void jit_assign_signatures(tfqg_batch* b) {
-  std::map<std::vector<uint32_t>, int> ids;
+  std::unordered_map<std::vector<uint32_t>, int, SignatureHash> ids;
   b->jit_signatures.clear();
   for (size_t o = 0; o < b->ops.size(); ++o) {
     DevOp& h = b->ops[o];
