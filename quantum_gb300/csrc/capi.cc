@@ -431,7 +431,8 @@ void build_lock_schedule(
   // tile passes)
   std::vector<std::vector<TcBlock>> tcb(nr);
   std::vector<std::vector<int32_t>> tcm(nr);
-  std::vector<uint8_t> tc(nr, 0);
+  std::vector<std::vector<TcUnit>> tmpl(nr);  // per block: targets, variant, geometry
+  std::vector<uint8_t> tc(nr, 0), bad(nr, 0);
   parallel_for(nr, [&](size_t k) {
     const int32_t pid = b->rows[size_t(b->lock_rows[k])].program;
     const DevProgram& p = b->programs[size_t(pid)];
@@ -454,12 +455,25 @@ void build_lock_schedule(
                                &tcm[k]) &&
                 !tcb[k].empty();
       }
+      if (tc[k]) {
+        tmpl[k].resize(tcb[k].size());
+        for (size_t q = 0; q < tcb[k].size(); ++q) {
+          TcUnit& u = tmpl[k][q];
+          u = TcUnit{};
+          const int v = tc_unit_geometry(tcb[k][q], p.n, &u.tpack, &u.tr);
+          if (v < 0) bad[k] = 1;
+          if (v > 0) u.tpack |= kTcUnitTrans;
+        }
+      }
     } catch (...) {
       tc[k] = 0;
       tcb[k].clear();
       tcm[k].clear();
+      tmpl[k].clear();
     }
   });
+  for (size_t k = 0; k < nr; ++k)
+    if (bad[k]) throw Error(kInternal, "tensor-core block outside its row's qubits");
   size_t i = 0;
   while (i < nr) {
     tfqg_batch::LockGroup g;
@@ -554,12 +568,11 @@ void build_lock_schedule(
         int64_t total = 0;
         for (size_t k = i; k < j; ++k) {
           if (!tc[k] || q >= tcb[k].size()) continue;
+          if (((tmpl[k][q].tpack & kTcUnitTrans) != 0) != (trans != 0)) continue;
           const int32_t row = b->lock_rows[k];
           const int n = prog(row).n;
-          TcUnit u{};
-          const int v = tc_unit_geometry(tcb[k][q], n, &u.tpack, &u.tr);
-          if (v < 0) throw Error(kInternal, "tensor-core block outside its row's qubits");
-          if (v != trans) continue;
+          TcUnit u = tmpl[k][q];
+          u.tpack &= ~kTcUnitTrans;
           u.off = off[k - i];
           u.row = row;
           u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
@@ -599,10 +612,7 @@ void build_lock_schedule(
           if (!tc[k] || q >= tcb[k].size()) continue;
           const int32_t row = b->lock_rows[k];
           const int n = prog(row).n;
-          TcUnit u{};
-          const int v = tc_unit_geometry(tcb[k][q], n, &u.tpack, &u.tr);
-          if (v < 0) throw Error(kInternal, "tensor-core block outside its row's qubits");
-          if (v) u.tpack |= kTcUnitTrans;
+          TcUnit u = tmpl[k][q];
           u.off = off[k - i];
           u.row = row;
           u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
