@@ -159,3 +159,31 @@ def test_graph_replay_marks_a_timeout(lock_tc):
         g.close()
     assert np.isnan(got[[0, 2]]).all()
     np.testing.assert_array_equal(got[1], ref[1])
+
+
+def test_wide_and_lockstep_rows_in_one_call(lock_tc):
+    """A 24-qubit wide row on tensor-core blocks (one launch per block), two
+    16-qubit lockstep rows on tensor-core blocks and a resident row in the
+    queue, in one expectation call: each path clears and checks the status
+    word, and every row matches complex128."""
+    from oracle import fast128 as F
+    from quantum_gb300 import workloads
+    g = workloads.grid_fsim(4, 6, 12, seed=3)
+    small, _, sp = _batch([16, 9, 16], [4, 4, 4], 16)
+    programs = [g["programs"][0]] + small
+    psums = [g["pauli_sums"][0] * 2] + sp
+    values = np.zeros((4, len(NAMES)), np.float32)
+    values[1:] = np.random.default_rng(5).uniform(-2, 2, size=(3, len(NAMES)))
+    prev = _native.set_tensor_core_gates(2)
+    try:
+        b = ops.Batch(programs, NAMES, psums)
+        assert _native.batch_lock_rows(b._h)[0] == 2
+        got = b.expectation(values)
+        assert _native.tc_blocks(b._h, 0) > 0 and _native.tc_status(b._h) == 0
+        assert _native.batch_lock_tc(b._h)[0] > 0
+    finally:
+        _native.set_tensor_core_gates(prev)
+    want = np.zeros_like(got, dtype=np.float64)
+    want[0] = F.simulate_expectation_row(programs[0], [], np.zeros(0, np.float32), psums[0])
+    want[1:] = O.simulate_expectation(programs[1:], NAMES, values[1:], psums[1:])
+    np.testing.assert_allclose(got, want, atol=expectation_atol(psums), rtol=0)
