@@ -575,7 +575,7 @@ void build_lock_schedule(
           u.tpack &= ~kTcUnitTrans;
           u.off = off[k - i];
           u.row = row;
-          u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
+          u.mat = uint32_t(first_block[k - i] - g.tc_block_begin) + uint32_t(q);
           const int64_t nch = int64_t(1) << (n - kTcBits - 7);
           rows_in.emplace_back(u, nch);
           total += nch;
@@ -615,7 +615,7 @@ void build_lock_schedule(
           TcUnit u = tmpl[k][q];
           u.off = off[k - i];
           u.row = row;
-          u.mat = uint32_t(first_block[k - i]) + uint32_t(q);
+          u.mat = uint32_t(first_block[k - i] - g.tc_block_begin) + uint32_t(q);
           u.slot = slot[k - i];
           u.need = row_units[k - i];
           const int64_t nch = int64_t(1) << (n - kTcBits - 7);
@@ -1466,8 +1466,10 @@ void tcl_prepare(tfqg_batch* b, bool persistent, cudaStream_t s) {
   b->d_tcl_units = reinterpret_cast<const TcUnit*>(base + o.units);
   // persistent form: a queue counter per group, then a count per row
   b->tcl_sync.reserve((b->lock_groups.size() + b->tcl_items.size()) * sizeof(int), b->device);
-  b->tcl_mats.reserve(std::max<size_t>(b->tcl_blocks.size(), 1) * tc_b_floats() * sizeof(float),
-                      b->device);
+  // B operands of one group at a time (groups run one after another)
+  size_t group_blocks = 1;
+  for (const auto& g : b->lock_groups) group_blocks = std::max(group_blocks, size_t(g.tc_block_count));
+  b->tcl_mats.reserve(group_blocks * tc_b_floats() * sizeof(float), b->device);
   b->tc_status.reserve(sizeof(int), b->device);
 }
 
@@ -1541,7 +1543,7 @@ void run_lock(tfqg_batch* b, int mode, const BatchDevice& bd, RunArgs* a, cudaSt
       TFQG_CUDA(launch_tc_fuse_b(bd, a->mats, b->d_tcl_block_rows + g.tc_block_begin,
                                  b->d_tcl_blocks + g.tc_block_begin, b->d_tcl_members,
                                  g.tc_block_count,
-                                 Bops + int64_t(g.tc_block_begin) * int64_t(tc_b_floats()), s));
+                                 Bops, s));
       TFQG_CUDA(launch_lock_zero(tc_state, row_shift, b->d_tcl_items + g.tc_rows.begin,
                                  g.tc_rows.count, g.tc_rows.ntiles, sms * 8, s));
       if (persistent)

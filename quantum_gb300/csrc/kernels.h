@@ -268,10 +268,11 @@ cudaError_t launch_tc_sweep2(float2* psi, int n, const float2* U0, const float2*
 // Lockstep rows on the tensor cores: block k of every row of a lockstep
 // group in one launch.  A unit is a run of consecutive chunks (128 groups of
 // 32 amplitudes each) of one row's state under one block: the state (arena
-// offset `off`, or batch row `row` of the output states), the block's
-// fused matrix (index `mat` into the matrices buffer), its packed targets
-// and, for the transposed variant, its chunk geometry.  Units of one launch
-// all take the same variant.
+// offset `off`, or batch row `row` of the output states), the block's B
+// operands (index `mat` among its group's blocks, whose B operands are
+// built for each group in turn), its packed targets and, for the
+// transposed variant, its chunk geometry.  Units of one launch all take the
+// same variant.
 // In the persistent form (one launch per group, see
 // launch_tc_lock_persistent) a unit also carries the transposed-variant flag
 // (tpack bit 31), its row's slot among the batch's tensor-core rows and the
